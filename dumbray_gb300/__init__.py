@@ -1,0 +1,486 @@
+"""dumbray_gb300 - GB300-native (sm_103a) implementation of DumbRay's rendering hot path.
+
+Python host mirror of the C ABI in ``include/dr_api.h``.  Every call goes through the native
+library ``dumbray_gb300/_build/libdumbray_gb300.so`` (built in-tree by ``dumbray_gb300.build``);
+there is no CPU fallback: if the library is missing, importing the API raises.
+
+Interfaces mirrored from the reference (paths relative to the DumbRay checkout):
+  * ``Scene``        - TriScene = Octree<Renderable<BakedTriFace>> + materials + lights
+                       (__source__/DataStructures/Objects/Scene/Scene.cuh:13-68)
+  * ``cast``         - Octree::cast (.../Raycasters/Octree/Octree.impl.cuh:174-212)
+  * ``BlockRenderer``- DumbRenderer's renderBlocksGPU and its configuration setters
+                       (__source__/DataStructures/Renderers/DumbRenderer/DumbRenderer.cuh:9-64)
+  * frame buffer     - BlockBasedFrameBuffer<8,16> layout helpers (BlockBasedFrameBuffer.impl.cuh:108-156)
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import scenes  # noqa: F401  (input generators)
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "_build" / "libdumbray_gb300.so"
+
+DR_OK, DR_E_ARG, DR_E_CUDA, DR_E_CAPACITY, DR_E_TIMEOUT, DR_E_NOMEM, DR_E_STATE = range(7)
+MAT_DUMB_BASED, MAT_SIMPLE_STOCHASTIC, MAT_LAMBERT, MAT_MIRROR, MAT_GLOSSY = range(5)
+LIGHT_SPHERICAL, LIGHT_SOFT_DIRECTIONAL, LIGHT_DIRECTIONAL = range(3)
+LENS_DEFAULT_PERSPECTIVE, LENS_SIMPLE_STOCHASTIC, LENS_SPHERICAL_SEGMENT, LENS_PINHOLE, LENS_FISHEYE, LENS_SPHERICAL = range(6)
+MODE_REFERENCE, MODE_PHYSICAL = 0, 1
+BOXING_HEIGHT, BOXING_WIDTH, BOXING_MIN, BOXING_MAX = range(4)
+BLOCK_W, BLOCK_H = 8, 16
+BLOCK_SIZE = BLOCK_W * BLOCK_H
+
+_F3 = ctypes.c_float * 3
+
+
+class DrBuildParams(ctypes.Structure):
+    _fields_ = [("max_depth", ctypes.c_int32), ("split_threshold", ctypes.c_int32), ("threads", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class DrMaterial(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("color", _F3), ("fresnel", _F3), ("specular", ctypes.c_float),
+                ("metal", ctypes.c_float), ("diffuse", ctypes.c_float), ("smoothness", ctypes.c_float),
+                ("shininess", ctypes.c_float), ("roughness", ctypes.c_float), ("emission", _F3)]
+
+
+class DrLight(ctypes.Structure):
+    _fields_ = [("type", ctypes.c_int32), ("color", _F3), ("position", _F3), ("direction", _F3),
+                ("radius", ctypes.c_float), ("distance", ctypes.c_float), ("softness", ctypes.c_float)]
+
+
+class DrCamera(ctypes.Structure):
+    _fields_ = [("lens", ctypes.c_int32), ("angle", ctypes.c_float * 2), ("focal_distance", ctypes.c_float),
+                ("softness", ctypes.c_float), ("filter", _F3), ("position", _F3), ("right", _F3), ("up", _F3),
+                ("forward", _F3)]
+
+
+class DrRenderParams(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("width", ctypes.c_int32), ("height", ctypes.c_int32),
+                ("samples_x", ctypes.c_int32), ("samples_y", ctypes.c_int32), ("max_bounces", ctypes.c_int32),
+                ("cull_backfaces", ctypes.c_int32), ("boxing", ctypes.c_int32), ("iteration", ctypes.c_int32),
+                ("seed", ctypes.c_uint32)]
+
+
+class DumbRayError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"dumbray_gb300 status {status}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The native library (loaded once).  Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"native library {LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'` "
+                           "(or python -m dumbray_gb300.build); there is no CPU fallback")
+    L = ctypes.CDLL(str(LIB_PATH))
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+    P = ctypes.POINTER
+    L.dr_last_error.restype = ctypes.c_char_p
+    L.dr_version.restype = i32
+    L.dr_block_count.restype = i32
+    L.dr_block_count.argtypes = [i32, i32]
+    L.dr_scene_create.restype = i32
+    L.dr_scene_create.argtypes = [vp, vp, vp, i32, vp, i32, vp, i32, vp, P(vp)]
+    L.dr_scene_set_triangle_params.restype = i32
+    L.dr_scene_set_triangle_params.argtypes = [vp, vp, vp, vp]
+    L.dr_scene_triangle_params_device.restype = i32
+    L.dr_scene_triangle_params_device.argtypes = [vp, P(vp), P(vp)]
+    L.dr_scene_stats.restype = i32
+    L.dr_scene_stats.argtypes = [vp, P(i64), P(i64), P(i64), P(i32)]
+    L.dr_scene_export_tree.restype = i32
+    L.dr_scene_export_tree.argtypes = [vp, vp, vp, vp, vp]
+    L.dr_scene_destroy.restype = None
+    L.dr_scene_destroy.argtypes = [vp]
+    L.dr_octree_create_host.restype = i32
+    L.dr_octree_create_host.argtypes = [vp, i32, vp, P(vp)]
+    L.dr_octree_stats.restype = i32
+    L.dr_octree_stats.argtypes = [vp, P(i64), P(i64), P(i64), P(i32)]
+    L.dr_octree_export.restype = i32
+    L.dr_octree_export.argtypes = [vp, vp, vp, vp, vp]
+    L.dr_octree_destroy.restype = None
+    L.dr_octree_destroy.argtypes = [vp]
+    L.dr_cast.restype = i32
+    L.dr_cast.argtypes = [vp, vp, vp, vp, i32, i32, vp, vp, vp]
+    L.dr_cast_counted.restype = i32
+    L.dr_cast_counted.argtypes = [vp, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp]
+    L.dr_renderer_create.restype = i32
+    L.dr_renderer_create.argtypes = [i32, P(vp)]
+    L.dr_renderer_destroy.restype = None
+    L.dr_renderer_destroy.argtypes = [vp]
+    L.dr_renderer_launch_count.restype = i64
+    L.dr_renderer_launch_count.argtypes = [vp]
+    L.dr_render_blocks.restype = i32
+    L.dr_render_blocks.argtypes = [vp, vp, vp, vp, i32, i32, vp, vp]
+    _lib = L
+    return L
+
+
+def check(status: int) -> None:
+    if status != DR_OK:
+        raise DumbRayError(status, lib().dr_last_error().decode(errors="replace"))
+
+
+def block_count(width: int, height: int) -> int:
+    return ((width + BLOCK_W - 1) // BLOCK_W) * ((height + BLOCK_H - 1) // BLOCK_H)
+
+
+# ---- material / light / camera constructors ------------------------------------------------------
+
+def dumb_based(fresnel=(0.2, 0.2, 0.2), specular=8.0, diffuse=(0.2, 0.2, 0.2), metal=0.5) -> DrMaterial:
+    """DumbBasedShader(fresnel, specular, diffuse, metal) (DumbBasedShader.impl.cuh:5-16)."""
+    m = DrMaterial()
+    m.type = MAT_DUMB_BASED
+    m.fresnel[:] = fresnel
+    m.specular = specular
+    m.color[:] = diffuse
+    m.metal = metal
+    return m
+
+
+def simple_stochastic(color=(1.0, 1.0, 1.0), diffuse=0.05, smoothness=0.95, shininess=2.0) -> DrMaterial:
+    """SimpleStochasticShader(color, diffuse, smoothness, shininess) (SimpleStochasticShader.impl.cuh:4-11)."""
+    m = DrMaterial()
+    m.type = MAT_SIMPLE_STOCHASTIC
+    m.color[:] = color
+    m.diffuse = diffuse
+    m.smoothness = smoothness
+    m.shininess = shininess
+    return m
+
+
+def lambert(albedo=(0.7, 0.7, 0.7), emission=(0.0, 0.0, 0.0)) -> DrMaterial:
+    m = DrMaterial()
+    m.type = MAT_LAMBERT
+    m.color[:] = albedo
+    m.emission[:] = emission
+    return m
+
+
+def mirror(reflectance=(0.9, 0.9, 0.9)) -> DrMaterial:
+    m = DrMaterial()
+    m.type = MAT_MIRROR
+    m.color[:] = reflectance
+    return m
+
+
+def glossy(albedo=(0.8, 0.8, 0.8), roughness=0.2) -> DrMaterial:
+    m = DrMaterial()
+    m.type = MAT_GLOSSY
+    m.color[:] = albedo
+    m.roughness = roughness
+    return m
+
+
+def spherical_light(color, position, radius) -> DrLight:
+    """SphericalLightEmitter(color, position, radius)."""
+    l = DrLight()
+    l.type = LIGHT_SPHERICAL
+    l.color[:] = color
+    l.position[:] = position
+    l.radius = radius
+    return l
+
+
+def soft_directional_light(color, direction, distance, softness) -> DrLight:
+    """SimpleSoftDirectionalLight(color, direction, distance, softness)."""
+    l = DrLight()
+    l.type = LIGHT_SOFT_DIRECTIONAL
+    l.color[:] = color
+    l.direction[:] = direction
+    l.distance = distance
+    l.softness = softness
+    return l
+
+
+def directional_light(color, direction, distance) -> DrLight:
+    """SimpleDirectionalLight(color, direction, distance)."""
+    l = DrLight()
+    l.type = LIGHT_DIRECTIONAL
+    l.color[:] = color
+    l.direction[:] = direction
+    l.distance = distance
+    return l
+
+
+def camera(lens: int, position=(0.0, 0.0, 0.0), target=None, angle=(60.0, 60.0), focal_distance=128.0, softness=1.0,
+           filter=(1.0, 1.0, 1.0), basis=None) -> DrCamera:
+    """Camera = lens + transform.  ``basis`` = (right, up, forward) or derived from ``target``; the
+    default is the identity orientation (+z forward), i.e. a reference Transform with zero Euler angles."""
+    c = DrCamera()
+    c.lens = lens
+    c.angle[:] = angle if hasattr(angle, "__len__") else (angle, angle)
+    c.focal_distance = focal_distance
+    c.softness = softness
+    c.filter[:] = filter
+    c.position[:] = position
+    if basis is None and target is not None:
+        _, r, u, f = scenes.camera_basis(position, target)
+        basis = (r, u, f)
+    if basis is None:
+        basis = ((1.0, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 1.0))
+    c.right[:] = [float(v) for v in basis[0]]
+    c.up[:] = [float(v) for v in basis[1]]
+    c.forward[:] = [float(v) for v in basis[2]]
+    return c
+
+
+def render_params(width, height, mode=MODE_REFERENCE, samples=(1, 1), max_bounces=2, cull_backfaces=True,
+                  boxing=BOXING_HEIGHT, iteration=1, seed=0) -> DrRenderParams:
+    p = DrRenderParams()
+    p.mode, p.width, p.height = mode, width, height
+    p.samples_x, p.samples_y = samples
+    p.max_bounces = max_bounces
+    p.cull_backfaces = 1 if cull_backfaces else 0
+    p.boxing = boxing
+    p.iteration = iteration
+    p.seed = seed & 0xFFFFFFFF
+    return p
+
+
+def _ptr(t) -> int:
+    """Device pointer of a CUDA torch tensor (contiguous), or 0 for None."""
+    if t is None:
+        return 0
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("expected a contiguous CUDA tensor")
+    return t.data_ptr()
+
+
+def _stream_ptr(stream) -> int:
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    return getattr(stream, "cuda_stream", stream)
+
+
+class Scene:
+    """Triangles + materials + lights, octree built on the host and uploaded once (immutable)."""
+
+    def __init__(self, tris, normals=None, mat_id=None, materials=(), lights=(), max_depth=0, split_threshold=0,
+                 threads=0):
+        L = lib()
+        self.tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 3, 3)
+        self.n = len(self.tris)
+        self._nrm = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3, 3)
+        self._mat = None if mat_id is None else np.ascontiguousarray(mat_id, dtype=np.int32)
+        mats = list(materials)
+        lts = list(lights)
+        self.materials, self.lights = mats, lts
+        marr = (DrMaterial * max(1, len(mats)))(*mats)
+        larr = (DrLight * max(1, len(lts)))(*lts)
+        bp = DrBuildParams(max_depth, split_threshold, threads, 0)
+        h = ctypes.c_void_p()
+        check(L.dr_scene_create(self.tris.ctypes.data, None if self._nrm is None else self._nrm.ctypes.data,
+                                None if self._mat is None else self._mat.ctypes.data, self.n,
+                                ctypes.addressof(marr) if mats else None, len(mats),
+                                ctypes.addressof(larr) if lts else None, len(lts), ctypes.byref(bp), ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise RuntimeError("scene destroyed")
+        return self._h
+
+    def stats(self):
+        L = lib()
+        nodes, leaves, refs = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        depth = ctypes.c_int32()
+        check(L.dr_scene_stats(self.handle, ctypes.byref(nodes), ctypes.byref(leaves), ctypes.byref(refs), ctypes.byref(depth)))
+        return dict(nodes=nodes.value, leaves=leaves.value, refs=refs.value, depth=depth.value)
+
+    def export_tree(self):
+        s = self.stats()
+        box = np.zeros((s["nodes"], 6), np.float32)
+        child = np.zeros(s["nodes"], np.int32)
+        leaf = np.zeros((s["nodes"], 2), np.int32)
+        refs = np.zeros(max(1, s["refs"]), np.int32)
+        check(lib().dr_scene_export_tree(self.handle, box.ctypes.data, child.ctypes.data, leaf.ctypes.data, refs.ctypes.data))
+        return box, child, leaf, refs[: s["refs"]]
+
+    def set_triangle_params(self, albedo=None, emission=None, roughness=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float32) for a in (albedo, emission, roughness)]
+        check(lib().dr_scene_set_triangle_params(self.handle, *[None if a is None else a.ctypes.data for a in arrs]))
+
+    def close(self):
+        if self._h is not None:
+            lib().dr_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def build_octree_host(tris, max_depth=0, split_threshold=0, threads=0):
+    """Host-only octree build (dr_octree_create_host); returns (stats, box, child, leaf, refs) with
+    node 0 = root, as dr_scene_export_tree."""
+    L = lib()
+    t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 3, 3)
+    bp = DrBuildParams(max_depth, split_threshold, threads, 0)
+    h = ctypes.c_void_p()
+    check(L.dr_octree_create_host(t.ctypes.data, len(t), ctypes.byref(bp), ctypes.byref(h)))
+    try:
+        nodes, leaves, refs = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        depth = ctypes.c_int32()
+        check(L.dr_octree_stats(h, ctypes.byref(nodes), ctypes.byref(leaves), ctypes.byref(refs), ctypes.byref(depth)))
+        box = np.zeros((nodes.value, 6), np.float32)
+        child = np.zeros(nodes.value, np.int32)
+        leaf = np.zeros((nodes.value, 2), np.int32)
+        ref = np.zeros(max(1, refs.value), np.int32)
+        check(L.dr_octree_export(h, box.ctypes.data, child.ctypes.data, leaf.ctypes.data, ref.ctypes.data))
+        stats = dict(nodes=nodes.value, leaves=leaves.value, refs=refs.value, depth=depth.value)
+        return stats, box, child, leaf, ref[: refs.value]
+    finally:
+        L.dr_octree_destroy(h)
+
+
+def canonical_tree(box, child, leaf, refs):
+    """Depth-first (child order) dump of an exported tree: (boxes [k,6], counts [k] (-1 = inner),
+    concatenated leaf triangle ids), comparable across builders regardless of node numbering."""
+    out_box, out_cnt, out_tri = [], [], []
+    stack = [0]
+    while stack:
+        i = stack.pop()
+        out_box.append(box[i])
+        if child[i] < 0:
+            f, c = leaf[i]
+            out_cnt.append(c)
+            out_tri.append(refs[f:f + c])
+        else:
+            out_cnt.append(-1)
+            stack.extend(range(child[i] + 7, child[i] - 1, -1))
+    tri = np.concatenate(out_tri) if out_tri else np.zeros(0, np.int32)
+    return np.asarray(out_box, np.float32), np.asarray(out_cnt, np.int32), tri.astype(np.int32)
+
+
+def cast(scene: Scene, origins, directions, ignore=None, cull_backfaces=True, counted=False, stream=None):
+    """Closest-hit casts through dr_cast for CUDA tensors origins/directions [n,3] float32.
+    Returns (hit_tri int32 [n], hit_t float32 [n]) (+ (box_tests, tri_tests) when counted)."""
+    import torch
+    n = origins.shape[0]
+    dev = origins.device
+    tri = torch.empty(n, dtype=torch.int32, device=dev)
+    t = torch.empty(n, dtype=torch.float32, device=dev)
+    sp = _stream_ptr(stream)
+    if counted:
+        nb = torch.empty(n, dtype=torch.int32, device=dev)
+        nt = torch.empty(n, dtype=torch.int32, device=dev)
+        check(lib().dr_cast_counted(scene.handle, _ptr(origins), _ptr(directions), _ptr(ignore), n, 1 if cull_backfaces else 0,
+                                    _ptr(tri), _ptr(t), _ptr(nb), _ptr(nt), sp))
+        return tri, t, nb, nt
+    check(lib().dr_cast(scene.handle, _ptr(origins), _ptr(directions), _ptr(ignore), n, 1 if cull_backfaces else 0,
+                        _ptr(tri), _ptr(t), sp))
+    return tri, t
+
+
+class Renderer:
+    """Owns the wavefront scratch of one caller (dr_renderer)."""
+
+    def __init__(self, wave_paths: int = 0):
+        h = ctypes.c_void_p()
+        check(lib().dr_renderer_create(int(wave_paths), ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def launches(self) -> int:
+        return int(lib().dr_renderer_launch_count(self._h))
+
+    def render_blocks(self, scene: Scene, cam: DrCamera, fb, start_block: int, end_block: int, params: DrRenderParams,
+                      stream=None):
+        """dr_render_blocks into ``fb`` (CUDA float32 tensor [blocks*128, 4], block-major)."""
+        check(lib().dr_render_blocks(self._h, scene.handle, ctypes.byref(cam), _ptr(fb), int(start_block), int(end_block),
+                                     ctypes.byref(params), _stream_ptr(stream)))
+
+    def close(self):
+        if self._h is not None:
+            lib().dr_renderer_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BlockRenderer:
+    """Host mirror of DumbRenderer's block-renderer interface (DumbRenderer.cuh:9-64): the same
+    configuration setters and a ``render_blocks_gpu`` that renders a block range of a device frame
+    buffer with the progressive blend of iteration ``iteration`` (DumbRenderer.cu:87-113)."""
+
+    def __init__(self, scene: Scene, camera: DrCamera, width: int, height: int, mode=MODE_REFERENCE, boxing=BOXING_HEIGHT,
+                 max_bounces=2, samples_per_pixel=(1, 1), ignore_backfaces=True, seed=0, wave_paths=0):
+        self.scene, self.camera = scene, camera
+        self.width, self.height, self.mode, self.seed = width, height, mode, seed
+        self.set_boxing_mode(boxing)
+        self.set_max_bounces(max_bounces)
+        self.set_samples_per_pixel(*samples_per_pixel)
+        self.set_ignore_backfaces(ignore_backfaces)
+        self._renderer = Renderer(wave_paths)
+
+    # configuration (DumbRenderer.cu:26-50)
+    def set_boxing_mode(self, mode):
+        self.boxing = int(mode)
+
+    def set_max_bounces(self, n):
+        self.max_bounces = min(int(n), 64)
+
+    def set_samples_per_pixel(self, x, y):
+        self.samples_x, self.samples_y = max(1, int(x)), max(1, int(y))
+
+    def set_ignore_backfaces(self, ignore):
+        self.ignore_backfaces = bool(ignore)
+
+    def block_count(self) -> int:
+        return block_count(self.width, self.height)
+
+    def params(self, iteration: int) -> DrRenderParams:
+        return render_params(self.width, self.height, self.mode, (self.samples_x, self.samples_y), self.max_bounces,
+                             self.ignore_backfaces, self.boxing, iteration, self.seed)
+
+    def render_blocks_gpu(self, device_fb, start_block: int, end_block: int, iteration: int = 1, stream=None) -> bool:
+        self._renderer.render_blocks(self.scene, self.camera, device_fb, start_block, end_block, self.params(iteration), stream)
+        return True
+
+    def launches(self) -> int:
+        return self._renderer.launches()
+
+
+def new_frame_buffer(width: int, height: int, device="cuda"):
+    import torch
+    return torch.zeros((block_count(width, height) * BLOCK_SIZE, 4), dtype=torch.float32, device=device)
+
+
+def blockmajor_to_image(fb, width: int, height: int) -> np.ndarray:
+    """Block-major float4 frame buffer -> row-major [H, W, 4] numpy image."""
+    a = fb.detach().cpu().numpy() if hasattr(fb, "detach") else np.asarray(fb)
+    bw = (width + BLOCK_W - 1) // BLOCK_W
+    bh = (height + BLOCK_H - 1) // BLOCK_H
+    a = a.reshape(bh, bw, BLOCK_H, BLOCK_W, 4).transpose(0, 2, 1, 3, 4).reshape(bh * BLOCK_H, bw * BLOCK_W, 4)
+    return np.ascontiguousarray(a[:height, :width])
+
+
+def image_to_blockmajor(img: np.ndarray) -> np.ndarray:
+    h, w = img.shape[:2]
+    bw = (w + BLOCK_W - 1) // BLOCK_W
+    bh = (h + BLOCK_H - 1) // BLOCK_H
+    pad = np.zeros((bh * BLOCK_H, bw * BLOCK_W, img.shape[2]), img.dtype)
+    pad[:h, :w] = img
+    return np.ascontiguousarray(pad.reshape(bh, BLOCK_H, bw, BLOCK_W, -1).transpose(0, 2, 1, 3, 4).reshape(-1, img.shape[2]))

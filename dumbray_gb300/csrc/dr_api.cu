@@ -1,0 +1,558 @@
+// dr_api.cu - C ABI of the GB300 DumbRay hot path (host side; see include/dr_api.h).
+//
+// Scene objects are immutable after creation and hold the uploaded octree, triangles and
+// materials.  Renderer objects own the wavefront scratch (queues, accumulators) for one caller
+// thread / stream at a time.  Every entry point validates its arguments, returns a dr_status and
+// records a message for dr_last_error(); none falls back to the CPU.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/dr_api.h"
+#include "dr_kernels.h"
+#include "octree_build.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+dr_status fail(dr_status s, const std::string &msg) {
+    g_err = msg;
+    return s;
+}
+dr_status cuda_fail(cudaError_t e, const char *where) {
+    g_err = std::string(where) + ": " + cudaGetErrorString(e);
+    return DR_E_CUDA;
+}
+
+template <class T>
+cudaError_t upload(T **dst, const T *src, size_t count) {
+    *dst = nullptr;
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc((void **)dst, sizeof(T) * count);
+    if (e != cudaSuccess) return e;
+    return cudaMemcpy(*dst, src, sizeof(T) * count, cudaMemcpyHostToDevice);
+}
+
+// normalised Triangle::normal() = (c - a) x (b - a) (flat shading default)
+void flat_normal(const float *p, float out[3]) {
+    float ax = p[0], ay = p[1], az = p[2];
+    float cax = p[6] - ax, cay = p[7] - ay, caz = p[8] - az;
+    float bax = p[3] - ax, bay = p[4] - ay, baz = p[5] - az;
+    float x = cay * baz - bay * caz;
+    float y = bax * caz - cax * baz;
+    float z = cax * bay - bax * cay;
+    float im = 1.0f / std::sqrt(x * x + y * y + z * z);
+    out[0] = x * im;
+    out[1] = y * im;
+    out[2] = z * im;
+}
+
+}  // namespace
+
+struct dr_scene {
+    drd::Scene dev{};
+    std::vector<void *> allocs;
+    drb::FlatOctree tree;
+    int64_t n = 0;
+    std::vector<float> xyz;              // host copy of the triangles
+    std::vector<int32_t> mat_id;
+    std::vector<dr_material> mats;
+    std::vector<float> albedo, emission, roughness;
+    float4 *shade = nullptr;
+    int *emissive = nullptr;
+    float *emissive_cdf = nullptr;
+    float *albedo_dev = nullptr;         // views for dr_scene_triangle_params_device
+    float *emission_dev = nullptr;
+
+    ~dr_scene() {
+        for (void *p : allocs) cudaFree(p);
+        cudaFree(shade);
+        cudaFree(emissive);
+        cudaFree(emissive_cdf);
+        cudaFree(albedo_dev);
+        cudaFree(emission_dev);
+    }
+};
+
+struct dr_octree {
+    drb::FlatOctree tree;
+};
+
+struct dr_renderer {
+    int capacity = 0;
+    float4 *q[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    int4 *q3[2] = {nullptr, nullptr};
+    float2 *hits = nullptr;
+    float4 *s[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int shadow_capacity = 0;
+    float *accum = nullptr;
+    size_t accum_slots = 0;
+    void *ctrl = nullptr;
+    long long launches = 0;
+
+    ~dr_renderer() {
+        for (int k = 0; k < 2; k++) {
+            for (int j = 0; j < 3; j++) cudaFree(q[k][j]);
+            cudaFree(q3[k]);
+        }
+        cudaFree(hits);
+        for (auto *p : s) cudaFree(p);
+        cudaFree(accum);
+        cudaFree(ctrl);
+    }
+};
+
+namespace {
+
+// Per-triangle shading records and the emissive-triangle sampling table (physical mode).
+dr_status upload_shading(dr_scene *sc) {
+    const int64_t n = sc->n;
+    std::vector<float4> shade(2 * n);
+    std::vector<int> em;
+    std::vector<float> cdf;
+    double total = 0.0;
+    for (int64_t i = 0; i < n; i++) {
+        int type = sc->mats.empty() ? DR_MAT_LAMBERT : sc->mats[sc->mat_id[i]].type;
+        shade[2 * i] = make_float4(sc->albedo[3 * i], sc->albedo[3 * i + 1], sc->albedo[3 * i + 2], sc->roughness[i]);
+        float4 e;
+        e.x = sc->emission[3 * i];
+        e.y = sc->emission[3 * i + 1];
+        e.z = sc->emission[3 * i + 2];
+        int bits = type;
+        std::memcpy(&e.w, &bits, 4);
+        shade[2 * i + 1] = e;
+        float esum = e.x + e.y + e.z;
+        if (esum > 0.0f) {
+            const float *p = &sc->xyz[9 * i];
+            double ux = p[3] - p[0], uy = p[4] - p[1], uz = p[5] - p[2];
+            double vx = p[6] - p[0], vy = p[7] - p[1], vz = p[8] - p[2];
+            double cx = uy * vz - uz * vy, cy = uz * vx - ux * vz, cz = ux * vy - uy * vx;
+            double area = 0.5 * std::sqrt(cx * cx + cy * cy + cz * cz);
+            total += (double)esum * area;
+            em.push_back((int)i);
+            cdf.push_back((float)total);
+        }
+    }
+    cudaFree(sc->shade);
+    cudaFree(sc->emissive);
+    cudaFree(sc->emissive_cdf);
+    cudaFree(sc->albedo_dev);
+    cudaFree(sc->emission_dev);
+    sc->shade = nullptr;
+    sc->emissive = nullptr;
+    sc->emissive_cdf = nullptr;
+    sc->albedo_dev = nullptr;
+    sc->emission_dev = nullptr;
+    cudaError_t e = upload(&sc->shade, shade.data(), shade.size());
+    if (e == cudaSuccess) e = upload(&sc->emissive, em.data(), em.size());
+    if (e == cudaSuccess) e = upload(&sc->emissive_cdf, cdf.data(), cdf.size());
+    if (e == cudaSuccess) e = upload(&sc->albedo_dev, sc->albedo.data(), sc->albedo.size());
+    if (e == cudaSuccess) e = upload(&sc->emission_dev, sc->emission.data(), sc->emission.size());
+    if (e != cudaSuccess) return cuda_fail(e, "upload shading");
+    sc->dev.shade = sc->shade;
+    sc->dev.emissive = sc->emissive;
+    sc->dev.emissive_cdf = sc->emissive_cdf;
+    sc->dev.n_emissive = (int)em.size();
+    sc->dev.emissive_total = (float)total;
+    return DR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *dr_last_error(void) { return g_err.c_str(); }
+
+int32_t dr_version(void) { return 100; }
+
+int32_t dr_block_count(int32_t width, int32_t height) {
+    if (width <= 0 || height <= 0) return 0;
+    return ((width + DR_BLOCK_W - 1) / DR_BLOCK_W) * ((height + DR_BLOCK_H - 1) / DR_BLOCK_H);
+}
+
+dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat_id, int32_t n, const dr_material *mats,
+                          int32_t n_mats, const dr_light *lights, int32_t n_lights, const dr_build_params *bp, dr_scene **out) {
+    if (out == nullptr) return fail(DR_E_ARG, "dr_scene_create: out is NULL");
+    *out = nullptr;
+    if (n < 0 || (n > 0 && xyz == nullptr)) return fail(DR_E_ARG, "dr_scene_create: bad triangle array");
+    if (n_mats < 0 || (n_mats > 0 && mats == nullptr)) return fail(DR_E_ARG, "dr_scene_create: bad material array");
+    if (n_lights < 0 || (n_lights > 0 && lights == nullptr)) return fail(DR_E_ARG, "dr_scene_create: bad light array");
+    if (n_lights > 16) return fail(DR_E_ARG, "dr_scene_create: at most 16 lights");
+    for (int32_t i = 0; mat_id && i < n; i++)
+        if (mat_id[i] < 0 || (n_mats > 0 && mat_id[i] >= n_mats) || (n_mats == 0 && mat_id[i] != 0))
+            return fail(DR_E_ARG, "dr_scene_create: material id out of range at triangle " + std::to_string(i));
+    for (int32_t i = 0; i < n_mats; i++)
+        if (mats[i].type < 0 || mats[i].type > DR_MAT_GLOSSY) return fail(DR_E_ARG, "dr_scene_create: bad material type");
+    for (int32_t i = 0; i < n_lights; i++)
+        if (lights[i].type < 0 || lights[i].type > DR_LIGHT_DIRECTIONAL) return fail(DR_E_ARG, "dr_scene_create: bad light type");
+
+    dr_scene *sc = new (std::nothrow) dr_scene();
+    if (!sc) return fail(DR_E_NOMEM, "dr_scene_create: out of host memory");
+    sc->n = n;
+    sc->xyz.assign(xyz, xyz + 9 * (size_t)n);
+    sc->mat_id.assign((size_t)n, 0);
+    if (mat_id) std::copy(mat_id, mat_id + n, sc->mat_id.begin());
+    sc->mats.assign(mats, mats + n_mats);
+
+    drb::BuildOptions opt;
+    if (bp) {
+        if (bp->max_depth > 0) opt.max_depth = std::min(bp->max_depth, drd::kMaxDepth);
+        if (bp->split_threshold > 0) opt.split_threshold = bp->split_threshold;
+        opt.threads = bp->threads;
+    }
+    if (!drb::build_octree(sc->xyz.data(), n, opt, sc->tree)) {
+        delete sc;
+        return fail(DR_E_ARG, "dr_scene_create: octree build failed");
+    }
+    const drb::FlatOctree &T = sc->tree;
+    if (T.node_count >= (int64_t(1) << 24)) {
+        delete sc;
+        return fail(DR_E_CAPACITY, "dr_scene_create: octree exceeds 2^24 nodes");
+    }
+    // pack nodes: {lo, first child | ~first ref}, {hi, ref count}
+    std::vector<float4> nodes(2 * (size_t)T.node_count);
+    for (int64_t i = 0; i < T.node_count; i++) {
+        int w = T.node_child[i] >= 0 ? T.node_child[i] : ~(int)T.node_leaf_first[i];
+        int c = T.node_child[i] >= 0 ? 0 : T.node_leaf_count[i];
+        float wf, cf;
+        std::memcpy(&wf, &w, 4);
+        std::memcpy(&cf, &c, 4);
+        nodes[2 * i] = make_float4(T.node_lo[3 * i], T.node_lo[3 * i + 1], T.node_lo[3 * i + 2], wf);
+        nodes[2 * i + 1] = make_float4(T.node_hi[3 * i], T.node_hi[3 * i + 1], T.node_hi[3 * i + 2], cf);
+    }
+    std::vector<float4> leaf_tris(3 * T.leaf_refs.size());
+    for (size_t r = 0; r < T.leaf_refs.size(); r++) {
+        int id = T.leaf_refs[r];
+        const float *p = &sc->xyz[9 * (size_t)id];
+        float idf;
+        std::memcpy(&idf, &id, 4);
+        leaf_tris[3 * r] = make_float4(p[0], p[1], p[2], idf);
+        leaf_tris[3 * r + 1] = make_float4(p[3], p[4], p[5], 0.0f);
+        leaf_tris[3 * r + 2] = make_float4(p[6], p[7], p[8], 0.0f);
+    }
+    std::vector<float4> tris(3 * (size_t)n), nrms(3 * (size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        const float *p = &sc->xyz[9 * i];
+        for (int k = 0; k < 3; k++) tris[3 * i + k] = make_float4(p[3 * k], p[3 * k + 1], p[3 * k + 2], 0.0f);
+        if (nrm) {
+            const float *q = nrm + 9 * i;
+            for (int k = 0; k < 3; k++) nrms[3 * i + k] = make_float4(q[3 * k], q[3 * k + 1], q[3 * k + 2], 0.0f);
+        } else {
+            float fn[3];
+            flat_normal(p, fn);
+            for (int k = 0; k < 3; k++) nrms[3 * i + k] = make_float4(fn[0], fn[1], fn[2], 0.0f);
+        }
+    }
+    std::vector<drd::Material> dm(std::max(n_mats, 1));
+    std::memset(dm.data(), 0, sizeof(drd::Material) * dm.size());
+    for (int32_t i = 0; i < n_mats; i++) {
+        const dr_material &m = mats[i];
+        drd::Material &d = dm[i];
+        d.type = m.type;
+        for (int k = 0; k < 3; k++) { d.color[k] = m.color[k]; d.fresnel[k] = m.fresnel[k]; d.emission[k] = m.emission[k]; }
+        d.specular = m.specular;
+        d.metal = m.metal;
+        d.diffuse = m.diffuse;
+        d.smoothness = m.smoothness;
+        d.shininess = m.shininess;
+        d.roughness = m.roughness;
+    }
+    if (n_mats == 0) dm[0].type = DR_MAT_LAMBERT;
+    std::vector<drd::Light> dl(std::max(n_lights, 1));
+    std::memset(dl.data(), 0, sizeof(drd::Light) * dl.size());
+    for (int32_t i = 0; i < n_lights; i++) {
+        const dr_light &l = lights[i];
+        drd::Light &d = dl[i];
+        d.type = l.type;
+        for (int k = 0; k < 3; k++) { d.color[k] = l.color[k]; d.position[k] = l.position[k]; d.direction[k] = l.direction[k]; }
+        d.radius = l.radius;
+        d.distance = l.distance;
+        d.softness = l.softness;
+    }
+
+    float4 *d_nodes = nullptr, *d_leaf = nullptr, *d_tris = nullptr, *d_nrms = nullptr;
+    int *d_mat = nullptr;
+    drd::Material *d_mats = nullptr;
+    drd::Light *d_lights = nullptr;
+    cudaError_t e = upload(&d_nodes, nodes.data(), nodes.size());
+    if (e == cudaSuccess) { sc->allocs.push_back(d_nodes); e = upload(&d_leaf, leaf_tris.data(), leaf_tris.size()); }
+    if (e == cudaSuccess) { sc->allocs.push_back(d_leaf); e = upload(&d_tris, tris.data(), tris.size()); }
+    if (e == cudaSuccess) { sc->allocs.push_back(d_tris); e = upload(&d_nrms, nrms.data(), nrms.size()); }
+    if (e == cudaSuccess) { sc->allocs.push_back(d_nrms); e = upload(&d_mat, sc->mat_id.data(), sc->mat_id.size()); }
+    if (e == cudaSuccess) { sc->allocs.push_back(d_mat); e = upload(&d_mats, dm.data(), dm.size()); }
+    if (e == cudaSuccess) { sc->allocs.push_back(d_mats); e = upload(&d_lights, dl.data(), dl.size()); }
+    if (e == cudaSuccess) sc->allocs.push_back(d_lights);
+    if (e != cudaSuccess) {
+        delete sc;
+        return cuda_fail(e, "dr_scene_create: upload");
+    }
+    drd::Scene &S = sc->dev;
+    S.nodes = d_nodes;
+    S.leaf_tris = d_leaf;
+    S.tris = d_tris;
+    S.nrms = d_nrms;
+    S.mat_id = d_mat;
+    S.mats = d_mats;
+    S.lights = d_lights;
+    for (int k = 0; k < 3; k++) { S.root_lo[k] = T.root_lo[k]; S.root_hi[k] = T.root_hi[k]; }
+    S.root_child = T.root_child >= 0 ? 0 : -1;
+    S.root_leaf_first = (int)T.root_leaf_first;
+    S.root_leaf_count = T.root_leaf_count;
+    S.n_tris = n;
+    S.n_mats = std::max(n_mats, 1);
+    S.n_lights = n_lights;
+    if (n == 0) { S.root_child = -1; S.root_leaf_count = 0; }
+
+    sc->albedo.resize(3 * (size_t)n);
+    sc->emission.resize(3 * (size_t)n);
+    sc->roughness.resize((size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        const drd::Material &m = dm[sc->mat_id[i]];
+        for (int k = 0; k < 3; k++) { sc->albedo[3 * i + k] = m.color[k]; sc->emission[3 * i + k] = m.emission[k]; }
+        sc->roughness[i] = m.roughness;
+    }
+    dr_status st = upload_shading(sc);
+    if (st != DR_OK) { delete sc; return st; }
+    *out = sc;
+    return DR_OK;
+}
+
+dr_status dr_scene_set_triangle_params(dr_scene *sc, const float *albedo, const float *emission, const float *roughness) {
+    if (!sc) return fail(DR_E_ARG, "dr_scene_set_triangle_params: scene is NULL");
+    size_t n = (size_t)sc->n;
+    if (albedo) std::copy(albedo, albedo + 3 * n, sc->albedo.begin());
+    if (emission) std::copy(emission, emission + 3 * n, sc->emission.begin());
+    if (roughness) std::copy(roughness, roughness + n, sc->roughness.begin());
+    return upload_shading(sc);
+}
+
+dr_status dr_scene_triangle_params_device(dr_scene *sc, float **albedo, float **emission) {
+    if (!sc) return fail(DR_E_ARG, "dr_scene_triangle_params_device: scene is NULL");
+    if (albedo) *albedo = sc->albedo_dev;
+    if (emission) *emission = sc->emission_dev;
+    return DR_OK;
+}
+
+static void tree_stats(const drb::FlatOctree &T, int64_t *nodes, int64_t *leaves, int64_t *refs, int32_t *depth) {
+    int64_t nl = (T.root_child < 0) ? 1 : 0;
+    for (int64_t i = 0; i < T.node_count; i++) nl += (T.node_child[i] < 0) ? 1 : 0;
+    if (nodes) *nodes = T.node_count + 1;
+    if (leaves) *leaves = nl;
+    if (refs) *refs = (int64_t)T.leaf_refs.size();
+    if (depth) *depth = T.depth;
+}
+
+static void tree_export(const drb::FlatOctree &T, float *node_box, int32_t *node_child, int32_t *node_leaf, int32_t *leaf_tri) {
+    // node 0 = root, node i + 1 = flat node i
+    auto put = [&](int64_t at, const float *lo, const float *hi, int32_t child, int64_t first, int32_t count) {
+        if (node_box) {
+            for (int k = 0; k < 3; k++) { node_box[6 * at + k] = lo[k]; node_box[6 * at + 3 + k] = hi[k]; }
+        }
+        if (node_child) node_child[at] = child;
+        if (node_leaf) {
+            node_leaf[2 * at] = child >= 0 ? 0 : (int32_t)first;
+            node_leaf[2 * at + 1] = child >= 0 ? 0 : count;
+        }
+    };
+    put(0, T.root_lo, T.root_hi, T.root_child >= 0 ? 1 : -1, T.root_leaf_first, T.root_leaf_count);
+    for (int64_t i = 0; i < T.node_count; i++)
+        put(i + 1, &T.node_lo[3 * i], &T.node_hi[3 * i], T.node_child[i] >= 0 ? T.node_child[i] + 1 : -1, T.node_leaf_first[i],
+            T.node_leaf_count[i]);
+    if (leaf_tri) std::copy(T.leaf_refs.begin(), T.leaf_refs.end(), leaf_tri);
+}
+
+dr_status dr_scene_stats(const dr_scene *sc, int64_t *nodes, int64_t *leaves, int64_t *refs, int32_t *depth) {
+    if (!sc) return fail(DR_E_ARG, "dr_scene_stats: scene is NULL");
+    tree_stats(sc->tree, nodes, leaves, refs, depth);
+    return DR_OK;
+}
+
+dr_status dr_scene_export_tree(const dr_scene *sc, float *node_box, int32_t *node_child, int32_t *node_leaf, int32_t *leaf_tri) {
+    if (!sc) return fail(DR_E_ARG, "dr_scene_export_tree: scene is NULL");
+    tree_export(sc->tree, node_box, node_child, node_leaf, leaf_tri);
+    return DR_OK;
+}
+
+dr_status dr_octree_create_host(const float *xyz, int32_t n, const dr_build_params *bp, dr_octree **out) {
+    if (!out) return fail(DR_E_ARG, "dr_octree_create_host: out is NULL");
+    *out = nullptr;
+    if (n < 0 || (n > 0 && !xyz)) return fail(DR_E_ARG, "dr_octree_create_host: bad triangle array");
+    dr_octree *t = new (std::nothrow) dr_octree();
+    if (!t) return fail(DR_E_NOMEM, "dr_octree_create_host: out of host memory");
+    drb::BuildOptions opt;
+    if (bp) {
+        if (bp->max_depth > 0) opt.max_depth = std::min(bp->max_depth, drd::kMaxDepth);
+        if (bp->split_threshold > 0) opt.split_threshold = bp->split_threshold;
+        opt.threads = bp->threads;
+    }
+    if (!drb::build_octree(xyz, n, opt, t->tree)) {
+        delete t;
+        return fail(DR_E_ARG, "dr_octree_create_host: build failed");
+    }
+    *out = t;
+    return DR_OK;
+}
+
+dr_status dr_octree_stats(const dr_octree *t, int64_t *nodes, int64_t *leaves, int64_t *refs, int32_t *depth) {
+    if (!t) return fail(DR_E_ARG, "dr_octree_stats: tree is NULL");
+    tree_stats(t->tree, nodes, leaves, refs, depth);
+    return DR_OK;
+}
+
+dr_status dr_octree_export(const dr_octree *t, float *node_box, int32_t *node_child, int32_t *node_leaf, int32_t *leaf_tri) {
+    if (!t) return fail(DR_E_ARG, "dr_octree_export: tree is NULL");
+    tree_export(t->tree, node_box, node_child, node_leaf, leaf_tri);
+    return DR_OK;
+}
+
+void dr_octree_destroy(dr_octree *t) { delete t; }
+
+void dr_scene_destroy(dr_scene *sc) { delete sc; }
+
+static dr_status cast_impl(const dr_scene *sc, const float *o, const float *d, const int32_t *ignore, int32_t n, int32_t clip,
+                           int32_t *hit_tri, float *hit_t, int32_t *nbox, int32_t *ntri, void *stream) {
+    if (!sc) return fail(DR_E_ARG, "dr_cast: scene is NULL");
+    if (n < 0) return fail(DR_E_ARG, "dr_cast: negative ray count");
+    if (n == 0) return DR_OK;
+    if (!o || !d || !hit_tri || !hit_t) return fail(DR_E_ARG, "dr_cast: NULL buffer");
+    cudaError_t e = drk::launch_cast(sc->dev, o, d, ignore, n, clip, hit_tri, hit_t, nbox, ntri, (cudaStream_t)stream, nullptr);
+    if (e != cudaSuccess) return cuda_fail(e, "dr_cast");
+    return DR_OK;
+}
+
+dr_status dr_cast(const dr_scene *sc, const float *o, const float *d, const int32_t *ignore, int32_t n, int32_t clip,
+                  int32_t *hit_tri, float *hit_t, void *stream) {
+    return cast_impl(sc, o, d, ignore, n, clip, hit_tri, hit_t, nullptr, nullptr, stream);
+}
+
+dr_status dr_cast_counted(const dr_scene *sc, const float *o, const float *d, const int32_t *ignore, int32_t n, int32_t clip,
+                          int32_t *hit_tri, float *hit_t, int32_t *nbox, int32_t *ntri, void *stream) {
+    if (!nbox || !ntri) return fail(DR_E_ARG, "dr_cast_counted: NULL counter buffer");
+    return cast_impl(sc, o, d, ignore, n, clip, hit_tri, hit_t, nbox, ntri, stream);
+}
+
+dr_status dr_renderer_create(int32_t wave_paths, dr_renderer **out) {
+    if (!out) return fail(DR_E_ARG, "dr_renderer_create: out is NULL");
+    *out = nullptr;
+    if (wave_paths < 0) return fail(DR_E_ARG, "dr_renderer_create: negative wave size");
+    if (wave_paths == 0) wave_paths = 1 << 22;
+    wave_paths = ((wave_paths + 31) / 32) * 32;
+    dr_renderer *r = new (std::nothrow) dr_renderer();
+    if (!r) return fail(DR_E_NOMEM, "dr_renderer_create: out of host memory");
+    r->capacity = wave_paths;
+    r->shadow_capacity = wave_paths * 2;
+    size_t W = (size_t)wave_paths;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+        for (int j = 0; j < 3 && e == cudaSuccess; j++) e = cudaMalloc((void **)&r->q[k][j], sizeof(float4) * W);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&r->q3[k], sizeof(int4) * W);
+    }
+    if (e == cudaSuccess) e = cudaMalloc((void **)&r->hits, sizeof(float2) * W);
+    for (int j = 0; j < 5 && e == cudaSuccess; j++) e = cudaMalloc((void **)&r->s[j], sizeof(float4) * (size_t)r->shadow_capacity);
+    if (e == cudaSuccess) e = cudaMalloc(&r->ctrl, drk::ctrl_bytes());
+    if (e != cudaSuccess) {
+        delete r;
+        return cuda_fail(e, "dr_renderer_create");
+    }
+    *out = r;
+    return DR_OK;
+}
+
+void dr_renderer_destroy(dr_renderer *r) { delete r; }
+
+int64_t dr_renderer_launch_count(const dr_renderer *r) { return r ? r->launches : 0; }
+
+dr_status dr_render_blocks(dr_renderer *r, const dr_scene *sc, const dr_camera *cam, float *fb, int32_t start_block,
+                           int32_t end_block, const dr_render_params *p, void *stream_ptr) {
+    if (!r || !sc || !cam || !fb || !p) return fail(DR_E_ARG, "dr_render_blocks: NULL argument");
+    if (p->mode != DR_MODE_REFERENCE && p->mode != DR_MODE_PHYSICAL) return fail(DR_E_ARG, "dr_render_blocks: bad mode");
+    if (p->width <= 0 || p->height <= 0) return fail(DR_E_ARG, "dr_render_blocks: bad resolution");
+    const int nblocks = dr_block_count(p->width, p->height);
+    if (start_block < 0 || end_block > nblocks || start_block > end_block) return fail(DR_E_ARG, "dr_render_blocks: bad block range");
+    if (p->max_bounces < 0 || p->max_bounces > 64) return fail(DR_E_ARG, "dr_render_blocks: max_bounces must be in [0, 64]");
+    if (p->boxing < 0 || p->boxing > 3) return fail(DR_E_ARG, "dr_render_blocks: bad boxing mode");
+    if (cam->lens < 0 || cam->lens > DR_LENS_SPHERICAL) return fail(DR_E_ARG, "dr_render_blocks: bad lens");
+    const bool ref_lens = cam->lens <= DR_LENS_SPHERICAL_SEGMENT;
+    if ((p->mode == DR_MODE_REFERENCE) != ref_lens)
+        return fail(DR_E_ARG, "dr_render_blocks: lens does not belong to the render mode");
+    if (start_block == end_block) return DR_OK;
+    cudaStream_t stream = (cudaStream_t)stream_ptr;
+    const int fx = std::max(1, p->samples_x), fy = std::max(1, p->samples_y);
+    const int spp = fx * fy;
+    const int n_slots = (end_block - start_block) * DR_BLOCK_W * DR_BLOCK_H;
+    const int per_path_shadow = (p->mode == DR_MODE_REFERENCE) ? std::max(1, sc->dev.n_lights) : 1;
+    long long wave = std::min<long long>(r->capacity, (long long)r->shadow_capacity / per_path_shadow);
+    wave = std::max<long long>(32, (wave / 32) * 32);
+
+    if (r->accum_slots < (size_t)n_slots) {
+        cudaFree(r->accum);
+        r->accum = nullptr;
+        r->accum_slots = 0;
+        cudaError_t e = cudaMalloc((void **)&r->accum, sizeof(float4) * (size_t)n_slots);
+        if (e != cudaSuccess) return cuda_fail(e, "dr_render_blocks: accumulator");
+        r->accum_slots = (size_t)n_slots;
+    }
+    cudaError_t e = cudaMemsetAsync(r->accum, 0, sizeof(float4) * (size_t)n_slots, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "dr_render_blocks: memset");
+
+    drk::WaveDesc W;
+    W.scene = sc->dev;
+    W.camera = *cam;
+    {
+        float angle = cam->angle[0];
+        if (angle < 1.0f) angle = 1.0f;
+        else if (angle > 179.0f) angle = 179.0f;
+        float radian = (angle / (2 * 57.29577951308233f));
+        W.cam_x = 0.5f / std::tan(radian);
+    }
+    W.mode = p->mode;
+    W.width = p->width;
+    W.height = p->height;
+    W.fsaa_x = fx;
+    W.fsaa_y = fy;
+    W.spp = spp;
+    W.max_bounces = p->max_bounces;
+    W.clip = p->cull_backfaces;
+    {
+        float w = (float)p->width, h = (float)p->height;
+        float ps = 1.0f;
+        if (p->boxing == DR_BOXING_HEIGHT) ps = 1.0f / h;
+        else if (p->boxing == DR_BOXING_WIDTH) ps = 1.0f / w;
+        else if (p->boxing == DR_BOXING_MIN) ps = 1.0f / ((h <= w) ? h : w);
+        else ps = 1.0f / ((h >= w) ? h : w);
+        W.pixel_size = ps;
+        W.pdx = ps / (float)fx;
+        W.pdy = ps / (float)fy;
+    }
+    W.seed = p->seed;
+    W.sample_base = (uint32_t)((p->iteration < 1 ? 0 : p->iteration - 1) * spp);
+    W.start_block = start_block;
+    W.n_slots = n_slots;
+    for (int k = 0; k < 2; k++) {
+        W.q_p0[k] = r->q[k][0];
+        W.q_p1[k] = r->q[k][1];
+        W.q_p2[k] = r->q[k][2];
+        W.q_p3[k] = r->q3[k];
+    }
+    W.hits = r->hits;
+    for (int j = 0; j < 5; j++) W.s[j] = r->s[j];
+    W.accum = r->accum;
+    W.ctrl = r->ctrl;
+    const long long total = (long long)n_slots * spp;
+    for (long long b = 0; b < total; b += wave) {
+        W.wave_begin = b;
+        W.wave_count = (int)std::min<long long>(wave, total - b);
+        e = drk::launch_wave(W, stream, &r->launches);
+        if (e != cudaSuccess) return cuda_fail(e, "dr_render_blocks: wave");
+    }
+    const float blend = (p->iteration <= 1) ? 1.0f : (1.0f / (float)p->iteration);
+    e = drk::launch_resolve(r->accum, fb, start_block, n_slots, p->width, p->height, 1.0f / (float)spp, blend, stream, &r->launches);
+    if (e != cudaSuccess) return cuda_fail(e, "dr_render_blocks: resolve");
+    return DR_OK;
+}
+
+}  // extern "C"

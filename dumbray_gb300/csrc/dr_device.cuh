@@ -1,0 +1,244 @@
+// dr_device.cuh - device-side scene layout and the exact octree cast for sm_103a.
+//
+// Layout in HBM (all read-only after upload):
+//   nodes      float4[2 * node_count]  node i = {lo.xyz, w = first child (inner) or ~first ref (leaf)},
+//                                               {hi.xyz, w = leaf ref count}
+//              children of an inner node are 8 consecutive nodes, 8-aligned (one 256-byte group).
+//   leaf_tris  float4[3 * refs]        leaf reference r = {a.xyz, w = triangle id}, {b.xyz}, {c.xyz}:
+//              the leaf's triangles duplicated in leaf order, so a leaf is one contiguous stream.
+//   tris       float4[3 * n]           triangles by id (shading, light sampling)
+// The cast reproduces DumbRay's Octree::cast (Octree.impl.cuh:174-212) bit for bit: every
+// floating-point operation of the slab test, the triangle plane test and the edge-angle
+// containment predicate is issued as an explicitly rounded intrinsic (__fadd_rn, __fmul_rn,
+// __fdiv_rn, __fsqrt_rn), so no FMA contraction or approximate division can change a result.
+#pragma once
+#include <cfloat>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace drd {
+
+constexpr float kEps = 0.000005f;               // VECTOR_EPSILON (Vector3.h:10)
+constexpr int kMaxDepth = 24;                    // OCTREE_MAX_DEPTH (Octree.cuh:13)
+constexpr int kStack = kMaxDepth + 2;
+
+struct Material {
+    int type;
+    float color[3];
+    float fresnel[3];
+    float specular, metal, diffuse, smoothness, shininess, roughness;
+    float emission[3];
+};
+
+struct Light {
+    int type;
+    float color[3];
+    float position[3];
+    float direction[3];
+    float radius, distance, softness;
+};
+
+struct Scene {
+    const float4 *nodes;
+    const float4 *leaf_tris;
+    const float4 *tris;
+    const float4 *nrms;
+    const int *mat_id;
+    const Material *mats;
+    const Light *lights;
+    const float4 *shade;        // physical: [2n] {albedo.rgb, roughness}, {emission.rgb, type bits}
+    const int *emissive;        // emissive triangle ids
+    const float *emissive_cdf;  // inclusive prefix sums of power
+    float root_lo[3], root_hi[3];
+    int root_child;             // 0 = root split (children are nodes 0..7), -1 = root is a leaf
+    int root_leaf_first, root_leaf_count;
+    int n_tris, n_mats, n_lights, n_emissive;
+    float emissive_total;
+};
+
+// ---- exactly rounded float3 arithmetic (reference operation order) -------------------------
+struct f3 {
+    float x, y, z;
+};
+__device__ __forceinline__ f3 mkf3(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 xsub(f3 a, f3 b) { return f3{__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)}; }
+__device__ __forceinline__ f3 xadd(f3 a, f3 b) { return f3{__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)}; }
+__device__ __forceinline__ f3 xmul(f3 a, float f) { return f3{__fmul_rn(a.x, f), __fmul_rn(a.y, f), __fmul_rn(a.z, f)}; }
+// Vector3 dot: (x*v.x + y*v.y) + z*v.z
+__device__ __forceinline__ float xdot(f3 a, f3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+// Vector3 cross a & v: (y*v.z - v.y*z, v.x*z - x*v.z, x*v.y - v.x*y)
+__device__ __forceinline__ f3 xcross(f3 a, f3 v) {
+    return f3{__fsub_rn(__fmul_rn(a.y, v.z), __fmul_rn(v.y, a.z)), __fsub_rn(__fmul_rn(v.x, a.z), __fmul_rn(a.x, v.z)),
+              __fsub_rn(__fmul_rn(a.x, v.y), __fmul_rn(v.x, a.y))};
+}
+__device__ __forceinline__ float xmag(f3 a) { return __fsqrt_rn(xdot(a, a)); }
+__device__ __forceinline__ bool xeq(f3 a, f3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+__device__ __forceinline__ f3 f3of(float4 v) { return f3{v.x, v.y, v.z}; }
+
+// AABB::castPreInversed + Shapes::castPreInversed<AABB>(.., clipBackface = false)
+// (AABB.impl.h:116-130, Shapes.impl.cuh:143-147)
+__device__ __forceinline__ bool slab_hit(float lx, float ly, float lz, float hx, float hy, float hz, f3 o, f3 inv) {
+    float ds = __fmul_rn(__fsub_rn(lx, o.x), inv.x);
+    float de = __fmul_rn(__fsub_rn(hx, o.x), inv.x);
+    float mn = fminf(ds, de), mx = fmaxf(ds, de);
+    ds = __fmul_rn(__fsub_rn(ly, o.y), inv.y);
+    de = __fmul_rn(__fsub_rn(hy, o.y), inv.y);
+    mn = fmaxf(mn, fminf(ds, de));
+    mx = fminf(mx, fmaxf(ds, de));
+    ds = __fmul_rn(__fsub_rn(lz, o.z), inv.z);
+    de = __fmul_rn(__fsub_rn(hz, o.z), inv.z);
+    mn = fmaxf(mn, fminf(ds, de));
+    mx = fminf(mx, fmaxf(ds, de));
+    if (mn > __fadd_rn(mx, kEps)) return false;
+    return mn != FLT_MAX;
+}
+
+// Triangle::containsVertex (Triangle.impl.h:283-302)
+__device__ __forceinline__ bool contains_vertex(f3 a, f3 b, f3 c, f3 p) {
+    if (xeq(a, b) || xeq(b, c) || xeq(c, a)) return false;
+    if (xeq(p, a) || xeq(p, b) || xeq(p, c)) return true;
+    const float S = 32 * kEps;
+    f3 ab = xsub(b, a), bc = xsub(c, b), ca = xsub(a, c);
+    f3 ax = xsub(p, a), bx = xsub(p, b), cx = xsub(p, c);
+    if (!(__fadd_rn(__fdiv_rn(xdot(ab, ax), xmag(ax)), S) >= __fdiv_rn(-xdot(ab, ca), xmag(ca)))) return false;
+    if (!(__fadd_rn(__fdiv_rn(xdot(bc, bx), xmag(bx)), S) >= __fdiv_rn(-xdot(bc, ab), xmag(ab)))) return false;
+    return __fadd_rn(__fdiv_rn(xdot(ca, cx), xmag(cx)), S) >= __fdiv_rn(-xdot(ca, bc), xmag(bc));
+}
+
+// Triangle::cast (Triangle.impl.h:334-348)
+__device__ __forceinline__ bool tri_cast(f3 a, f3 b, f3 c, f3 o, f3 d, bool clip, float &dist, f3 &hp) {
+    f3 n = xcross(xsub(b, a), xsub(c, a));
+    float dp = xdot(xsub(a, o), n);
+    if (clip && (dp < -kEps)) return false;
+    float dirp = xdot(d, n);
+    if (__fmul_rn(dp, dirp) <= 0.0f) return false;
+    float distance = __fdiv_rn(dp, dirp);
+    f3 hv = xadd(o, xmul(d, distance));
+    if (!contains_vertex(a, b, c, hv)) return false;
+    dist = distance;
+    hp = hv;
+    return true;
+}
+
+struct Hit {
+    int tri;     // -1 = miss
+    float t;     // in units of |d|
+    f3 p;        // hit point o + d * t (exactly as the reference computes it)
+};
+
+// castInLeaf (Octree.impl.cuh:584-612): strict-min distance over the leaf list (ties keep the
+// first), `ignore` = validateNotSameAsObject, accept only if the hit point is inside the leaf box.
+__device__ __forceinline__ bool cast_leaf(const Scene &S, int first, int count, float lx, float ly, float lz, float hx,
+                                          float hy, float hz, f3 o, f3 d, bool clip, int ignore, Hit &h, int &ntri) {
+    if (count <= 0) return false;
+    float best = FLT_MAX;
+    f3 bp = mkf3(0.f, 0.f, 0.f);
+    int bi = -1;
+    const float4 *lt = S.leaf_tris + 3 * (size_t)first;
+    for (int r = 0; r < count; r++) {
+        float4 A = __ldg(lt + 3 * r), B = __ldg(lt + 3 * r + 1), C = __ldg(lt + 3 * r + 2);
+        int id = __float_as_int(A.w);
+        float dist;
+        f3 hp;
+        ntri++;
+        bool ok = tri_cast(f3of(A), f3of(B), f3of(C), o, d, clip, dist, hp);
+        if (ok && id == ignore) ok = false;
+        if (ok && dist < best) { best = dist; bp = hp; bi = id; }
+    }
+    if (best != FLT_MAX && bp.x >= lx && bp.y >= ly && bp.z >= lz && bp.x <= hx && bp.y <= hy && bp.z <= hz) {
+        h.tri = bi;
+        h.t = best;
+        h.p = bp;
+        return true;
+    }
+    return false;
+}
+
+// Tests the 8 children of a group; bit k of the result = child (order ^ k) is hit.
+__device__ __forceinline__ unsigned test_group(const Scene &S, int group, int order, f3 o, f3 inv) {
+    unsigned m = 0;
+    const float4 *g = S.nodes + 16 * (size_t)group;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        int c = order ^ k;
+        float4 lo = __ldg(g + 2 * c), hi = __ldg(g + 2 * c + 1);
+        if (slab_hit(lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, o, inv)) m |= 1u << k;
+    }
+    return m;
+}
+
+// Octree::cast (Octree.impl.cuh:174-212).  Visits children in the reference's sign order
+// (canonicalOrder ^ k); the 8 slab tests of a group are done up front (they are pure), which
+// visits exactly the same leaves in the same order.  With COUNT, nbox receives the number of
+// child-box tests the reference's sequential scan performs (it stops scanning a group when a hit
+// is returned below it) plus the root test, and ntri the triangle tests.
+template <bool COUNT>
+__device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool clip, int ignore, Hit &h, int &nbox,
+                                             int &ntri) {
+    h.tri = -1;
+    h.t = FLT_MAX;
+    f3 inv = mkf3(__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z));
+    if (S.root_child < 0)
+        return cast_leaf(S, S.root_leaf_first, S.root_leaf_count, S.root_lo[0], S.root_lo[1], S.root_lo[2], S.root_hi[0],
+                         S.root_hi[1], S.root_hi[2], o, d, clip, ignore, h, ntri);
+    if (COUNT) nbox++;
+    if (!slab_hit(S.root_lo[0], S.root_lo[1], S.root_lo[2], S.root_hi[0], S.root_hi[1], S.root_hi[2], o, inv)) return false;
+    const int order = (d.z < 0 ? 1 : 0) + (d.y < 0 ? 2 : 0) + (d.x < 0 ? 4 : 0);
+    // stack entry: group << 11 | position taken << 8 | remaining hit mask (visit order)
+    uint32_t stack[kStack];
+    int sp = 0;
+    uint32_t cur = test_group(S, 0, order, o, inv);
+    if (COUNT) nbox += 8;
+    for (;;) {
+        uint32_t m = cur & 0xFFu;
+        if (m == 0) {
+            if (sp == 0) return false;
+            cur = stack[--sp];
+            continue;
+        }
+        int k = __ffs(m) - 1;
+        cur &= ~(1u << k);
+        int group = (int)(cur >> 11);
+        int node = group * 8 + (order ^ k);
+        float4 lo = __ldg(S.nodes + 2 * (size_t)node), hi = __ldg(S.nodes + 2 * (size_t)node + 1);
+        int w = __float_as_int(lo.w);
+        if (w < 0) {
+            if (cast_leaf(S, ~w, __float_as_int(hi.w), lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, o, d, clip, ignore, h, ntri)) {
+                if (COUNT) {
+                    nbox -= 7 - k;
+                    for (int s = 0; s < sp; s++) nbox -= 7 - (int)((stack[s] >> 8) & 7u);
+                }
+                return true;
+            }
+        } else {
+            if (sp >= kStack) return false;  // unreachable for trees of depth <= 24
+            stack[sp++] = (cur & ~(7u << 8)) | ((uint32_t)k << 8);
+            cur = ((uint32_t)(w >> 3) << 11) | test_group(S, w >> 3, order, o, inv);
+            if (COUNT) nbox += 8;
+        }
+    }
+}
+
+// ---- counter-based random numbers ----------------------------------------------------------
+// u32 = H(H(key + 0x9E3779B9 * (bounce * 128 + dim + 1))), key = H(H(H(seed ^ 0x2545F491) ^ pixel) + sample),
+// H = lowbias32 (C. Wellons' public-domain integer hash).  Float = (u >> 8) * 2^-24 in [0, 1).
+__host__ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352dU;
+    x ^= x >> 15;
+    x *= 0x846ca68bU;
+    x ^= x >> 16;
+    return x;
+}
+__host__ __device__ __forceinline__ uint32_t path_key(uint32_t seed, uint32_t pixel, uint32_t sample) {
+    return hash32(hash32(hash32(seed ^ 0x2545F491U) ^ pixel) + sample);
+}
+__device__ __forceinline__ float rnd(uint32_t key, uint32_t bounce, uint32_t dim) {
+    uint32_t u = hash32(hash32(key + 0x9E3779B9U * (bounce * 128U + dim + 1U)));
+    return (float)(u >> 8) * (1.0f / 16777216.0f);
+}
+constexpr uint32_t kLensBounce = 1023;
+
+}  // namespace drd

@@ -1,0 +1,681 @@
+// dr_kernels.cu - sm_103a kernels of the GB300 DumbRay hot path.
+//
+//   k_cast            ray batch -> closest hit (Octree::cast, Octree.impl.cuh:174-212)
+//   k_camera          per path: lens sample -> ray queue            (Lense::getPixelSamples)
+//   k_trace           ray queue -> hit records                       (Octree::cast)
+//   k_shade_ref       DumbRenderer layer step (DumbRenderer.cu:249-443) as one forward path step:
+//                     indirect request, light photons -> shadow queue, next ray -> next queue
+//   k_shadow_ref      light -> point visibility with the reference's transparency re-casts
+//   k_shade_phys      physical path step (emission + MIS, NEE -> shadow queue, BSDF sample)
+//   k_shadow_phys     point -> light visibility
+//   k_resolve         accumulators -> BlockBasedFrameBuffer<8,16> set / blend (BlockBasedFrameBuffer.impl.cuh:149-156)
+//
+// Wavefront design: queues are structure-of-arrays of float4/int4 records in HBM; work is pulled by
+// persistent warps through one atomic per warp; outputs are compacted with a warp ballot and one
+// atomic per warp.  Queue counts live in a device control block, so a whole wave is a fixed launch
+// sequence with no host synchronisation.
+#include "dr_kernels.h"
+#include "dr_shading.cuh"
+
+#include <cstdio>
+
+namespace drd {
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// Warp-aggregated slot allocation: every lane of the warp must call this together.
+__device__ __forceinline__ int warp_alloc(int *counter, bool want) {
+    unsigned ballot = __ballot_sync(0xFFFFFFFFu, want);
+    if (ballot == 0) return -1;
+    int leader = __ffs(ballot) - 1;
+    int base = 0;
+    if ((int)lane_id() == leader) base = atomicAdd(counter, __popc(ballot));
+    base = __shfl_sync(0xFFFFFFFFu, base, leader);
+    return want ? base + __popc(ballot & ((1u << lane_id()) - 1u)) : -1;
+}
+
+// Warp-level work fetch from a dynamic counter; returns the base index (warp-uniform).
+__device__ __forceinline__ int warp_fetch(int *counter) {
+    int base = 0;
+    if (lane_id() == 0) base = atomicAdd(counter, 32);
+    return __shfl_sync(0xFFFFFFFFu, base, 0);
+}
+
+// ---------------------------------------------------------------------------------------------
+template <bool COUNT>
+__global__ void __launch_bounds__(256) k_cast(Scene S, const float *__restrict__ o, const float *__restrict__ d,
+                                              const int *__restrict__ ignore, int n, int clip, int *__restrict__ hit_tri,
+                                              float *__restrict__ hit_t, int *__restrict__ nbox, int *__restrict__ ntri) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        f3 ro = mkf3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
+        f3 rd = mkf3(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
+        int ign = ignore ? ignore[i] : -1;
+        Hit h;
+        int nb = 0, nt = 0;
+        cast_closest<COUNT>(S, ro, rd, clip != 0, ign, h, nb, nt);
+        hit_tri[i] = h.tri;
+        hit_t[i] = h.tri >= 0 ? h.t : FLT_MAX;
+        if (COUNT) {
+            nbox[i] = nb;
+            ntri[i] = nt;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Wave control block (int slots, zeroed at the start of every wave).
+//   ray_count[b]   rays in the queue consumed at bounce b
+//   fetch_trace[b], fetch_shade[b], fetch_shadow[b], shadow_count[b]
+struct Ctrl {
+    int ray_count[kMaxBounceSlots];
+    int shadow_count[kMaxBounceSlots];
+    int fetch_trace[kMaxBounceSlots];
+    int fetch_shade[kMaxBounceSlots];
+    int fetch_shadow[kMaxBounceSlots];
+    int fetch_camera;
+    int error;
+};
+
+// Ray queue record (64 B, 4 x 16 B SoA planes):
+//   p0 = {o.xyz, pixel slot}   p1 = {d.xyz, sample index}   p2 = {throughput.rgb, prev pdf}
+//   p3 = {prev triangle, flags (bit0 = prev delta), pixel id, unused}
+struct Queue {
+    float4 *p0, *p1, *p2;
+    int4 *p3;
+};
+// Hit record: {tri, t}
+// Shadow record (80 B): s0 = {origin.xyz, pixel slot}, s1 = {dir.xyz, target tri}, s2 = {target point.xyz, ignore tri},
+//                       s3 = {light colour rgb, -}, s4 = {contribution rgb, -}
+struct ShadowQ {
+    float4 *s0, *s1, *s2, *s3, *s4;
+};
+
+struct WaveArgs {
+    Scene S;
+    dr_camera cam;
+    float cam_x;            // 0.5 / tan(fov/2) for the reference pinhole lenses
+    int mode;
+    int width, height;
+    int fsaa_x, fsaa_y;
+    int spp;
+    int max_bounces;
+    int clip;
+    float pixel_size, pdx, pdy;
+    uint32_t seed;
+    uint32_t sample_base;
+    int start_block;
+    int n_slots;            // pixel slots in the block range (blocks * 128)
+    long long wave_begin;   // first path index of this wave
+    int wave_count;         // paths in this wave
+    Queue q[2];
+    float2 *hits;
+    ShadowQ sq;
+    float *accum;           // [n_slots][4]
+    Ctrl *ctrl;
+};
+
+__device__ __forceinline__ void accum_add(float *acc, int slot, c3 c) {
+    if (c.r != 0.0f) atomicAdd(acc + 4 * slot, c.r);
+    if (c.g != 0.0f) atomicAdd(acc + 4 * slot + 1, c.g);
+    if (c.b != 0.0f) atomicAdd(acc + 4 * slot + 2, c.b);
+}
+
+__device__ __forceinline__ f3 cam_to_world(const dr_camera &c, f3 d) {
+    return f3{d.x * c.right[0] + d.y * c.up[0] + d.z * c.forward[0], d.x * c.right[1] + d.y * c.up[1] + d.z * c.forward[1],
+              d.x * c.right[2] + d.y * c.up[2] + d.z * c.forward[2]};
+}
+
+// Lens sample for one path.  Returns false for pixels that produce no ray.
+__device__ inline bool lens_ray(const WaveArgs &A, int x, int y, int s, uint32_t key, f3 &o, f3 &d, c3 &filter) {
+    const dr_camera &c = A.cam;
+    filter = mkc(1, 1, 1);
+    if (A.mode == DR_MODE_REFERENCE) {
+        int fi = s / A.fsaa_y, fj = s - fi * A.fsaa_y;
+        float px = ((float)x - ((float)A.width / 2.0f)) * A.pixel_size;
+        float py = (((float)A.height / 2.0f) - (float)y) * A.pixel_size;
+        float sx = px + (((float)fi) + 0.5f) * A.pdx;
+        float sy = py + (((float)fj) + 0.5f) * A.pdy;
+        float ox = A.pdx / 2.0f, oy = A.pdy / 2.0f;
+        if (c.lens == DR_LENS_DEFAULT_PERSPECTIVE) {
+            o = f3{0, 0, 0};
+            d = norm3(f3{sx, sy, A.cam_x});
+        } else if (c.lens == DR_LENS_SIMPLE_STOCHASTIC) {
+            float jx = (rnd(key, kLensBounce, 0) * (ox - (-ox))) + (-ox);
+            float jy = (rnd(key, kLensBounce, 1) * (oy - (-oy))) + (-oy);
+            o = f3{0, 0, 0};
+            d = f3{sx + jx, sy + jy, A.cam_x};
+        } else {
+            float jx = (rnd(key, kLensBounce, 0) * (ox - (-ox))) + (-ox);
+            float jy = (rnd(key, kLensBounce, 1) * (oy - (-oy))) + (-oy);
+            const float RADIAN = 57.29577951308233f;
+            float ha = ((sx + jx) * c.angle[0] / RADIAN);
+            float va = ((sy + jy) * c.angle[1] / RADIAN);
+            f3 td = f3{sinf(ha) * cosf(va), sinf(va), cosf(ha) * cosf(va)};
+            f3 target = mul3(td, c.focal_distance);
+            float ra = (rnd(key, kLensBounce, 2) * (2.0f * 3.14159265359f - 0.0f)) + 0.0f;
+            f3 origin = mul3(mul3(f3{cosf(ra), sinf(ra), 0.0f}, asinf(rnd(key, kLensBounce, 3))), c.softness);
+            o = origin;
+            d = norm3(sub3(target, origin));
+            filter = mkc(c.filter[0], c.filter[1], c.filter[2]);
+        }
+    } else {
+        float jx = rnd(key, kLensBounce, 0), jy = rnd(key, kLensBounce, 1);
+        float sx = ((float)x + jx - 0.5f * (float)A.width) / (float)A.height;
+        float sy = (0.5f * (float)A.height - ((float)y + jy)) / (float)A.height;
+        f3 dl;
+        const float PI = 3.14159265358979f;
+        if (c.lens == DR_LENS_FISHEYE) {
+            float r = sqrtf(sx * sx + sy * sy);
+            float theta = r * (c.angle[0] * PI / 180.0f);
+            if (theta > PI) return false;
+            float phi = atan2f(sy, sx);
+            float st = sinf(theta);
+            dl = f3{st * cosf(phi), st * sinf(phi), cosf(theta)};
+        } else if (c.lens == DR_LENS_SPHERICAL) {
+            float h = sx * (c.angle[0] * PI / 180.0f);
+            float v = sy * (c.angle[1] * PI / 180.0f);
+            dl = f3{sinf(h) * cosf(v), sinf(v), cosf(h) * cosf(v)};
+        } else {
+            dl = norm3(f3{sx, sy, A.cam_x});
+        }
+        o = f3{0, 0, 0};
+        d = norm3(cam_to_world(c, dl));
+        o = f3{c.position[0], c.position[1], c.position[2]};
+        return true;
+    }
+    o = add3(cam_to_world(c, o), f3{c.position[0], c.position[1], c.position[2]});
+    d = cam_to_world(c, d);
+    return true;
+}
+
+__global__ void __launch_bounds__(256) k_camera(WaveArgs A) {
+    Ctrl *C = A.ctrl;
+    for (;;) {
+        int base = warp_fetch(&C->fetch_camera);
+        if (base >= A.wave_count) break;
+        int i = base + (int)lane_id();
+        bool valid = i < A.wave_count;
+        f3 o = f3{0, 0, 0}, d = f3{0, 0, 1};
+        c3 filt = mkc(0, 0, 0);
+        int slot = 0, pixel = 0;
+        uint32_t sample = 0;
+        if (valid) {
+            long long g = A.wave_begin + i;
+            int s = (int)(g / A.n_slots);
+            slot = (int)(g - (long long)s * A.n_slots);
+            int blk = A.start_block + slot / (DR_BLOCK_W * DR_BLOCK_H);
+            int pid = slot % (DR_BLOCK_W * DR_BLOCK_H);
+            int bw = (A.width + DR_BLOCK_W - 1) / DR_BLOCK_W;
+            int by = blk / bw, bx = blk - by * bw;
+            int x = bx * DR_BLOCK_W + (pid % DR_BLOCK_W), y = by * DR_BLOCK_H + pid / DR_BLOCK_W;
+            valid = (x < A.width) && (y < A.height);
+            if (valid) {
+                pixel = y * A.width + x;
+                sample = A.sample_base + (uint32_t)s;
+                uint32_t key = path_key(A.seed, (uint32_t)pixel, sample);
+                valid = lens_ray(A, x, y, s, key, o, d, filt);
+            }
+        }
+        int w = warp_alloc(&C->ray_count[0], valid);
+        if (valid) {
+            Queue &Q = A.q[0];
+            Q.p0[w] = make_float4(o.x, o.y, o.z, __int_as_float(slot));
+            Q.p1[w] = make_float4(d.x, d.y, d.z, __uint_as_float(sample));
+            Q.p2[w] = make_float4(filt.r, filt.g, filt.b, 0.0f);
+            Q.p3[w] = make_int4(-1, 1, pixel, 0);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_trace(WaveArgs A, int b) {
+    Ctrl *C = A.ctrl;
+    const Queue Q = A.q[b & 1];
+    const int n = *((volatile int *)&C->ray_count[b]);
+    const bool clip = A.mode == DR_MODE_REFERENCE ? (A.clip != 0) : false;
+    for (;;) {
+        int base = warp_fetch(&C->fetch_trace[b]);
+        if (base >= n) break;
+        int i = base + (int)lane_id();
+        if (i < n) {
+            float4 p0 = Q.p0[i], p1 = Q.p1[i];
+            int4 p3 = Q.p3[i];
+            Hit h;
+            int nb = 0, nt = 0;
+            cast_closest<false>(A.S, f3of(p0), f3of(p1), clip, p3.x, h, nb, nt);
+            A.hits[i] = make_float2(__int_as_float(h.tri), h.t);
+        }
+    }
+}
+
+// Reference semantics: one layer of DumbRenderer's state machine, with the layer gather folded
+// into a forward throughput (getReflectedColor is linear in the photon colour).
+__global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
+    Ctrl *C = A.ctrl;
+    const Scene &S = A.S;
+    const Queue Q = A.q[b & 1];
+    const Queue N = A.q[(b + 1) & 1];
+    const int n = *((volatile int *)&C->ray_count[b]);
+    for (;;) {
+        int base = warp_fetch(&C->fetch_shade[b]);
+        if (base >= n) break;
+        int i = base + (int)lane_id();
+        bool active = i < n;
+        int tri = -1;
+        float4 p0, p1, p2;
+        int4 p3;
+        float t = 0.0f;
+        if (active) {
+            float2 h = A.hits[i];
+            tri = __float_as_int(h.x);
+            t = h.y;
+            p0 = Q.p0[i];
+            p1 = Q.p1[i];
+            p2 = Q.p2[i];
+            p3 = Q.p3[i];
+        }
+        active = active && tri >= 0;
+        bool child = false;
+        f3 hp = f3{0, 0, 0}, cd = f3{0, 0, 0};
+        c3 thr = mkc(0, 0, 0);
+        uint32_t key = 0;
+        if (active) {
+            f3 o = f3of(p0), d = f3of(p1);
+            hp = xadd(o, xmul(d, t));
+            thr = mkc(p2.x, p2.y, p2.z);
+            key = path_key(A.seed, (uint32_t)p3.z, __float_as_uint(p1.w));
+            if (b < A.max_bounces) {
+                const Material &m = S.mats[__ldg(S.mat_id + tri)];
+                TriV v = load_tri(S.tris, tri), nt = load_tri(S.nrms, tri);
+                int ctype = 0;
+                if (m.type == 0) child = dumb_based_request(m, v, nt, hp, d, key, (uint32_t)b, cd, ctype);
+                else {
+                    cd = ss_request(m, v, nt, hp, d, key, (uint32_t)b);
+                    child = true;
+                }
+                if (child) {
+                    c3 w = ref_reflect(S, tri, hp, neg3(cd), neg3(d), false, ctype);
+                    child = true;
+                    // throughput of the child layer
+                    p2 = make_float4(thr.r * w.r, thr.g * w.g, thr.b * w.b, 0.0f);
+                }
+            }
+        }
+        // light photons: one shadow record per light
+        for (int li = 0; li < S.n_lights; li++) {
+            bool emit = false;
+            f3 lo, ld;
+            c3 lc, contrib;
+            if (active) {
+                light_photon(S.lights[li], hp, key, (uint32_t)b, li, lo, ld, lc);
+                c3 r = ref_reflect(S, tri, hp, ld, neg3(f3of(p1)), true, 0);
+                contrib = cmul(thr, r);
+                emit = (contrib.r + contrib.g + contrib.b) != 0.0f && (lc.r + lc.g + lc.b) != 0.0f;
+            }
+            int w = warp_alloc(&C->shadow_count[b], emit);
+            if (emit) {
+                A.sq.s0[w] = make_float4(lo.x, lo.y, lo.z, __int_as_float(__float_as_int(p0.w)));
+                A.sq.s1[w] = make_float4(ld.x, ld.y, ld.z, __int_as_float(tri));
+                A.sq.s2[w] = make_float4(hp.x, hp.y, hp.z, __int_as_float(-1));
+                A.sq.s3[w] = make_float4(lc.r, lc.g, lc.b, 0.0f);
+                A.sq.s4[w] = make_float4(contrib.r, contrib.g, contrib.b, 0.0f);
+            }
+        }
+        int w = warp_alloc(&C->ray_count[b + 1], child);
+        if (child) {
+            N.p0[w] = make_float4(hp.x, hp.y, hp.z, p0.w);
+            N.p1[w] = make_float4(cd.x, cd.y, cd.z, p1.w);
+            N.p2[w] = p2;
+            N.p3[w] = make_int4(tri, 0, p3.z, 0);
+        }
+    }
+}
+
+// Reference light visibility (DumbRenderer.cu:361-428): cast from the light sample toward the
+// point; it counts if the first hit is the shaded triangle or lies within sqrt(8 eps) of the
+// point; otherwise the blocker's reflected colour decides whether the photon continues.
+__global__ void __launch_bounds__(256) k_shadow_ref(WaveArgs A, int b) {
+    Ctrl *C = A.ctrl;
+    const Scene &S = A.S;
+    const int n = *((volatile int *)&C->shadow_count[b]);
+    const bool clip = A.clip != 0;
+    for (;;) {
+        int base = warp_fetch(&C->fetch_shadow[b]);
+        if (base >= n) break;
+        int i = base + (int)lane_id();
+        if (i < n) {
+            float4 s0 = A.sq.s0[i], s1 = A.sq.s1[i], s2 = A.sq.s2[i], s3 = A.sq.s3[i], s4 = A.sq.s4[i];
+            f3 lo = f3of(s0), ld = f3of(s1), hp = f3of(s2);
+            int target = __float_as_int(s1.w);
+            int slot = __float_as_int(s0.w);
+            c3 lc = mkc(s3.x, s3.y, s3.z);
+            int restrict_obj = -1;
+            for (int guard = 0; guard < 64; guard++) {
+                Hit h;
+                int nb = 0, nt = 0;
+                cast_closest<false>(S, lo, ld, clip, restrict_obj, h, nb, nt);
+                if (h.tri < 0) break;
+                f3 dd = xsub(h.p, hp);
+                if (h.tri == target || xdot(dd, dd) <= (8.0f * kEps)) {
+                    accum_add(A.accum, slot, mkc(s4.x * lc.r, s4.y * lc.g, s4.z * lc.b));
+                    break;
+                }
+                c3 tr = cmul(ref_reflect(S, h.tri, h.p, ld, ld, true, 0), lc);
+                if ((tr.r + tr.g + tr.b) > kEps) {
+                    lc = tr;
+                    lo = add3(h.p, mul3(norm3(ld), 64.0f * kEps));
+                    restrict_obj = h.tri;
+                } else break;
+            }
+        }
+    }
+}
+
+// Physical path step.
+__global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
+    Ctrl *C = A.ctrl;
+    const Scene &S = A.S;
+    const Queue Q = A.q[b & 1];
+    const Queue N = A.q[(b + 1) & 1];
+    const int n = *((volatile int *)&C->ray_count[b]);
+    for (;;) {
+        int base = warp_fetch(&C->fetch_shade[b]);
+        if (base >= n) break;
+        int i = base + (int)lane_id();
+        bool active = i < n;
+        int tri = -1;
+        float4 p0, p1, p2;
+        int4 p3;
+        float t = 0.0f;
+        if (active) {
+            float2 h = A.hits[i];
+            tri = __float_as_int(h.x);
+            t = h.y;
+            p0 = Q.p0[i];
+            p1 = Q.p1[i];
+            p2 = Q.p2[i];
+            p3 = Q.p3[i];
+        }
+        active = active && tri >= 0;
+        bool emit_shadow = false, child = false;
+        f3 hp = f3{0, 0, 0}, sdir = f3{0, 0, 0}, nd = f3{0, 0, 0};
+        c3 scontrib = mkc(0, 0, 0), thr = mkc(0, 0, 0);
+        int light_tri = -1;
+        float new_pdf = 0.0f;
+        int new_delta = 0;
+        int slot = 0;
+        if (active) {
+            slot = __float_as_int(p0.w);
+            f3 o = f3of(p0), d = f3of(p1);
+            hp = xadd(o, xmul(d, t));
+            thr = mkc(p2.x, p2.y, p2.z);
+            uint32_t key = path_key(A.seed, (uint32_t)p3.z, __float_as_uint(p1.w));
+            TriV v = load_tri(S.tris, tri);
+            f3 outward = tri_normal(v);
+            f3 ng = norm3(outward);
+            f3 wo = neg3(d);
+            if (dot3(ng, wo) < 0) ng = neg3(ng);
+            float4 sh0 = __ldg(S.shade + 2 * (size_t)tri), sh1 = __ldg(S.shade + 2 * (size_t)tri + 1);
+            // emission (one-sided, outward side)
+            if (sh1.x + sh1.y + sh1.z > 0.0f) {
+                f3 out = norm3(outward);
+                float cosl = dot3(out, wo);
+                if (cosl > 0) {
+                    float w = 1.0f;
+                    if (!(p3.y & 1) && S.emissive_total > 0) {
+                        float area = tri_area(v);
+                        float pl = ((sh1.x + sh1.y + sh1.z) * area) / S.emissive_total / area;
+                        float pls = pl * (t * t * sqr3(d)) / cosl;
+                        w = mis2(p2.w, pls);
+                    }
+                    accum_add(A.accum, slot, mkc(thr.r * sh1.x * w, thr.g * sh1.y * w, thr.b * sh1.z * w));
+                }
+            }
+            if (b < A.max_bounces) {
+                int mt = __float_as_int(sh1.w);
+                c3 alb = mkc(sh0.x, sh0.y, sh0.z);
+                float alpha = fmaxf(sh0.w, 1e-3f);
+                if (mt != DR_MAT_MIRROR && S.n_emissive > 0) {
+                    float u = rnd(key, (uint32_t)b, 3) * S.emissive_total;
+                    int lo = 0, hi = S.n_emissive - 1;
+                    while (lo < hi) {
+                        int mid = (lo + hi) >> 1;
+                        if (__ldg(S.emissive_cdf + mid) < u) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    int li = __ldg(S.emissive + lo);
+                    float u1 = rnd(key, (uint32_t)b, 4), u2 = rnd(key, (uint32_t)b, 5);
+                    float su = sqrtf(u1);
+                    float ba = 1.0f - su, bb = u2 * su;
+                    TriV lt = load_tri(S.tris, li);
+                    f3 lp = add3(add3(mul3(lt.a, ba), mul3(lt.b, bb)), mul3(lt.c, 1.0f - ba - bb));
+                    f3 ldv = sub3(lp, hp);
+                    float dist2 = sqr3(ldv);
+                    f3 wi = mul3(ldv, 1.0f / sqrtf(dist2));
+                    f3 lout = norm3(tri_normal(lt));
+                    float cosl = -dot3(lout, wi);
+                    float cosi = dot3(ng, wi);
+                    if (cosl > 0 && cosi > 0) {
+                        float4 le = __ldg(S.shade + 2 * (size_t)li + 1);
+                        float area = tri_area(lt);
+                        float pl = ((le.x + le.y + le.z) * area) / S.emissive_total / area;
+                        float pls = pl * dist2 / cosl;
+                        c3 f;
+                        float pb;
+                        if (mt == DR_MAT_GLOSSY) {
+                            f3 h = norm3(add3(wi, wo));
+                            float ndh = dot3(ng, h), ndo = dot3(ng, wo);
+                            float D = ggx_d(ndh, alpha);
+                            float G = ggx_g1(ndo, alpha) * ggx_g1(cosi, alpha);
+                            float spec = D * G / (4.0f * ndo * cosi);
+                            f = cscale(alb, spec);
+                            pb = D * ndh / (4.0f * fabsf(dot3(wo, h)));
+                        } else {
+                            f = cscale(alb, 1.0f / 3.14159265358979f);
+                            pb = cosi / 3.14159265358979f;
+                        }
+                        float w = mis2(pls, pb);
+                        float k = cosi / pls * w;
+                        scontrib = mkc(thr.r * f.r * le.x * k, thr.g * f.g * le.y * k, thr.b * f.b * le.z * k);
+                        emit_shadow = (scontrib.r + scontrib.g + scontrib.b) > 0.0f;
+                        sdir = ldv;
+                        light_tri = li;
+                    }
+                }
+                float u1 = rnd(key, (uint32_t)b, 1), u2 = rnd(key, (uint32_t)b, 2);
+                f3 T, B;
+                onb(ng, T, B);
+                child = true;
+                if (mt == DR_MAT_MIRROR) {
+                    nd = sub3(d, mul3(ng, 2.0f * dot3(d, ng)));
+                    thr = cmul(thr, alb);
+                    new_delta = 1;
+                    new_pdf = 0.0f;
+                } else if (mt == DR_MAT_GLOSSY) {
+                    float phi = 2.0f * 3.14159265358979f * u1;
+                    float ct = sqrtf((1.0f - u2) / (1.0f + (alpha * alpha - 1.0f) * u2));
+                    float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+                    f3 h = add3(add3(mul3(T, st * cosf(phi)), mul3(B, st * sinf(phi))), mul3(ng, ct));
+                    nd = sub3(mul3(h, 2.0f * dot3(wo, h)), wo);
+                    float cosi = dot3(ng, nd);
+                    if (cosi <= 0) child = false;
+                    else {
+                        float ndo = dot3(ng, wo);
+                        float G = ggx_g1(ndo, alpha) * ggx_g1(cosi, alpha);
+                        float wgt = G * fabsf(dot3(wo, h)) / (ndo * ct);
+                        thr = cscale(cmul(thr, alb), wgt);
+                        new_pdf = ggx_d(ct, alpha) * ct / (4.0f * fabsf(dot3(wo, h)));
+                        new_delta = 0;
+                    }
+                } else {
+                    float r = sqrtf(u1), phi = 2.0f * 3.14159265358979f * u2;
+                    float z = sqrtf(fmaxf(0.0f, 1.0f - u1));
+                    nd = add3(add3(mul3(T, r * cosf(phi)), mul3(B, r * sinf(phi))), mul3(ng, z));
+                    thr = cmul(thr, alb);
+                    new_pdf = z / 3.14159265358979f;
+                    new_delta = 0;
+                }
+                if (child) nd = norm3(nd);
+            }
+        }
+        int ws = warp_alloc(&C->shadow_count[b], emit_shadow);
+        if (emit_shadow) {
+            A.sq.s0[ws] = make_float4(hp.x, hp.y, hp.z, __int_as_float(slot));
+            A.sq.s1[ws] = make_float4(sdir.x, sdir.y, sdir.z, __int_as_float(light_tri));
+            A.sq.s2[ws] = make_float4(0.f, 0.f, 0.f, __int_as_float(tri));
+            A.sq.s4[ws] = make_float4(scontrib.r, scontrib.g, scontrib.b, 0.0f);
+        }
+        int w = warp_alloc(&C->ray_count[b + 1], child);
+        if (child) {
+            N.p0[w] = make_float4(hp.x, hp.y, hp.z, p0.w);
+            N.p1[w] = make_float4(nd.x, nd.y, nd.z, p1.w);
+            N.p2[w] = make_float4(thr.r, thr.g, thr.b, new_pdf);
+            N.p3[w] = make_int4(tri, new_delta, p3.z, 0);
+        }
+    }
+}
+
+// Physical visibility: closest hit from the shading point toward the light point (segment
+// length 1 in units of the direction), ignoring the shading triangle; visible if nothing but
+// the light triangle is hit before t = 0.999.
+__global__ void __launch_bounds__(256) k_shadow_phys(WaveArgs A, int b) {
+    Ctrl *C = A.ctrl;
+    const int n = *((volatile int *)&C->shadow_count[b]);
+    for (;;) {
+        int base = warp_fetch(&C->fetch_shadow[b]);
+        if (base >= n) break;
+        int i = base + (int)lane_id();
+        if (i < n) {
+            float4 s0 = A.sq.s0[i], s1 = A.sq.s1[i], s2 = A.sq.s2[i], s4 = A.sq.s4[i];
+            Hit h;
+            int nb = 0, nt = 0;
+            cast_closest<false>(A.S, f3of(s0), f3of(s1), false, __float_as_int(s2.w), h, nb, nt);
+            bool vis = (h.tri < 0) || (h.tri == __float_as_int(s1.w)) || !(h.t < 0.999f);
+            if (vis) accum_add(A.accum, __float_as_int(s0.w), mkc(s4.x, s4.y, s4.z));
+        }
+    }
+}
+
+// Accumulators -> frame buffer: set (blend >= 1) or blend like blendBlockPixelColor.
+__global__ void k_resolve(const float *__restrict__ accum, float4 *__restrict__ fb, int start_block, int n_slots, int width,
+                          int height, float inv_spp, float blend) {
+    int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= n_slots) return;
+    int blk = start_block + slot / (DR_BLOCK_W * DR_BLOCK_H);
+    int pid = slot % (DR_BLOCK_W * DR_BLOCK_H);
+    int bw = (width + DR_BLOCK_W - 1) / DR_BLOCK_W;
+    int by = blk / bw, bx = blk - by * bw;
+    int x = bx * DR_BLOCK_W + (pid % DR_BLOCK_W), y = by * DR_BLOCK_H + pid / DR_BLOCK_W;
+    if (x >= width || y >= height) return;
+    float4 a = reinterpret_cast<const float4 *>(accum)[slot];
+    float4 c = make_float4(a.x * inv_spp, a.y * inv_spp, a.z * inv_spp, 1.0f);
+    size_t at = (size_t)blk * (DR_BLOCK_W * DR_BLOCK_H) + pid;
+    if (blend >= 1.0f) fb[at] = c;
+    else {
+        float4 old = fb[at];
+        fb[at] = make_float4((c.x * blend) + (old.x * (1.0f - blend)), (c.y * blend) + (old.y * (1.0f - blend)),
+                             (c.z * blend) + (old.z * (1.0f - blend)), (c.w * blend) + (old.w * (1.0f - blend)));
+    }
+}
+
+}  // namespace drd
+
+// ---------------------------------------------------------------------------------------------
+// Host launchers
+namespace drk {
+
+using namespace drd;
+
+static int g_sms = 0;
+static int sm_count() {
+    if (g_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 148;
+    }
+    return g_sms;
+}
+
+cudaError_t launch_cast(const Scene &S, const float *o, const float *d, const int *ignore, int n, int clip, int *hit_tri,
+                        float *hit_t, int *nbox, int *ntri, cudaStream_t stream, long long *launches) {
+    if (n <= 0) return cudaSuccess;
+    int threads = 128;
+    int blocks = (n + threads - 1) / threads;
+    if (nbox || ntri)
+        k_cast<true><<<blocks, threads, 0, stream>>>(S, o, d, ignore, n, clip, hit_tri, hit_t, nbox, ntri);
+    else
+        k_cast<false><<<blocks, threads, 0, stream>>>(S, o, d, ignore, n, clip, hit_tri, hit_t, nullptr, nullptr);
+    if (launches) (*launches)++;
+    return cudaGetLastError();
+}
+
+size_t ctrl_bytes() { return sizeof(Ctrl); }
+
+cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launches) {
+    WaveArgs A;
+    A.S = W.scene;
+    A.cam = W.camera;
+    A.cam_x = W.cam_x;
+    A.mode = W.mode;
+    A.width = W.width;
+    A.height = W.height;
+    A.fsaa_x = W.fsaa_x;
+    A.fsaa_y = W.fsaa_y;
+    A.spp = W.spp;
+    A.max_bounces = W.max_bounces;
+    A.clip = W.clip;
+    A.pixel_size = W.pixel_size;
+    A.pdx = W.pdx;
+    A.pdy = W.pdy;
+    A.seed = W.seed;
+    A.sample_base = W.sample_base;
+    A.start_block = W.start_block;
+    A.n_slots = W.n_slots;
+    A.wave_begin = W.wave_begin;
+    A.wave_count = W.wave_count;
+    for (int k = 0; k < 2; k++) {
+        A.q[k].p0 = W.q_p0[k];
+        A.q[k].p1 = W.q_p1[k];
+        A.q[k].p2 = W.q_p2[k];
+        A.q[k].p3 = W.q_p3[k];
+    }
+    A.hits = W.hits;
+    A.sq.s0 = W.s[0];
+    A.sq.s1 = W.s[1];
+    A.sq.s2 = W.s[2];
+    A.sq.s3 = W.s[3];
+    A.sq.s4 = W.s[4];
+    A.accum = W.accum;
+    A.ctrl = reinterpret_cast<Ctrl *>(W.ctrl);
+    cudaError_t e = cudaMemsetAsync(W.ctrl, 0, sizeof(Ctrl), stream);
+    if (e != cudaSuccess) return e;
+    const int grid = sm_count() * 8;
+    long long nl = 0;
+    k_camera<<<grid, 256, 0, stream>>>(A);
+    nl++;
+    for (int b = 0; b <= W.max_bounces; b++) {
+        k_trace<<<grid, 256, 0, stream>>>(A, b);
+        if (W.mode == DR_MODE_REFERENCE) {
+            k_shade_ref<<<grid, 256, 0, stream>>>(A, b);
+            k_shadow_ref<<<grid, 256, 0, stream>>>(A, b);
+        } else {
+            k_shade_phys<<<grid, 256, 0, stream>>>(A, b);
+            k_shadow_phys<<<grid, 256, 0, stream>>>(A, b);
+        }
+        nl += 3;
+    }
+    if (launches) *launches += nl;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resolve(const float *accum, float *fb, int start_block, int n_slots, int width, int height, float inv_spp,
+                           float blend, cudaStream_t stream, long long *launches) {
+    int threads = 256;
+    int blocks = (n_slots + threads - 1) / threads;
+    k_resolve<<<blocks, threads, 0, stream>>>(accum, reinterpret_cast<float4 *>(fb), start_block, n_slots, width, height,
+                                             inv_spp, blend);
+    if (launches) (*launches)++;
+    return cudaGetLastError();
+}
+
+}  // namespace drk

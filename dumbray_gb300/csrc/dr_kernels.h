@@ -1,0 +1,41 @@
+// dr_kernels.h - host-visible launch interface of the device kernels (no torch types).
+#pragma once
+#include <cuda_runtime.h>
+#include "../../include/dr_api.h"
+#include "dr_device.cuh"
+
+namespace drd {
+constexpr int kMaxBounceSlots = 68;  // bounce limit 64 (DUMB_RENDERER_BOUNCE_LIMIT) + camera + spare
+}
+
+namespace drk {
+
+// One wave of the wavefront renderer: paths [wave_begin, wave_begin + wave_count) of the
+// (sample-major, block-major pixel slot) path space of one dr_render_blocks call.
+struct WaveDesc {
+    drd::Scene scene;
+    dr_camera camera;
+    float cam_x;
+    int mode, width, height, fsaa_x, fsaa_y, spp, max_bounces, clip;
+    float pixel_size, pdx, pdy;
+    uint32_t seed, sample_base;
+    int start_block, n_slots;
+    long long wave_begin;
+    int wave_count;
+    float4 *q_p0[2], *q_p1[2], *q_p2[2];
+    int4 *q_p3[2];
+    float2 *hits;
+    float4 *s[5];
+    float *accum;
+    void *ctrl;
+};
+
+size_t ctrl_bytes();
+
+cudaError_t launch_cast(const drd::Scene &S, const float *o, const float *d, const int *ignore, int n, int clip, int *hit_tri,
+                        float *hit_t, int *nbox, int *ntri, cudaStream_t stream, long long *launches);
+cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launches);
+cudaError_t launch_resolve(const float *accum, float *fb, int start_block, int n_slots, int width, int height, float inv_spp,
+                           float blend, cudaStream_t stream, long long *launches);
+
+}  // namespace drk

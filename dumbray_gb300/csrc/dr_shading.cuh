@@ -1,0 +1,241 @@
+// dr_shading.cuh - device shading models.
+//
+// Reference semantics (DR_MODE_REFERENCE): DumbBasedShader and SimpleStochasticShader
+// (__source__/DataStructures/Objects/Components/Shaders/DumbBasedShader/DumbBasedShader.impl.cuh:18-122,
+//  .../SimpleStochasticShader/SimpleStochasticShader.impl.cuh:13-37), the three analytic lights
+// (.../Scene/Lights/*: SphericalLightEmitter.impl.cuh:10-18, SimpleSoftDirectionalLight.impl.cuh:12-19,
+//  SimpleDirectionalLight.impl.cuh:13-16) and lenses (.../Components/Lenses/*).  getReflectedColor is
+// linear in the photon colour, so every function here returns the colour FACTOR and callers multiply.
+// Physical semantics (DR_MODE_PHYSICAL): Lambert / mirror / GGX glossy with emissive triangles.
+#pragma once
+#include "dr_device.cuh"
+
+namespace drd {
+
+struct c3 {
+    float r, g, b;
+};
+__device__ __forceinline__ c3 mkc(float r, float g, float b) { return c3{r, g, b}; }
+__device__ __forceinline__ c3 cmul(c3 a, c3 b) { return c3{a.r * b.r, a.g * b.g, a.b * b.b}; }
+__device__ __forceinline__ c3 cscale(c3 a, float f) { return c3{a.r * f, a.g * f, a.b * f}; }
+__device__ __forceinline__ c3 cadd(c3 a, c3 b) { return c3{a.r + b.r, a.g + b.g, a.b + b.b}; }
+
+// plain float3 helpers (shading only; contraction is disabled for the whole library)
+__device__ __forceinline__ f3 add3(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 sub3(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 mul3(f3 a, float f) { return f3{a.x * f, a.y * f, a.z * f}; }
+__device__ __forceinline__ f3 neg3(f3 a) { return f3{-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 cross3(f3 a, f3 v) { return f3{a.y * v.z - v.y * a.z, v.x * a.z - a.x * v.z, a.x * v.y - v.x * a.y}; }
+__device__ __forceinline__ float sqr3(f3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+__device__ __forceinline__ f3 norm3(f3 a) { float im = 1.0f / sqrtf(a.x * a.x + a.y * a.y + a.z * a.z); return f3{a.x * im, a.y * im, a.z * im}; }
+__device__ __forceinline__ f3 divf3(f3 a, float f) { float fi = 1.0f / f; return f3{a.x * fi, a.y * fi, a.z * fi}; }
+__device__ __forceinline__ f3 reflect3(f3 v, f3 n) { float m = (2.0f * dot3(v, n) / sqr3(n)); return f3{v.x - n.x * m, v.y - n.y * m, v.z - n.z * m}; }
+__device__ __forceinline__ f3 normal_on3(f3 a, f3 v) { return mul3(v, dot3(a, v) / sqr3(v)); }
+
+struct TriV {
+    f3 a, b, c;
+};
+__device__ __forceinline__ TriV load_tri(const float4 *p, int i) {
+    float4 A = __ldg(p + 3 * (size_t)i), B = __ldg(p + 3 * (size_t)i + 1), C = __ldg(p + 3 * (size_t)i + 2);
+    return TriV{f3of(A), f3of(B), f3of(C)};
+}
+// Triangle::normal() = (c - a) x (b - a)
+__device__ __forceinline__ f3 tri_normal(const TriV &t) { return cross3(sub3(t.c, t.a), sub3(t.b, t.a)); }
+
+// Triangle::getMasses (Triangle.impl.h:248-276)
+__device__ inline f3 get_masses(const TriV &t, f3 center) {
+    f3 ab = sub3(t.b, t.a);
+    f3 bc = sub3(t.c, t.b);
+    f3 ae = sub3(ab, normal_on3(ab, bc));
+    f3 ax = sub3(center, t.a);
+    f3 ad = normal_on3(ax, ae);
+    if (ae.x < 0) { ad.x = -ad.x; ae.x = -ae.x; }
+    if (ae.y < 0) { ad.y = -ad.y; ae.y = -ae.y; }
+    if (ae.z < 0) { ad.z = -ad.z; ae.z = -ae.z; }
+    float div = ad.x + ad.y + ad.z;
+    if (div == 0) return f3{1, 0, 0};
+    float g = (ae.x + ae.y + ae.z) / div;
+    float tt;
+    f3 by = sub3(add3(t.a, mul3(ax, g)), t.b);
+    if (bc.x < 0) { bc.x = -bc.x; by.x = -by.x; }
+    if (bc.y < 0) { bc.y = -bc.y; by.y = -by.y; }
+    if (bc.z < 0) { bc.z = -bc.z; by.z = -by.z; }
+    div = bc.x + bc.y + bc.z;
+    tt = (div == 0) ? 0.0f : (by.x + by.y + by.z) / div;
+    float cc = tt, bb = (1 - tt), aa = (g - 1);
+    return divf3(f3{aa, bb, cc}, aa + bb + cc);
+}
+__device__ __forceinline__ f3 mass_center(const TriV &t, f3 m) { return add3(add3(mul3(t.a, m.x), mul3(t.b, m.y)), mul3(t.c, m.z)); }
+
+// DumbRand::pointOnSphere from two uniforms (DumbRand.impl.cuh:70-77)
+__device__ __forceinline__ f3 point_on_sphere(float u0, float u1, float radius) {
+    float theta = (2.0f * 3.14159265359f * u0);
+    float cosPhi = (1.0f - (2.0f * u1));
+    float sinPhi = sqrtf(1.0f - (cosPhi * cosPhi));
+    return f3{(sinPhi * cosf(theta)) * radius, (sinPhi * sinf(theta)) * radius, cosPhi * radius};
+}
+
+// ---- DumbBasedShader -------------------------------------------------------------------------
+__device__ inline bool dumb_based_request(const Material &m, const TriV &v, const TriV &nt, f3 hit, f3 raydir, uint32_t key,
+                                          uint32_t bounce, f3 &dir, int &type) {
+    f3 normal = norm3(tri_normal(v));
+    f3 masses = get_masses(v, hit);
+    float metal = fmaxf(fminf(m.metal, 1.0f), 0.0f);
+    if (rnd(key, bounce, 0) <= metal) {
+        f3 n = norm3(mass_center(nt, masses));
+        if (dot3(n, raydir) >= 0.0f) return false;
+        f3 r = norm3(reflect3(raydir, n));
+        if (dot3(r, normal) < 0) normal = mul3(normal, -1.0f);
+        f3 a = cross3(r, f3{1.0f, 0.0f, 0.0f});
+        if (sqr3(normal) < kEps) a = cross3(r, f3{0.0f, 1.0f, 0.0f});
+        a = norm3(a);
+        f3 b = cross3(r, a);
+        f3 sd = f3{0, 0, 0};
+        for (int tries = 0; tries < 32; tries++) {
+            float cosine = powf(rnd(key, bounce, 8 + 2 * tries), 1.0f / m.specular);
+            float sinus = sqrtf(1.0f - (cosine * cosine));
+            float angle = (rnd(key, bounce, 9 + 2 * tries) * 2.0f * 3.14159265359f);
+            float angleCos = cosf(angle);
+            float angleSin = sqrtf(1.0f - (angleCos * angleCos));
+            sd = add3(mul3(r, cosine), mul3(add3(mul3(a, angleCos), mul3(b, angleSin)), sinus));
+            if (dot3(sd, normal) >= 0.0f) break;
+        }
+        dir = sd;
+        type = 1;
+        return true;
+    }
+    f3 sd = point_on_sphere(rnd(key, bounce, 1), rnd(key, bounce, 2), 1.0f);
+    if (dot3(sd, normal) < 0.0f) sd = mul3(sd, -1.0f);
+    dir = sd;
+    type = 2;
+    return true;
+}
+
+__device__ inline c3 dumb_based_reflect(const Material &m, const TriV &v, const TriV &nt, f3 hit, f3 photon_dir, f3 observer,
+                                        bool direct, int sample_type) {
+    f3 masses = get_masses(v, hit);
+    if (dot3(norm3(tri_normal(v)), photon_dir) > 0.0f)
+        if (!direct) return mkc(1, 1, 1);
+    if (dot3(mass_center(nt, masses), observer) < 0.0f) return mkc(0, 0, 0);
+    f3 n = norm3(mass_center(nt, masses));
+    f3 wi = neg3(norm3(photon_dir));
+    float metal = fmaxf(fminf(m.metal, 1.0f), 0.0f);
+    float spec = m.specular;
+    c3 brdf = mkc(0, 0, 0);
+    bool brdfMatters = (direct || sample_type == 1);
+    if (brdfMatters) {
+        f3 w0 = norm3(observer);
+        f3 wh = norm3(add3(w0, wi));
+        float val = (1.0f - dot3(wh, wi));
+        float sq = val * val;
+        float f5 = sq * sq * val;
+        c3 fwi = mkc(m.fresnel[0] + (1 - m.fresnel[0]) * f5, m.fresnel[1] + (1 - m.fresnel[1]) * f5,
+                     m.fresnel[2] + (1 - m.fresnel[2]) * f5);
+        float multiplier;
+        if (direct) {
+            float dwh = ((spec + 2) / (2.0f * 3.14159265359f)) * powf(dot3(n, wh), spec);
+            float gwiw0 = fminf(1.0f, fminf(2.0f * dot3(n, wh) * dot3(n, w0) / dot3(w0, wh),
+                                            2.0f * dot3(n, wh) * dot3(n, wi) / dot3(w0, wh)));
+            multiplier = (dwh * gwiw0) / (4.0f * dot3(n, w0) * dot3(n, wi));
+        } else multiplier = 1.0f;
+        c3 bb = cscale(fwi, multiplier);
+        brdf = mkc(fmaxf(0.0f, fminf(bb.r, 1.0f)), fmaxf(0.0f, fminf(bb.g, 1.0f)), fmaxf(0.0f, fminf(bb.b, 1.0f)));
+    }
+    bool diffuseMatters = (direct || sample_type == 2);
+    c3 diff = cscale(mkc(m.color[0], m.color[1], m.color[2]), 1.0f - metal);
+    c3 diffuse = diffuseMatters ? cscale(diff, dot3(n, wi)) : mkc(0, 0, 0);
+    if (brdfMatters && diffuseMatters)
+        return mkc(fmaxf(0.0f, fminf((brdf.r * metal) + diffuse.r, 1.0f)), fmaxf(0.0f, fminf((brdf.g * metal) + diffuse.g, 1.0f)),
+                   fmaxf(0.0f, fminf((brdf.b * metal) + diffuse.b, 1.0f)));
+    if (brdfMatters) return brdf;
+    return cscale(diffuse, 1.0f / (1.0f - metal));
+}
+
+// ---- SimpleStochasticShader ------------------------------------------------------------------
+__device__ __forceinline__ void ss_params(const Material &m, float &diff, float &gloss) {
+    float total = m.diffuse + m.smoothness;
+    float mul = ((total > 1.0f) ? (1.0f / total) : 1.0f);
+    diff = m.diffuse * mul;
+    gloss = m.smoothness * mul;
+}
+__device__ inline f3 ss_request(const Material &m, const TriV &v, const TriV &nt, f3 hit, f3 raydir, uint32_t key, uint32_t bounce) {
+    float diff, gloss;
+    ss_params(m, diff, gloss);
+    f3 direction = point_on_sphere(rnd(key, bounce, 1), rnd(key, bounce, 2), 1.0f);
+    if (dot3(direction, tri_normal(v)) < 0) direction = neg3(direction);
+    f3 hn = mass_center(nt, get_masses(v, hit));
+    f3 refl = reflect3(raydir, hn);
+    return norm3(add3(mul3(direction, diff), mul3(refl, gloss)));
+}
+__device__ inline c3 ss_reflect(const Material &m, const TriV &v, const TriV &nt, f3 hit, f3 photon_dir, f3 observer) {
+    float diff, gloss;
+    ss_params(m, diff, gloss);
+    f3 hn = mass_center(nt, get_masses(v, hit));
+    f3 refl = reflect3(photon_dir, hn);
+    float rc = dot3(refl, hn) / sqrtf(sqr3(refl) * sqr3(hn));
+    if (rc < 0.0f) rc = 0.0f;
+    float oc = dot3(observer, refl) / sqrtf(sqr3(observer) * sqr3(refl));
+    if (oc < 0.0f) oc = 0.0f;
+    return cscale(mkc(m.color[0], m.color[1], m.color[2]), (diff * rc) + (gloss * powf(oc, m.shininess)));
+}
+
+// Material::getReflectedColor dispatch (colour factor).
+__device__ inline c3 ref_reflect(const Scene &S, int tri, f3 hit, f3 photon_dir, f3 observer, bool direct, int sample_type) {
+    const Material &m = S.mats[__ldg(S.mat_id + tri)];
+    TriV v = load_tri(S.tris, tri), nt = load_tri(S.nrms, tri);
+    if (m.type == 0) return dumb_based_reflect(m, v, nt, hit, photon_dir, observer, direct, sample_type);
+    return ss_reflect(m, v, nt, hit, photon_dir, observer);
+}
+
+// Light::getVertexPhotons (photon origin, direction, colour) for light `li`.
+__device__ inline void light_photon(const Light &l, f3 point, uint32_t key, uint32_t bounce, int li, f3 &o, f3 &d, c3 &c) {
+    uint32_t d0 = 72 + 3 * (uint32_t)li;
+    if (l.type == 0) {
+        f3 ep = point_on_sphere(rnd(key, bounce, d0), rnd(key, bounce, d0 + 1), l.radius);
+        ep = mul3(ep, rnd(key, bounce, d0 + 2));
+        ep = add3(ep, f3{l.position[0], l.position[1], l.position[2]});
+        f3 delta = sub3(point, ep);
+        o = ep;
+        d = norm3(delta);
+        float inv = 1.0f / sqr3(delta);
+        c = mkc(l.color[0] * inv, l.color[1] * inv, l.color[2] * inv);
+    } else if (l.type == 1) {
+        f3 dir = norm3(f3{l.direction[0], l.direction[1], l.direction[2]});
+        float soft = l.distance * l.softness;
+        float rad = soft * rnd(key, bounce, d0);
+        f3 off = point_on_sphere(rnd(key, bounce, d0 + 1), rnd(key, bounce, d0 + 2), rad);
+        f3 origin = add3(sub3(point, mul3(dir, l.distance)), off);
+        o = origin;
+        d = sub3(point, origin);
+        c = mkc(l.color[0], l.color[1], l.color[2]);
+    } else {
+        f3 dir = norm3(f3{l.direction[0], l.direction[1], l.direction[2]});
+        o = sub3(point, mul3(dir, l.distance));
+        d = dir;
+        c = mkc(l.color[0], l.color[1], l.color[2]);
+    }
+}
+
+// ---- physical mode ---------------------------------------------------------------------------
+__device__ __forceinline__ void onb(f3 n, f3 &t, f3 &b) {
+    float s = n.z >= 0 ? 1.0f : -1.0f;
+    float a = -1.0f / (s + n.z);
+    float bb = n.x * n.y * a;
+    t = f3{1.0f + s * n.x * n.x * a, s * bb, -s * n.x};
+    b = f3{bb, s + n.y * n.y * a, -n.y};
+}
+__device__ __forceinline__ float ggx_d(float ndh, float a) {
+    float a2 = a * a;
+    float c2 = ndh * ndh;
+    float den = c2 * (a2 - 1.0f) + 1.0f;
+    return a2 / (3.14159265358979f * den * den);
+}
+__device__ __forceinline__ float ggx_g1(float ndv, float a) {
+    float a2 = a * a;
+    return 2.0f * ndv / (ndv + sqrtf(a2 + (1.0f - a2) * ndv * ndv));
+}
+__device__ __forceinline__ float mis2(float a, float b) { return (a * a) / (a * a + b * b); }
+__device__ __forceinline__ float tri_area(const TriV &t) { return 0.5f * sqrtf(sqr3(cross3(sub3(t.b, t.a), sub3(t.c, t.a)))); }
+
+}  // namespace drd

@@ -1,0 +1,248 @@
+/*
+ * dr_api.h - C ABI of the GB300-native DumbRay rendering hot path.
+ *
+ * Drop-in boundary: this library replaces the per-pixel path tracer that DumbRay plugs under its
+ * block renderer, i.e. the pair of virtuals
+ *     BlockRenderer::renderBlocksCPU / renderBlocksGPU
+ *       (__source__/DataStructures/Renderers/BlockRenderer/BlockRenderer.cuh:43-44)
+ * implemented by DumbRenderer (__source__/DataStructures/Renderers/DumbRenderer/DumbRenderer.cu:52-113),
+ * together with the function packs that path calls: Octree cast, Shader, Lense, Light and the
+ * block-based frame buffer.  Every entry point is extern "C", takes plain pointers and sizes, and
+ * returns a dr_status; there is no CPU fallback.  Device pointers are CUDA device memory owned by
+ * the caller unless stated otherwise; `stream` is a cudaStream_t passed as void*.
+ *
+ * Threading: a dr_scene is immutable after creation and may be shared by any number of threads.
+ * A dr_renderer owns per-caller scratch (wavefront queues) and must be used by one thread / one
+ * stream at a time, mirroring the reference's one DeviceBlockManager per GPU worker thread
+ * (__source__/DataStructures/Screen/FrameBuffer/FrameBuffer.impl.cuh:271-317).
+ */
+#ifndef DR_API_H
+#define DR_API_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t dr_status;
+#define DR_OK 0
+#define DR_E_ARG 1       /* invalid argument (null pointer, bad size, bad enum) */
+#define DR_E_CUDA 2      /* a CUDA runtime call failed; see dr_last_error() */
+#define DR_E_CAPACITY 3  /* a caller-provided capacity is too small */
+#define DR_E_TIMEOUT 4   /* a bounded device-side wait gave up */
+#define DR_E_NOMEM 5     /* host or device allocation failed */
+#define DR_E_STATE 6     /* object used in a state that does not allow the call */
+
+typedef struct dr_scene dr_scene;
+typedef struct dr_renderer dr_renderer;
+
+/* ---- octree build parameters -------------------------------------------------------------
+ * Octree.cuh:10-13: OCTREE_MAX_DEPTH 24, OCTREE_POLYCOUNT_TO_SPLIT_NODE 8.  Zero fields take
+ * those defaults; threads = 0 uses every host core. */
+typedef struct {
+    int32_t max_depth;
+    int32_t split_threshold;
+    int32_t threads;
+    int32_t reserved;
+} dr_build_params;
+
+/* ---- materials --------------------------------------------------------------------------
+ * Reference-semantics shaders (Material<BakedTriFace> function packs):
+ *   DR_MAT_DUMB_BASED        DumbBasedShader(fresnel, specular, diffuse=color, metal)
+ *                            (__source__/.../Shaders/DumbBasedShader/DumbBasedShader.impl.cuh:5-122)
+ *   DR_MAT_SIMPLE_STOCHASTIC SimpleStochasticShader(albedo=color, diffuse, smoothness, shininess)
+ *                            (__source__/.../Shaders/SimpleStochasticShader/SimpleStochasticShader.impl.cuh:4-37)
+ * Physical-mode materials (no reference counterpart; albedo = color, overridable per triangle):
+ *   DR_MAT_LAMBERT, DR_MAT_MIRROR, DR_MAT_GLOSSY (GGX, alpha = roughness). */
+#define DR_MAT_DUMB_BASED 0
+#define DR_MAT_SIMPLE_STOCHASTIC 1
+#define DR_MAT_LAMBERT 2
+#define DR_MAT_MIRROR 3
+#define DR_MAT_GLOSSY 4
+
+typedef struct {
+    int32_t type;
+    float color[3];
+    float fresnel[3];
+    float specular;
+    float metal;
+    float diffuse;
+    float smoothness;
+    float shininess;
+    float roughness;
+    float emission[3];
+} dr_material;
+
+/* ---- lights (reference semantics; Light function pack, Light.cuh:14-59) -----------------
+ *   DR_LIGHT_SPHERICAL         SphericalLightEmitter(color, position, radius)
+ *   DR_LIGHT_SOFT_DIRECTIONAL  SimpleSoftDirectionalLight(color, direction, distance, softness)
+ *   DR_LIGHT_DIRECTIONAL       SimpleDirectionalLight(color, direction, distance) */
+#define DR_LIGHT_SPHERICAL 0
+#define DR_LIGHT_SOFT_DIRECTIONAL 1
+#define DR_LIGHT_DIRECTIONAL 2
+
+typedef struct {
+    int32_t type;
+    float color[3];
+    float position[3];
+    float direction[3];
+    float radius;
+    float distance;
+    float softness;
+} dr_light;
+
+/* ---- camera / lenses (Lense function pack, Lense.cuh:46-82; Camera.impl.cuh:7-14) --------
+ *   DR_LENS_DEFAULT_PERSPECTIVE  DefaultPerspectiveLense(angle[0])   (normalised pinhole)
+ *   DR_LENS_SIMPLE_STOCHASTIC    SimpleStochasticLense(angle[0])     (jittered, unnormalised)
+ *   DR_LENS_SPHERICAL_SEGMENT    Lenses::SphericalSegmentLense(angle, focal_distance, softness, filter)
+ * Physical mode only:
+ *   DR_LENS_PINHOLE   jittered pinhole, vertical fov angle[0]
+ *   DR_LENS_FISHEYE   equidistant fisheye, angle[0] = full field of view across the image height
+ *   DR_LENS_SPHERICAL latitude/longitude, angle[0] x angle[1] degrees per unit screen space
+ * Camera space is +x right, +y up, +z forward; world direction = x*right + y*up + z*forward,
+ * origin = position + (lens origin expressed in the same basis). */
+#define DR_LENS_DEFAULT_PERSPECTIVE 0
+#define DR_LENS_SIMPLE_STOCHASTIC 1
+#define DR_LENS_SPHERICAL_SEGMENT 2
+#define DR_LENS_PINHOLE 3
+#define DR_LENS_FISHEYE 4
+#define DR_LENS_SPHERICAL 5
+
+typedef struct {
+    int32_t lens;
+    float angle[2];
+    float focal_distance;
+    float softness;
+    float filter[3];
+    float position[3];
+    float right[3];
+    float up[3];
+    float forward[3];
+} dr_camera;
+
+/* ---- render parameters ---------------------------------------------------------------------
+ * DR_MODE_REFERENCE: DumbRenderer's estimator (DumbRenderer.cu:174-443): fsaa samples_x x
+ *   samples_y sub-pixels, max_bounces indirect layers, analytic-light NEE cast from the light
+ *   toward the point, backface culling flag, HEIGHT/WIDTH/MIN/MAX boxing (DumbRenderer.cu:190-200).
+ * DR_MODE_PHYSICAL: unbiased path tracer over emissive triangles with Lambert/mirror/GGX,
+ *   samples_x*samples_y jittered samples per pixel, max_bounces = path depth.
+ * iteration: 1-based progressive index; blend = (iteration <= 1) ? 1 : 1/iteration
+ *   (DumbRenderer.cu:64,102).  Random numbers are counter-based, keyed by
+ *   (seed, pixel, sample, bounce, dimension), so any sample is reproducible. */
+#define DR_MODE_REFERENCE 0
+#define DR_MODE_PHYSICAL 1
+
+#define DR_BOXING_HEIGHT 0
+#define DR_BOXING_WIDTH 1
+#define DR_BOXING_MIN 2
+#define DR_BOXING_MAX 3
+
+typedef struct {
+    int32_t mode;
+    int32_t width;
+    int32_t height;
+    int32_t samples_x;
+    int32_t samples_y;
+    int32_t max_bounces;
+    int32_t cull_backfaces;
+    int32_t boxing;
+    int32_t iteration;
+    uint32_t seed;
+} dr_render_params;
+
+/* Frame buffer: BlockBasedFrameBuffer<8,16> layout (BlockBasedFrameBuffer.cuh:91,
+ * BlockBasedFrameBuffer.impl.cuh:108-156): float4 data[128*blockId + pixelId],
+ * blockId = by*ceil(W/8) + bx, pixelId = oy*8 + ox. */
+#define DR_BLOCK_W 8
+#define DR_BLOCK_H 16
+
+/* ---- library ------------------------------------------------------------------------------ */
+
+/* Message of the last failing call on this thread (never NULL). */
+const char *dr_last_error(void);
+
+/* Library / ABI version (major*10000 + minor*100 + patch). */
+int32_t dr_version(void);
+
+/* ---- host octree (no device work) ----------------------------------------------------------
+ * The octree alone, built on the host with the reference's split rule (Octree.impl.cuh:97-129,
+ * 339-533) and kept in host memory, e.g. to inspect or cache it.  Export layout is the same as
+ * dr_scene_export_tree (node 0 = root). */
+typedef struct dr_octree dr_octree;
+dr_status dr_octree_create_host(const float *xyz, int32_t n, const dr_build_params *bp, dr_octree **out);
+dr_status dr_octree_stats(const dr_octree *tree, int64_t *nodes, int64_t *leaves, int64_t *refs, int32_t *depth);
+dr_status dr_octree_export(const dr_octree *tree, float *node_box, int32_t *node_child, int32_t *node_leaf, int32_t *leaf_tri);
+void dr_octree_destroy(dr_octree *tree);
+
+/* ---- scene ---------------------------------------------------------------------------------
+ * Replaces Octree<Renderable<BakedTriFace>>::push + build (Octree.impl.cuh:97-129) and the lazy
+ * device upload of the scene (ReferenceManager::gpuHandle, ReferenceManager.impl.cuh:18-51).
+ * xyz: host float[n][3][3] triangle vertices; nrm: host float[n][3][3] per-vertex normals or NULL
+ * (flat shading); mat_id: host int32[n] or NULL (all 0).  The octree is built on the host with the
+ * reference's split rule and uploaded once; triangle index i is the push order. */
+dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat_id, int32_t n,
+                          const dr_material *mats, int32_t n_mats, const dr_light *lights, int32_t n_lights,
+                          const dr_build_params *bp, dr_scene **out);
+
+/* Physical-mode per-triangle overrides (host arrays, any may be NULL): albedo float[n][3],
+ * emission float[n][3], roughness float[n]. */
+dr_status dr_scene_set_triangle_params(dr_scene *scene, const float *albedo, const float *emission,
+                                       const float *roughness);
+
+/* Device pointers to the scene's per-triangle albedo and emission (float[n][3] each), for
+ * callers that update them in place (e.g. an optimiser).  Emissive-triangle sampling tables are
+ * not rebuilt by in-place writes; call dr_scene_set_triangle_params to change which are emissive. */
+dr_status dr_scene_triangle_params_device(dr_scene *scene, float **albedo, float **emission);
+
+/* Octree statistics: node count, leaf count, total leaf references, tree depth. */
+dr_status dr_scene_stats(const dr_scene *scene, int64_t *nodes, int64_t *leaves, int64_t *refs, int32_t *depth);
+
+/* Copies the flattened octree to host arrays for inspection (sizes from dr_scene_stats):
+ * node_box float[nodes][6] (min xyz, max xyz), node_child int32[nodes] (first child or -1),
+ * node_leaf int32[nodes][2] (first ref, ref count; zeros for inner nodes), leaf_tri int32[refs]. */
+dr_status dr_scene_export_tree(const dr_scene *scene, float *node_box, int32_t *node_child,
+                               int32_t *node_leaf, int32_t *leaf_tri);
+
+void dr_scene_destroy(dr_scene *scene);
+
+/* ---- ray casting ---------------------------------------------------------------------------
+ * Replaces Octree<...>::cast (Octree.impl.cuh:174-212) / Raycaster::cast (Raycaster.cuh:75-83):
+ * closest hit in units of |direction| (directions are not normalised), backface culling flag,
+ * self-hit avoidance by object identity (validateNotSameAsObject, Octree.impl.cuh:126):
+ * ignore_tri int32[n] or NULL (-1 = none).
+ * Device arrays: origin float[n][3], direction float[n][3]; outputs hit_tri int32[n] (-1 = miss),
+ * hit_t float[n] (FLT_MAX on a miss). */
+dr_status dr_cast(const dr_scene *scene, const float *origin, const float *direction, const int32_t *ignore_tri,
+                  int32_t n, int32_t cull_backfaces, int32_t *hit_tri, float *hit_t, void *stream);
+
+/* Same as dr_cast, also writing per-ray traversal counters (device int32[n] each): child-box slab
+ * tests and triangle tests.  Used to compute the algorithmic bytes per ray. */
+dr_status dr_cast_counted(const dr_scene *scene, const float *origin, const float *direction, const int32_t *ignore_tri,
+                          int32_t n, int32_t cull_backfaces, int32_t *hit_tri, float *hit_t,
+                          int32_t *box_tests, int32_t *tri_tests, void *stream);
+
+/* ---- block renderer ------------------------------------------------------------------------
+ * A renderer owns the wavefront scratch (ray / hit / shadow queues, per-pixel accumulators) for
+ * at most `wave_paths` paths in flight (0 = default 4M). */
+dr_status dr_renderer_create(int32_t wave_paths, dr_renderer **out);
+void dr_renderer_destroy(dr_renderer *r);
+
+/* Replaces DumbRenderer::renderBlocksGPU (DumbRenderer.cu:87-113): renders blocks
+ * [start_block, end_block) of a width x height image into the caller's device frame buffer
+ * (BlockBasedFrameBuffer<8,16> layout, float4), setting (iteration <= 1) or blending (1/iteration)
+ * each pixel exactly like setBlockPixelColor / blendBlockPixelColor.  Asynchronous on `stream`. */
+dr_status dr_render_blocks(dr_renderer *r, const dr_scene *scene, const dr_camera *camera, float *fb_blockmajor,
+                           int32_t start_block, int32_t end_block, const dr_render_params *params, void *stream);
+
+/* Number of blocks of a width x height image (ceil(W/8) * ceil(H/16)). */
+int32_t dr_block_count(int32_t width, int32_t height);
+
+/* Kernel launches issued by this renderer since creation (for launch accounting). */
+int64_t dr_renderer_launch_count(const dr_renderer *r);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DR_API_H */

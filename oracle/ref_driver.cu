@@ -1,0 +1,164 @@
+// Thin C-ABI driver around the UNMODIFIED reference DumbRay host path, compiled together with the
+// reference's own sources by oracle/build_ref.sh into oracle/_ref/libdumbref.so.
+//
+// Test infrastructure only: used by the parity tests (as the checker that pins the oracle) and by
+// bench.py's reference arm (as the timed CPU baseline).  Nothing in the product links it.
+//
+// What it calls (reference file:line, relative to the DumbRay checkout):
+//   Octree<Renderable<BakedTriFace>>::push/build   __source__/DataStructures/Objects/Scene/Raycasters/Octree/Octree.impl.cuh:97-129
+//   Octree<...>::cast                              Octree.impl.cuh:174-212
+//   DumbRenderer (CPU threads) via Renderer::iterate  __source__/DataStructures/Renderers/Renderer/Renderer.cu:143-156
+//   DumbBasedShader / SimpleStochasticShader        __source__/DataStructures/Objects/Components/Shaders/*
+//   SphericalLightEmitter / SimpleSoftDirectionalLight / SimpleDirectionalLight   __source__/DataStructures/Objects/Scene/Lights/*
+//   DefaultPerspectiveLense / SimpleStochasticLense / Lenses::SphericalSegmentLense  __source__/DataStructures/Objects/Components/Lenses/*
+#include "DataStructures/Renderers/DumbRenderer/DumbRenderer.cuh"
+#include "DataStructures/Screen/FrameBuffer/BlockBasedFrameBuffer/BlockBasedFrameBuffer.cuh"
+#include "DataStructures/Objects/Components/Shaders/DumbBasedShader/DumbBasedShader.cuh"
+#include "DataStructures/Objects/Components/Shaders/SimpleStochasticShader/SimpleStochasticShader.cuh"
+#include "DataStructures/Objects/Components/Lenses/DefaultPerspectiveLense/DefaultPerspectiveLense.cuh"
+#include "DataStructures/Objects/Components/Lenses/SimpleStochasticLense/SimpleStochasticLense.cuh"
+#include "DataStructures/Objects/Components/Lenses/SphericalSegmentLense/SphericalSegmentLense.cuh"
+#include "DataStructures/Objects/Scene/Lights/SphericalLightEmitter/SphericalLightEmitter.cuh"
+#include "DataStructures/Objects/Scene/Lights/SimpleSoftDirectionalLight/SimpleSoftDirectionalLight.cuh"
+#include "DataStructures/Objects/Scene/Lights/SimpleDirectionalLight/SimpleDirectionalLight.cuh"
+#include <thread>
+#include <vector>
+#include <chrono>
+
+typedef Renderable<BakedTriFace> RefUnit;
+typedef Octree<RefUnit> RefOctree;
+
+static BakedTriFace make_face(const float *v, const float *n) {
+	Triangle vert(Vector3(v[0], v[1], v[2]), Vector3(v[3], v[4], v[5]), Vector3(v[6], v[7], v[8]));
+	Triangle norm;
+	if (n != NULL) norm = Triangle(Vector3(n[0], n[1], n[2]), Vector3(n[3], n[4], n[5]), Vector3(n[6], n[7], n[8]));
+	else {
+		// Flat shading: the reference's outward normal is Triangle::normal() = (c-a)x(b-a).
+		Vector3 fn = vert.normal().normalized();
+		norm = Triangle(fn, fn, fn);
+	}
+	Triangle tex(Vector3(0, 0, 0), Vector3(1, 0, 0), Vector3(0, 1, 0));
+	return BakedTriFace(vert, norm, tex);
+}
+
+extern "C" {
+
+// Builds the reference octree over n triangles (xyz[9*n], optional per-vertex normals nrm[9*n],
+// optional material ids).  Push order = triangle index, so hit index = hit.object - data.
+void *dref_octree_create(const float *xyz, const float *nrm, const int *mat, int n) {
+	RefOctree *tree = new RefOctree();
+	for (int i = 0; i < n; i++)
+		tree->push(RefUnit(make_face(xyz + 9 * i, (nrm != NULL) ? (nrm + 9 * i) : NULL), (mat != NULL) ? mat[i] : 0));
+	tree->build();
+	return (void *)tree;
+}
+
+int dref_octree_node_count(void *h) { return ((RefOctree *)h)->getNodeCount(); }
+
+void dref_octree_destroy(void *h) { delete (RefOctree *)h; }
+
+// Closest-hit casts of n rays (origins o[3n], directions d[3n]) with the reference's Octree::cast.
+// idx = triangle index or -1, t = hitDistance (FLT_MAX on a miss).  Runs on `threads` host threads.
+void dref_octree_cast(void *h, const float *o, const float *d, int n, int clip, int threads, int *idx, float *t) {
+	const RefOctree *tree = (const RefOctree *)h;
+	const RefUnit *base = (tree->getData() + 0);
+	if (threads < 1) threads = 1;
+	auto work = [&](int tid) {
+		for (int i = tid; i < n; i += threads) {
+			Ray r(Vector3(o[3 * i], o[3 * i + 1], o[3 * i + 2]), Vector3(d[3 * i], d[3 * i + 1], d[3 * i + 2]));
+			RaycastHit<RefUnit> hit;
+			if (tree->cast(r, hit, clip != 0)) {
+				idx[i] = (int)(hit.object - base);
+				t[i] = hit.hitDistance;
+			}
+			else {
+				idx[i] = -1;
+				t[i] = FLT_MAX;
+			}
+		}
+	};
+	std::vector<std::thread> pool;
+	for (int k = 1; k < threads; k++) pool.emplace_back(work, k);
+	work(0);
+	for (auto &th : pool) th.join();
+}
+
+// Material / light / lens records are flat float[16] arrays:
+//   material: [0]=type (0 DumbBasedShader, 1 SimpleStochasticShader)
+//     DumbBased: [1..3] fresnel rgb, [4] specular, [5..7] diffuse rgb, [8] metal
+//     SimpleStochastic: [1..3] albedo rgb, [4] diffuse, [5] smoothness, [6] shininess
+//   light: [0]=type (0 SphericalLightEmitter, 1 SimpleSoftDirectionalLight, 2 SimpleDirectionalLight)
+//     Spherical: [1..3] color, [4..6] position, [7] radius
+//     SoftDirectional: [1..3] color, [4..6] direction, [7] distance, [8] softness
+//     Directional: [1..3] color, [4..6] direction, [7] distance
+//   camera: [0]=lens (0 DefaultPerspectiveLense, 1 SimpleStochasticLense, 2 SphericalSegmentLense)
+//     [1] angle (deg) / [1..2] alpha for spherical, [3] focal distance, [4] softness, [5..7] filter,
+//     [8..10] position, [11..13] euler angles (deg)
+struct RefScene {
+	TriScene scene;
+	DumbRenderer::CameraManager camera;
+};
+
+void *dref_scene_create(const float *xyz, const float *nrm, const int *mat, int n,
+                        const float *mats, int n_mats, const float *lights, int n_lights, const float *cam) {
+	RefScene *s = new RefScene();
+	s->scene.materials.cpuHandle()->flush(n_mats);
+	for (int i = 0; i < n_mats; i++) {
+		const float *m = mats + 16 * i;
+		Material<BakedTriFace> &dst = s->scene.materials.cpuHandle()->operator[](i);
+		if ((int)m[0] == 0)
+			dst.use<DumbBasedShader>((ColoredTexture)ColorRGB(m[1], m[2], m[3]), m[4], (ColoredTexture)ColorRGB(m[5], m[6], m[7]), m[8]);
+		else
+			dst.use<SimpleStochasticShader>(ColorRGB(m[1], m[2], m[3]), m[4], m[5], m[6]);
+	}
+	s->scene.lights.cpuHandle()->flush(n_lights);
+	for (int i = 0; i < n_lights; i++) {
+		const float *l = lights + 16 * i;
+		Light &dst = s->scene.lights.cpuHandle()->operator[](i);
+		Color c(l[1], l[2], l[3], 1.0f);
+		Vector3 v(l[4], l[5], l[6]);
+		if ((int)l[0] == 0) dst.use<SphericalLightEmitter>(c, v, l[7]);
+		else if ((int)l[0] == 1) dst.use<SimpleSoftDirectionalLight>(c, v, l[7], l[8]);
+		else dst.use<SimpleDirectionalLight>(c, v, l[7]);
+	}
+	int lens = (int)cam[0];
+	if (lens == 0) s->camera.cpuHandle()->lense.use<DefaultPerspectiveLense>(cam[1]);
+	else if (lens == 1) s->camera.cpuHandle()->lense.use<SimpleStochasticLense>(cam[1]);
+	else s->camera.cpuHandle()->lense.use<Lenses::SphericalSegmentLense>(Vector2(cam[1], cam[2]), cam[3], cam[4], Color(cam[5], cam[6], cam[7], 1.0f));
+	s->camera.cpuHandle()->transform = Transform(Vector3(cam[8], cam[9], cam[10]), Vector3(cam[11], cam[12], cam[13]), Vector3(1.0f, 1.0f, 1.0f));
+	RefOctree *tree = s->scene.geometry.cpuHandle();
+	for (int i = 0; i < n; i++)
+		tree->push(RefUnit(make_face(xyz + 9 * i, (nrm != NULL) ? (nrm + 9 * i) : NULL), (mat != NULL) ? mat[i] : 0));
+	tree->build();
+	return (void *)s;
+}
+
+void dref_scene_destroy(void *h) { delete (RefScene *)h; }
+
+// Renders `iterations` progressive iterations with the reference DumbRenderer on `threads` CPU
+// threads (BlockBuffer = 8x16 blocks) and writes the blended float4 image row-major to rgba[4*W*H].
+// Returns the wall time of the iterations in seconds (scene build excluded), or -1 on failure.
+double dref_render(void *h, int width, int height, int fsaa_x, int fsaa_y, int max_bounces,
+                   int cull_backfaces, int iterations, int threads, float *rgba) {
+	RefScene *s = (RefScene *)h;
+	FrameBufferManager fb;
+	fb.cpuHandle()->use<BlockBuffer>();
+	if (!fb.cpuHandle()->setResolution(width, height)) return -1.0;
+	DumbRenderer renderer(Renderer::ThreadConfiguration::cpuOnly(threads), BlockRenderer::BlockConfiguration(),
+		&fb, &s->scene, &s->camera, DumbRenderer::BOXING_MODE_HEIGHT_BASED, max_bounces, fsaa_x, fsaa_y, 1, cull_backfaces != 0);
+	auto t0 = std::chrono::steady_clock::now();
+	for (int i = 0; i < iterations; i++)
+		if (!renderer.iterate()) return -1.0;
+	auto t1 = std::chrono::steady_clock::now();
+	if (rgba != NULL) {
+		for (int y = 0; y < height; y++)
+			for (int x = 0; x < width; x++) {
+				Color c = fb.cpuHandle()->getColor(x, y);
+				float *p = rgba + 4 * (y * width + x);
+				p[0] = c.r; p[1] = c.g; p[2] = c.b; p[3] = c.a;
+			}
+	}
+	return std::chrono::duration<double>(t1 - t0).count();
+}
+
+}  // extern "C"

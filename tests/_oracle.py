@@ -1,0 +1,203 @@
+"""ctypes bindings of the CPU oracle (oracle/_build/libdroracle.so) and, when it has been built, of
+the reference DumbRay host path (oracle/_ref/libdumbref.so).  Test infrastructure only."""
+from __future__ import annotations
+
+import ctypes
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+import dumbray_gb300 as dr
+
+ROOT = Path(__file__).resolve().parent.parent
+ORACLE_LIB = ROOT / "oracle" / "_build" / "libdroracle.so"
+REF_LIB = ROOT / "oracle" / "_ref" / "libdumbref.so"
+
+_o = None
+_r = None
+vp, ci = ctypes.c_void_p, ctypes.c_int
+
+
+def oracle():
+    global _o
+    if _o is None:
+        if not ORACLE_LIB.exists():
+            subprocess.run(["bash", str(ROOT / "oracle" / "build_oracle.sh")], check=True, capture_output=True)
+        L = ctypes.CDLL(str(ORACLE_LIB))
+        L.dro_scene_create.restype = vp
+        L.dro_scene_create.argtypes = [vp, vp, vp, ci, vp, ci, vp, ci, ci, ci, ci]
+        L.dro_scene_set_triangle_params.argtypes = [vp, vp, vp, vp]
+        L.dro_scene_destroy.argtypes = [vp]
+        L.dro_node_count.restype = ctypes.c_longlong
+        L.dro_node_count.argtypes = [vp]
+        L.dro_tree_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                                     ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ci)]
+        L.dro_tree_canonical.restype = ctypes.c_longlong
+        L.dro_tree_canonical.argtypes = [vp, vp, vp, vp, ctypes.c_longlong, ctypes.c_longlong]
+        L.dro_cast.argtypes = [vp, vp, vp, vp, ci, ci, ci, vp, vp, vp, vp]
+        L.dro_render_blocks.argtypes = [vp, vp, vp, vp, ci, ci, ci]
+        L.dro_rng_u32.restype = ctypes.c_uint32
+        L.dro_rng_u32.argtypes = [ctypes.c_uint32] * 5
+        _o = L
+    return _o
+
+
+def reference_available() -> bool:
+    return REF_LIB.exists()
+
+
+def reference():
+    global _r
+    if _r is None:
+        L = ctypes.CDLL(str(REF_LIB))
+        L.dref_octree_create.restype = vp
+        L.dref_octree_create.argtypes = [vp, vp, vp, ci]
+        L.dref_octree_node_count.restype = ci
+        L.dref_octree_node_count.argtypes = [vp]
+        L.dref_octree_destroy.argtypes = [vp]
+        L.dref_octree_cast.argtypes = [vp, vp, vp, ci, ci, ci, vp, vp]
+        L.dref_scene_create.restype = vp
+        L.dref_scene_create.argtypes = [vp, vp, vp, ci, vp, ci, vp, ci, vp]
+        L.dref_scene_destroy.argtypes = [vp]
+        L.dref_render.restype = ctypes.c_double
+        L.dref_render.argtypes = [vp, ci, ci, ci, ci, ci, ci, ci, ci, vp]
+        _r = L
+    return _r
+
+
+class OracleScene:
+    def __init__(self, tris, normals=None, mat_id=None, materials=(), lights=(), threads=8):
+        L = oracle()
+        self.tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 3, 3)
+        self.nrm = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32)
+        self.mat = None if mat_id is None else np.ascontiguousarray(mat_id, dtype=np.int32)
+        mats = list(materials)
+        lts = list(lights)
+        self._marr = (dr.DrMaterial * max(1, len(mats)))(*mats)
+        self._larr = (dr.DrLight * max(1, len(lts)))(*lts)
+        self.h = L.dro_scene_create(self.tris.ctypes.data, None if self.nrm is None else self.nrm.ctypes.data,
+                                    None if self.mat is None else self.mat.ctypes.data, len(self.tris),
+                                    ctypes.addressof(self._marr), len(mats), ctypes.addressof(self._larr), len(lts), 0, 0,
+                                    threads)
+
+    def set_triangle_params(self, albedo=None, emission=None, roughness=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float32) for a in (albedo, emission, roughness)]
+        oracle().dro_scene_set_triangle_params(self.h, *[None if a is None else a.ctypes.data for a in arrs])
+        self._keep = arrs
+
+    def node_count(self):
+        return oracle().dro_node_count(self.h)
+
+    def stats(self):
+        n, l, r = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        d = ctypes.c_int()
+        oracle().dro_tree_stats(self.h, ctypes.byref(n), ctypes.byref(l), ctypes.byref(r), ctypes.byref(d))
+        return dict(nodes=n.value, leaves=l.value, refs=r.value, depth=d.value)
+
+    def canonical(self):
+        s = self.stats()
+        box = np.zeros((s["nodes"], 6), np.float32)
+        cnt = np.zeros(s["nodes"], np.int32)
+        tri = np.zeros(max(1, s["refs"]), np.int32)
+        k = oracle().dro_tree_canonical(self.h, box.ctypes.data, cnt.ctypes.data, tri.ctypes.data, s["nodes"], s["refs"])
+        return box[:k], cnt[:k], tri[: s["refs"]]
+
+    def cast(self, o, d, ignore=None, cull=True, threads=8):
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        n = len(o)
+        idx = np.zeros(n, np.int32)
+        t = np.zeros(n, np.float32)
+        nb = np.zeros(n, np.int32)
+        nt = np.zeros(n, np.int32)
+        ig = None if ignore is None else np.ascontiguousarray(ignore, np.int32)
+        oracle().dro_cast(self.h, o.ctypes.data, d.ctypes.data, None if ig is None else ig.ctypes.data, n, 1 if cull else 0,
+                          threads, idx.ctypes.data, t.ctypes.data, nb.ctypes.data, nt.ctypes.data)
+        return idx, t, nb, nt
+
+    def render_blocks(self, cam, params, fb=None, start=0, end=None, threads=8):
+        nb = dr.block_count(params.width, params.height)
+        end = nb if end is None else end
+        if fb is None:
+            fb = np.zeros((nb * dr.BLOCK_SIZE, 4), np.float32)
+        oracle().dro_render_blocks(self.h, ctypes.byref(cam), ctypes.byref(params), fb.ctypes.data, start, end, threads)
+        return fb
+
+    def __del__(self):
+        try:
+            oracle().dro_scene_destroy(self.h)
+        except Exception:
+            pass
+
+
+def ref_cast(tris, o, d, cull=True, threads=8):
+    """The reference's own Octree::cast (oracle/_ref)."""
+    L = reference()
+    tris = np.ascontiguousarray(tris, np.float32)
+    h = L.dref_octree_create(tris.ctypes.data, None, None, len(tris))
+    try:
+        n = len(o)
+        idx = np.zeros(n, np.int32)
+        t = np.zeros(n, np.float32)
+        o = np.ascontiguousarray(o, np.float32)
+        d = np.ascontiguousarray(d, np.float32)
+        L.dref_octree_cast(h, o.ctypes.data, d.ctypes.data, n, 1 if cull else 0, threads, idx.ctypes.data, t.ctypes.data)
+        return idx, t, L.dref_octree_node_count(h)
+    finally:
+        L.dref_octree_destroy(h)
+
+
+def ref_material_record(m: dr.DrMaterial) -> np.ndarray:
+    r = np.zeros(16, np.float32)
+    if m.type == dr.MAT_DUMB_BASED:
+        r[:9] = [0, *m.fresnel, m.specular, *m.color, m.metal]
+    elif m.type == dr.MAT_SIMPLE_STOCHASTIC:
+        r[:7] = [1, *m.color, m.diffuse, m.smoothness, m.shininess]
+    else:
+        raise ValueError("material has no reference counterpart")
+    return r
+
+
+def ref_light_record(l: dr.DrLight) -> np.ndarray:
+    r = np.zeros(16, np.float32)
+    if l.type == dr.LIGHT_SPHERICAL:
+        r[:8] = [0, *l.color, *l.position, l.radius]
+    elif l.type == dr.LIGHT_SOFT_DIRECTIONAL:
+        r[:9] = [1, *l.color, *l.direction, l.distance, l.softness]
+    else:
+        r[:8] = [2, *l.color, *l.direction, l.distance]
+    return r
+
+
+def ref_camera_record(c: dr.DrCamera) -> np.ndarray:
+    """Only identity camera orientation is expressible here (reference Transform with zero Euler angles)."""
+    assert tuple(c.right) == (1.0, 0.0, 0.0) and tuple(c.up) == (0.0, 1.0, 0.0) and tuple(c.forward) == (0.0, 0.0, 1.0)
+    r = np.zeros(16, np.float32)
+    r[0] = c.lens
+    r[1], r[2] = c.angle[0], c.angle[1]
+    r[3], r[4] = c.focal_distance, c.softness
+    r[5:8] = list(c.filter)
+    r[8:11] = list(c.position)
+    return r
+
+
+def ref_render(tris, mat_id, materials, lights, cam, width, height, fsaa=(1, 1), max_bounces=2, cull=True, iterations=1,
+               threads=8, normals=None):
+    """Reference DumbRenderer on CPU threads; returns (row-major RGBA image, seconds)."""
+    L = reference()
+    tris = np.ascontiguousarray(tris, np.float32)
+    mat = np.ascontiguousarray(mat_id, np.int32)
+    mrec = np.ascontiguousarray(np.stack([ref_material_record(m) for m in materials]))
+    lrec = np.ascontiguousarray(np.stack([ref_light_record(l) for l in lights]))
+    crec = ref_camera_record(cam)
+    nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
+    h = L.dref_scene_create(tris.ctypes.data, None if nrm is None else nrm.ctypes.data, mat.ctypes.data, len(tris),
+                            mrec.ctypes.data, len(mrec), lrec.ctypes.data, len(lrec), crec.ctypes.data)
+    try:
+        img = np.zeros((height, width, 4), np.float32)
+        sec = L.dref_render(h, width, height, fsaa[0], fsaa[1], max_bounces, 1 if cull else 0, iterations, threads,
+                            img.ctypes.data)
+        return img, sec
+    finally:
+        L.dref_scene_destroy(h)
