@@ -1,0 +1,417 @@
+"""Benchmark: Mpaths/s of the full path trace at 1920x1080, 64 spp, depth 8 on one GB300.
+
+Workload (synthetic, seeded; no dataset): icosphere level 8 (1,310,720 triangles) radially displaced
+by 3-octave value noise (amplitude 0.1, seed 1) on a 2-triangle ground plane, lit by 4 emissive
+quads; materials by triangle-index hash (60% Lambert albedo U[0.2,0.8]^3, 25% mirror, 15% GGX
+glossy roughness U[0.05,0.4]); pinhole 60 degrees.  One step = one full frame (132,710,400 paths)
+rendered through dr_render_blocks into the block-major float4 frame buffer.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` = paths of all ranks / max-over-ranks device time of the K
+timed steps (inputs resident in HBM).  `e2e` = the same through the public API with the frame buffer
+copied host->device before and device->host after every step (pinned host memory).  `roofline`
+describes the dominant kernel (k_trace): algorithmic bytes per launch = rays x (40 + 32 C_box +
+36 C_tri) with C_box / C_tri the reference traversal's mean child-box / triangle tests per ray
+(counted in an untimed pass), divided by its CUDA-event launch time measured over the timed region.
+N > 1: every rank renders its own frame of distinct samples (weak scaling, no collective on the data
+path).  `--impl reference` times the reference DumbRenderer on host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mpaths/s 1080p 64spp on 1 GB300: plain vs batched, fwd vs fwd+adjoint, at RMSE"
+UNIT = "Mpaths/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--spp", type=int, default=64)
+    ap.add_argument("--depth", type=int, default=8)
+    ap.add_argument("--level", type=int, default=8)
+    ap.add_argument("--lens", default="pinhole", choices=["pinhole", "fisheye", "spherical"])
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--wave", type=int, default=1 << 22)
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def samples_xy(spp):
+    sx = int(round(spp ** 0.5))
+    while spp % sx:
+        sx -= 1
+    return sx, spp // sx
+
+
+def build_scene(dr, level):
+    from dumbray_gb300 import scenes
+    S = scenes.full_scene(level=level, seed=1)
+    mats = [dr.lambert(), dr.mirror(), dr.glossy()]
+    t0 = time.time()
+    scene = dr.Scene(S["tris"], mat_id=S["mat_id"], materials=mats)
+    scene.set_triangle_params(S["albedo"], S["emission"], S["roughness"])
+    return S, scene, time.time() - t0
+
+
+def make_camera(dr, lens):
+    pos, target = (0.0, 0.6, -3.4), (0.0, -0.15, 0.0)
+    if lens == "fisheye":
+        return dr.camera(dr.LENS_FISHEYE, position=pos, target=target, angle=(180.0, 180.0))
+    if lens == "spherical":
+        return dr.camera(dr.LENS_SPHERICAL, position=pos, target=target, angle=(200.0, 180.0))
+    return dr.camera(dr.LENS_PINHOLE, position=pos, target=target, angle=(60.0, 60.0))
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def cpu_sample_ranges(W, H, rows=8, cols=12):
+    """Block ranges of a rows x cols patch of blocks at the image centre (the bounded CPU sample)."""
+    bw = (W + 7) // 8
+    bh = (H + 15) // 16
+    r0, c0 = bh // 2 - rows // 2, bw // 2 - cols // 2
+    return [((r0 + r) * bw + c0, (r0 + r) * bw + c0 + cols) for r in range(rows)]
+
+
+def cpu_baseline_ours(S, cam, W, H, depth, seed):
+    """FP64 oracle (physical mode) on a bounded sample: an 8x12-block patch (12,288 pixels) at the
+    image centre, 1 spp, same depth."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import dumbray_gb300 as dr
+    import _oracle as O
+    threads = os.cpu_count() or 1
+    osc = O.OracleScene(S["tris"], mat_id=S["mat_id"], materials=[dr.lambert(), dr.mirror(), dr.glossy()], threads=threads)
+    osc.set_triangle_params(S["albedo"], S["emission"], S["roughness"])
+    p = dr.render_params(W, H, dr.MODE_PHYSICAL, samples=(1, 1), max_bounces=depth, seed=seed)
+    fb = np.zeros((dr.block_count(W, H) * 128, 4), np.float32)
+    ranges = cpu_sample_ranges(W, H)
+    t0 = time.time()
+    for a, b in ranges:
+        osc.render_blocks(cam, p, fb=fb, start=a, end=b, threads=threads)
+    dt = time.time() - t0
+    paths = sum(b - a for a, b in ranges) * 128
+    return dict(value=paths / dt / 1e6, unit=UNIT, cores=threads, kind="port",
+                sample=f"FP64 oracle, centre patch of 8x12 blocks of {W}x{H} ({paths:,} px) x 1 spp, depth {depth}, "
+                       f"{dt:.1f} s"), (ranges, fb, p)
+
+
+def run_ours(a):
+    import torch
+    import dumbray_gb300 as dr
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+    S, scene, build_s = build_scene(dr, a.level)
+    cam = make_camera(dr, a.lens)
+    W, H = a.width, a.height
+    sx, sy = samples_xy(a.spp)
+    nb = dr.block_count(W, H)
+    paths_per_frame = W * H * a.spp
+    fb = dr.new_frame_buffer(W, H, dev)
+    rend = dr.Renderer(a.wave)
+    stream = torch.cuda.current_stream()
+
+    def params(it):
+        # each rank renders distinct samples: iteration index offset by rank
+        return dr.render_params(W, H, dr.MODE_PHYSICAL, samples=(sx, sy), max_bounces=a.depth,
+                                iteration=1 + rank * 100000 + it, seed=1234)
+
+    for i in range(a.warmup):
+        rend.render_blocks(scene, cam, fb, 0, nb, params(i), stream)
+    torch.cuda.synchronize()
+    # timed region: device-resident inputs
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    rend.set_profiling(True)
+    launches0 = rend.launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(a.steps):
+        rend.render_blocks(scene, cam, fb, 0, nb, params(a.warmup + i), stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    launches = rend.launches() - launches0
+    ktimes = rend.kernel_times()
+    rend.set_profiling(False)
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        ms = float(t.item())
+    value = world * paths_per_frame * a.steps / (ms / 1e3) / 1e6
+
+    # e2e through the public API with host buffers (pinned), copies inside the timed region
+    host_fb = torch.zeros(fb.shape, dtype=torch.float32).pin_memory()
+    host_out = torch.zeros(fb.shape, dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for i in range(a.steps):
+        fb.copy_(host_fb, non_blocking=True)
+        rend.render_blocks(scene, cam, fb, 0, nb, params(a.warmup + a.steps + i), stream)
+        host_out.copy_(fb, non_blocking=True)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = f0.elapsed_time(f1)
+    if world > 1:
+        t = torch.tensor([ms_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    e2e = world * paths_per_frame * a.steps / (ms_e2e / 1e3) / 1e6
+    fb_bytes = fb.numel() * 4
+
+    # counting pass (untimed): reference traversal counts of the extension rays of one frame
+    rend.set_counting(True)
+    rend.render_blocks(scene, cam, fb, 0, nb, params(0), stream)
+    cnt = rend.counters()
+    rend.set_counting(False)
+    c_box = cnt["trace_box"] / max(1, cnt["trace_rays"])
+    c_tri = cnt["trace_tri"] / max(1, cnt["trace_rays"])
+    bytes_per_ray = 40.0 + 32.0 * c_box + 36.0 * c_tri
+    trace_ms, trace_launches = ktimes["trace"]
+    frames = a.steps
+    trace_bytes_per_frame = cnt["trace_rays"] * bytes_per_ray
+    achieved = (trace_bytes_per_frame * frames) / (trace_ms / 1e3) / 1e9 if trace_ms > 0 else 0.0
+    peak, peak_src = measured_peak()
+
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": round(ms / a.steps, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"full path trace: {len(S['tris']):,}-tri displaced icosphere L{a.level} + ground + 4 emissive "
+                               f"quads, {W}x{H}, {a.spp} spp, depth {a.depth}, {a.lens}",
+                   "triangles": int(len(S["tris"])), "width": W, "height": H, "spp": a.spp, "depth": a.depth,
+                   "lens": a.lens, "mode": "physical", "wave_paths": a.wave, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (scene ~0.3 GB, wavefront queues ~2 GB), no flush",
+                   "scene_build_s": round(build_s, 2)},
+        "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": fb_bytes, "d2h_bytes_per_step": fb_bytes},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "kernel": "k_trace",
+                     "peak_source": f"{peak_src} hbm_gbs", "bytes_per_ray": round(bytes_per_ray, 1),
+                     "c_box": round(c_box, 2), "c_tri": round(c_tri, 2),
+                     "launch_ms_avg": round(trace_ms / max(1, trace_launches), 4)},
+        "kernel_ms_per_step": {k: round(v[0] / a.steps, 2) for k, v in ktimes.items()},
+        "rays_per_frame": {"extension": cnt["trace_rays"], "shadow": cnt["shadow_casts"]},
+        "mrays_per_s": round((cnt["trace_rays"] + cnt["shadow_casts"]) * a.steps / (ms / 1e3) / 1e6, 1),
+    }
+    if clocks:
+        out["clocks"] = clocks
+    if rank == 0 and world == 1 and not a.no_variants:
+        variants = {}
+        for lens in ("fisheye", "spherical"):
+            c2 = make_camera(dr, lens)
+            rend.render_blocks(scene, c2, fb, 0, nb, params(0), stream)
+            torch.cuda.synchronize()
+            g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            g0.record(stream)
+            rend.render_blocks(scene, c2, fb, 0, nb, params(1), stream)
+            g1.record(stream)
+            torch.cuda.synchronize()
+            variants[lens] = round(paths_per_frame / (g0.elapsed_time(g1) / 1e3) / 1e6, 3)
+        out["lens_variants_mpaths_s"] = variants
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        base, (ranges, ofb, p) = cpu_baseline_ours(S, cam, W, H, a.depth, 4321)
+        out["cpu_baseline"] = base
+        # accuracy on the same sample: GPU at the same samples vs the FP64 oracle
+        gfb = dr.new_frame_buffer(W, H, dev)
+        for s0, s1 in ranges:
+            rend.render_blocks(scene, cam, gfb, s0, s1, p, stream)
+        torch.cuda.synchronize()
+        gall = gfb.cpu().numpy()
+        g = np.concatenate([gall[s0 * 128:s1 * 128, :3] for s0, s1 in ranges]).astype(np.float64)
+        o = np.concatenate([ofb[s0 * 128:s1 * 128, :3] for s0, s1 in ranges]).astype(np.float64)
+        out["rmse_vs_fp64_oracle_rel"] = float(np.sqrt(np.mean((g - o) ** 2)) / max(o.mean(), 1e-9))
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def reference_twin(S, dr):
+    """Reference-expressible twin of the workload: emissive quads -> SphericalLightEmitter at the
+    quad centres (colour = radiance x area x pi so the power matches), Lambert -> DumbBasedShader
+    (metal 0), mirror -> SimpleStochasticShader(diffuse 0, smoothness 1), glossy -> DumbBasedShader
+    (metal 1, Phong exponent 2/r^2 - 2), lens -> SimpleStochasticLense(60)."""
+    tris = S["tris"]
+    n_geo = S["n_mesh"] + S["n_ground"]
+    mat = S["mat_id"][:n_geo].copy()
+    mats = [dr.dumb_based(diffuse=(0.5, 0.5, 0.5), metal=0.0), dr.simple_stochastic((0.9, 0.9, 0.9), 0.0, 1.0, 64.0),
+            dr.dumb_based(fresnel=(0.6, 0.6, 0.6), specular=2.0 / 0.2 ** 2 - 2.0, diffuse=(1, 1, 1), metal=1.0)]
+    lights = []
+    lt = tris[n_geo:].reshape(-1, 2, 3, 3)
+    for q in lt:
+        c = q.reshape(-1, 3).mean(0)
+        lights.append(dr.spherical_light((10.0 * np.pi,) * 3, tuple(c - np.array([0, 0.05, 0])), 0.3))
+    return tris[:n_geo], mat, mats, lights
+
+
+def run_reference(a):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "tests"))
+    import dumbray_gb300 as dr
+    import _oracle as O
+    from dumbray_gb300 import scenes
+    S = scenes.full_scene(level=a.level, seed=1)
+    tris, mat, mats, lights = reference_twin(S, dr)
+    threads = os.cpu_count() or 1
+    cam_pos = (0.0, 0.6, -3.4)
+    cam = dr.camera(dr.LENS_SIMPLE_STOCHASTIC, position=cam_pos, angle=60.0)
+    # bounded sample of the 1080p frame: a 240x136 image (1/64 of the pixels) at 1 spp per step
+    sw, sh = 240, 136
+    paths = sw * sh
+    if O.reference_available():
+        L = O.reference()
+        import ctypes
+        t_ = np.ascontiguousarray(tris, np.float32)
+        m_ = np.ascontiguousarray(mat, np.int32)
+        mrec = np.ascontiguousarray(np.stack([O.ref_material_record(m) for m in mats]))
+        lrec = np.ascontiguousarray(np.stack([O.ref_light_record(l) for l in lights]))
+        crec = O.ref_camera_record(cam)
+        t0 = time.time()
+        h = L.dref_scene_create(t_.ctypes.data, None, m_.ctypes.data, len(t_), mrec.ctypes.data, len(mrec),
+                                lrec.ctypes.data, len(lrec), crec.ctypes.data)
+        build_s = time.time() - t0
+        img = np.zeros((sh, sw, 4), np.float32)
+        for _ in range(a.warmup):
+            L.dref_render(h, sw, sh, 1, 1, a.depth, 1, 1, threads, img.ctypes.data)
+        secs = [L.dref_render(h, sw, sh, 1, 1, a.depth, 1, 1, threads, img.ctypes.data) for _ in range(a.steps)]
+        L.dref_scene_destroy(h)
+        kind = "reference"
+        what = "reference DumbRenderer (CPU threads) compiled from the reference sources"
+    else:
+        osc = O.OracleScene(tris, mat_id=mat, materials=mats, lights=lights, threads=threads)
+        build_s = 0.0
+        p = dr.render_params(sw, sh, dr.MODE_REFERENCE, samples=(1, 1), max_bounces=a.depth)
+        for _ in range(a.warmup):
+            osc.render_blocks(cam, p, threads=threads)
+        secs = []
+        for _ in range(a.steps):
+            t0 = time.time()
+            osc.render_blocks(cam, p, threads=threads)
+            secs.append(time.time() - t0)
+        kind = "port"
+        what = "oracle restatement of DumbRenderer (reference library unavailable on this machine)"
+    sec = float(np.mean(secs))
+    value = paths / sec / 1e6
+    out = {"metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": round(sec * 1e3, 1), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic", "impl": "reference",
+           "config": {"workload": f"reference-expressible twin of the full path trace ({len(tris):,} tris, 4 spherical lights), "
+                                  f"{sw}x{sh} sample of 1920x1080, 1 spp per step, depth {a.depth}",
+                      "octree_build_s": round(build_s, 1)},
+           "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": kind,
+                            "sample": f"{what}; {sw}x{sh} px x 1 spp per step ({paths:,} paths)"},
+           "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -120,6 +120,14 @@ def lib() -> ctypes.CDLL:
     L.dr_renderer_destroy.argtypes = [vp]
     L.dr_renderer_launch_count.restype = i64
     L.dr_renderer_launch_count.argtypes = [vp]
+    L.dr_renderer_set_profiling.restype = i32
+    L.dr_renderer_set_profiling.argtypes = [vp, i32]
+    L.dr_renderer_kernel_times.restype = i32
+    L.dr_renderer_kernel_times.argtypes = [vp, vp, vp]
+    L.dr_renderer_set_counting.restype = i32
+    L.dr_renderer_set_counting.argtypes = [vp, i32]
+    L.dr_renderer_counters.restype = i32
+    L.dr_renderer_counters.argtypes = [vp, vp]
     L.dr_render_blocks.restype = i32
     L.dr_render_blocks.argtypes = [vp, vp, vp, vp, i32, i32, vp, vp]
     _lib = L
@@ -401,6 +409,25 @@ class Renderer:
 
     def launches(self) -> int:
         return int(lib().dr_renderer_launch_count(self._h))
+
+    def set_profiling(self, enable: bool):
+        check(lib().dr_renderer_set_profiling(self._h, 1 if enable else 0))
+
+    def kernel_times(self):
+        """{class: (ms, launches)} for camera / trace / shade / shadow / resolve."""
+        ms = np.zeros(5, np.float64)
+        n = np.zeros(5, np.int64)
+        check(lib().dr_renderer_kernel_times(self._h, ms.ctypes.data, n.ctypes.data))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("camera", "trace", "shade", "shadow", "resolve"))}
+
+    def set_counting(self, enable: bool):
+        check(lib().dr_renderer_set_counting(self._h, 1 if enable else 0))
+
+    def counters(self):
+        c = np.zeros(6, np.int64)
+        check(lib().dr_renderer_counters(self._h, c.ctypes.data))
+        return dict(trace_rays=int(c[0]), trace_box=int(c[1]), trace_tri=int(c[2]), shadow_casts=int(c[3]),
+                    shadow_box=int(c[4]), shadow_tri=int(c[5]))
 
     def render_blocks(self, scene: Scene, cam: DrCamera, fb, start_block: int, end_block: int, params: DrRenderParams,
                       stream=None):

@@ -93,8 +93,12 @@ struct dr_renderer {
     size_t accum_slots = 0;
     void *ctrl = nullptr;
     long long launches = 0;
+    drk::Profiler prof;
+    unsigned long long *counters = nullptr;
+    bool counting = false;
 
     ~dr_renderer() {
+        cudaFree(counters);
         for (int k = 0; k < 2; k++) {
             for (int j = 0; j < 3; j++) cudaFree(q[k][j]);
             cudaFree(q3[k]);
@@ -466,6 +470,48 @@ void dr_renderer_destroy(dr_renderer *r) { delete r; }
 
 int64_t dr_renderer_launch_count(const dr_renderer *r) { return r ? r->launches : 0; }
 
+dr_status dr_renderer_set_profiling(dr_renderer *r, int32_t enable) {
+    if (!r) return fail(DR_E_ARG, "dr_renderer_set_profiling: renderer is NULL");
+    r->prof.reset();
+    r->prof.enabled = enable != 0;
+    return DR_OK;
+}
+
+dr_status dr_renderer_kernel_times(dr_renderer *r, double *ms, int64_t *launches) {
+    if (!r) return fail(DR_E_ARG, "dr_renderer_kernel_times: renderer is NULL");
+    cudaError_t e = r->prof.harvest();
+    if (e != cudaSuccess) return cuda_fail(e, "dr_renderer_kernel_times");
+    for (int k = 0; k < DR_KERNEL_CLASSES; k++) {
+        if (ms) ms[k] = r->prof.ms[k];
+        if (launches) launches[k] = r->prof.launches[k];
+    }
+    return DR_OK;
+}
+
+dr_status dr_renderer_set_counting(dr_renderer *r, int32_t enable) {
+    if (!r) return fail(DR_E_ARG, "dr_renderer_set_counting: renderer is NULL");
+    if (!r->counters) {
+        cudaError_t e = cudaMalloc((void **)&r->counters, 6 * sizeof(unsigned long long));
+        if (e != cudaSuccess) return cuda_fail(e, "dr_renderer_set_counting");
+    }
+    cudaError_t e = cudaMemset(r->counters, 0, 6 * sizeof(unsigned long long));
+    if (e != cudaSuccess) return cuda_fail(e, "dr_renderer_set_counting");
+    r->counting = enable != 0;
+    return DR_OK;
+}
+
+dr_status dr_renderer_counters(dr_renderer *r, int64_t *counts) {
+    if (!r || !counts) return fail(DR_E_ARG, "dr_renderer_counters: NULL argument");
+    unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
+    if (r->counters) {
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e == cudaSuccess) e = cudaMemcpy(h, r->counters, sizeof(h), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "dr_renderer_counters");
+    }
+    for (int k = 0; k < 6; k++) counts[k] = (int64_t)h[k];
+    return DR_OK;
+}
+
 dr_status dr_render_blocks(dr_renderer *r, const dr_scene *sc, const dr_camera *cam, float *fb, int32_t start_block,
                            int32_t end_block, const dr_render_params *p, void *stream_ptr) {
     if (!r || !sc || !cam || !fb || !p) return fail(DR_E_ARG, "dr_render_blocks: NULL argument");
@@ -546,11 +592,12 @@ dr_status dr_render_blocks(dr_renderer *r, const dr_scene *sc, const dr_camera *
     for (long long b = 0; b < total; b += wave) {
         W.wave_begin = b;
         W.wave_count = (int)std::min<long long>(wave, total - b);
-        e = drk::launch_wave(W, stream, &r->launches);
+        e = drk::launch_wave(W, stream, &r->launches, &r->prof, r->counting ? r->counters : nullptr);
         if (e != cudaSuccess) return cuda_fail(e, "dr_render_blocks: wave");
     }
     const float blend = (p->iteration <= 1) ? 1.0f : (1.0f / (float)p->iteration);
-    e = drk::launch_resolve(r->accum, fb, start_block, n_slots, p->width, p->height, 1.0f / (float)spp, blend, stream, &r->launches);
+    e = drk::launch_resolve(r->accum, fb, start_block, n_slots, p->width, p->height, 1.0f / (float)spp, blend, stream, &r->launches,
+                             &r->prof);
     if (e != cudaSuccess) return cuda_fail(e, "dr_render_blocks: resolve");
     return DR_OK;
 }

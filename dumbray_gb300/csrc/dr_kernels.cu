@@ -112,7 +112,20 @@ struct WaveArgs {
     ShadowQ sq;
     float *accum;           // [n_slots][4]
     Ctrl *ctrl;
+    unsigned long long *counters;  // counting pass only
 };
+
+// Warp-sum of per-lane traversal counts into the 64-bit counters (counting pass only).
+__device__ __forceinline__ void count_add(unsigned long long *c, int rays, int nb, int nt) {
+    unsigned r = __reduce_add_sync(0xFFFFFFFFu, (unsigned)rays);
+    unsigned b = __reduce_add_sync(0xFFFFFFFFu, (unsigned)nb);
+    unsigned t = __reduce_add_sync(0xFFFFFFFFu, (unsigned)nt);
+    if (lane_id() == 0) {
+        atomicAdd(c, (unsigned long long)r);
+        atomicAdd(c + 1, (unsigned long long)b);
+        atomicAdd(c + 2, (unsigned long long)t);
+    }
+}
 
 __device__ __forceinline__ void accum_add(float *acc, int slot, c3 c) {
     if (c.r != 0.0f) atomicAdd(acc + 4 * slot, c.r);
@@ -227,6 +240,7 @@ __global__ void __launch_bounds__(256) k_camera(WaveArgs A) {
     }
 }
 
+template <bool COUNT>
 __global__ void __launch_bounds__(256) k_trace(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const Queue Q = A.q[b & 1];
@@ -236,14 +250,15 @@ __global__ void __launch_bounds__(256) k_trace(WaveArgs A, int b) {
         int base = warp_fetch(&C->fetch_trace[b]);
         if (base >= n) break;
         int i = base + (int)lane_id();
+        int nb = 0, nt = 0;
         if (i < n) {
             float4 p0 = Q.p0[i], p1 = Q.p1[i];
             int4 p3 = Q.p3[i];
             Hit h;
-            int nb = 0, nt = 0;
-            cast_closest<false>(A.S, f3of(p0), f3of(p1), clip, p3.x, h, nb, nt);
+            cast_closest<COUNT>(A.S, f3of(p0), f3of(p1), clip, p3.x, h, nb, nt);
             A.hits[i] = make_float2(__int_as_float(h.tri), h.t);
         }
+        if (COUNT) count_add(A.counters, i < n ? 1 : 0, nb, nt);
     }
 }
 
@@ -333,6 +348,7 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
 // Reference light visibility (DumbRenderer.cu:361-428): cast from the light sample toward the
 // point; it counts if the first hit is the shaded triangle or lies within sqrt(8 eps) of the
 // point; otherwise the blocker's reflected colour decides whether the photon continues.
+template <bool COUNT>
 __global__ void __launch_bounds__(256) k_shadow_ref(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const Scene &S = A.S;
@@ -342,6 +358,7 @@ __global__ void __launch_bounds__(256) k_shadow_ref(WaveArgs A, int b) {
         int base = warp_fetch(&C->fetch_shadow[b]);
         if (base >= n) break;
         int i = base + (int)lane_id();
+        int casts = 0, nb = 0, nt = 0;
         if (i < n) {
             float4 s0 = A.sq.s0[i], s1 = A.sq.s1[i], s2 = A.sq.s2[i], s3 = A.sq.s3[i], s4 = A.sq.s4[i];
             f3 lo = f3of(s0), ld = f3of(s1), hp = f3of(s2);
@@ -351,8 +368,8 @@ __global__ void __launch_bounds__(256) k_shadow_ref(WaveArgs A, int b) {
             int restrict_obj = -1;
             for (int guard = 0; guard < 64; guard++) {
                 Hit h;
-                int nb = 0, nt = 0;
-                cast_closest<false>(S, lo, ld, clip, restrict_obj, h, nb, nt);
+                casts++;
+                cast_closest<COUNT>(S, lo, ld, clip, restrict_obj, h, nb, nt);
                 if (h.tri < 0) break;
                 f3 dd = xsub(h.p, hp);
                 if (h.tri == target || xdot(dd, dd) <= (8.0f * kEps)) {
@@ -367,6 +384,7 @@ __global__ void __launch_bounds__(256) k_shadow_ref(WaveArgs A, int b) {
                 } else break;
             }
         }
+        if (COUNT) count_add(A.counters + 3, casts, nb, nt);
     }
 }
 
@@ -537,6 +555,7 @@ __global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
 // Physical visibility: closest hit from the shading point toward the light point (segment
 // length 1 in units of the direction), ignoring the shading triangle; visible if nothing but
 // the light triangle is hit before t = 0.999.
+template <bool COUNT>
 __global__ void __launch_bounds__(256) k_shadow_phys(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const int n = *((volatile int *)&C->shadow_count[b]);
@@ -544,14 +563,15 @@ __global__ void __launch_bounds__(256) k_shadow_phys(WaveArgs A, int b) {
         int base = warp_fetch(&C->fetch_shadow[b]);
         if (base >= n) break;
         int i = base + (int)lane_id();
+        int nb = 0, nt = 0;
         if (i < n) {
             float4 s0 = A.sq.s0[i], s1 = A.sq.s1[i], s2 = A.sq.s2[i], s4 = A.sq.s4[i];
             Hit h;
-            int nb = 0, nt = 0;
-            cast_closest<false>(A.S, f3of(s0), f3of(s1), false, __float_as_int(s2.w), h, nb, nt);
+            cast_closest<COUNT>(A.S, f3of(s0), f3of(s1), false, __float_as_int(s2.w), h, nb, nt);
             bool vis = (h.tri < 0) || (h.tri == __float_as_int(s1.w)) || !(h.t < 0.999f);
             if (vis) accum_add(A.accum, __float_as_int(s0.w), mkc(s4.x, s4.y, s4.z));
         }
+        if (COUNT) count_add(A.counters + 3, i < n ? 1 : 0, nb, nt);
     }
 }
 
@@ -611,7 +631,57 @@ cudaError_t launch_cast(const Scene &S, const float *o, const float *d, const in
 
 size_t ctrl_bytes() { return sizeof(Ctrl); }
 
-cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launches) {
+Profiler::~Profiler() {
+    reset();
+    for (cudaEvent_t e : pool_) cudaEventDestroy(e);
+}
+cudaEvent_t Profiler::take() {
+    if (!pool_.empty()) {
+        cudaEvent_t e = pool_.back();
+        pool_.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+void Profiler::begin(int cls, cudaStream_t s) {
+    if (!enabled) return;
+    open_[cls] = take();
+    cudaEventRecord(open_[cls], s);
+}
+void Profiler::end(int cls, cudaStream_t s) {
+    if (!enabled || !open_[cls]) return;
+    cudaEvent_t e = take();
+    cudaEventRecord(e, s);
+    pending_.push_back({cls, {open_[cls], e}});
+    open_[cls] = nullptr;
+    launches[cls]++;
+}
+cudaError_t Profiler::harvest() {
+    cudaError_t err = cudaSuccess;
+    for (auto &p : pending_) {
+        cudaError_t e = cudaEventSynchronize(p.second.second);
+        float t = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, p.second.first, p.second.second);
+        if (e != cudaSuccess) err = e;
+        else ms[p.first] += t;
+        pool_.push_back(p.second.first);
+        pool_.push_back(p.second.second);
+    }
+    pending_.clear();
+    return err;
+}
+void Profiler::reset() {
+    harvest();
+    for (int k = 0; k < KC_COUNT; k++) {
+        ms[k] = 0.0;
+        launches[k] = 0;
+    }
+}
+
+cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launches, Profiler *prof,
+                        unsigned long long *counters) {
     WaveArgs A;
     A.S = W.scene;
     A.cam = W.camera;
@@ -647,21 +717,36 @@ cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launc
     A.sq.s4 = W.s[4];
     A.accum = W.accum;
     A.ctrl = reinterpret_cast<Ctrl *>(W.ctrl);
+    A.counters = counters;
+    const bool count = counters != nullptr;
     cudaError_t e = cudaMemsetAsync(W.ctrl, 0, sizeof(Ctrl), stream);
     if (e != cudaSuccess) return e;
     const int grid = sm_count() * 8;
     long long nl = 0;
+    Profiler dummy;
+    Profiler &P = prof ? *prof : dummy;
+    P.begin(KC_CAMERA, stream);
     k_camera<<<grid, 256, 0, stream>>>(A);
+    P.end(KC_CAMERA, stream);
     nl++;
     for (int b = 0; b <= W.max_bounces; b++) {
-        k_trace<<<grid, 256, 0, stream>>>(A, b);
+        P.begin(KC_TRACE, stream);
+        if (count) k_trace<true><<<grid, 256, 0, stream>>>(A, b);
+        else k_trace<false><<<grid, 256, 0, stream>>>(A, b);
+        P.end(KC_TRACE, stream);
+        P.begin(KC_SHADE, stream);
+        if (W.mode == DR_MODE_REFERENCE) k_shade_ref<<<grid, 256, 0, stream>>>(A, b);
+        else k_shade_phys<<<grid, 256, 0, stream>>>(A, b);
+        P.end(KC_SHADE, stream);
+        P.begin(KC_SHADOW, stream);
         if (W.mode == DR_MODE_REFERENCE) {
-            k_shade_ref<<<grid, 256, 0, stream>>>(A, b);
-            k_shadow_ref<<<grid, 256, 0, stream>>>(A, b);
+            if (count) k_shadow_ref<true><<<grid, 256, 0, stream>>>(A, b);
+            else k_shadow_ref<false><<<grid, 256, 0, stream>>>(A, b);
         } else {
-            k_shade_phys<<<grid, 256, 0, stream>>>(A, b);
-            k_shadow_phys<<<grid, 256, 0, stream>>>(A, b);
+            if (count) k_shadow_phys<true><<<grid, 256, 0, stream>>>(A, b);
+            else k_shadow_phys<false><<<grid, 256, 0, stream>>>(A, b);
         }
+        P.end(KC_SHADOW, stream);
         nl += 3;
     }
     if (launches) *launches += nl;
@@ -669,11 +754,13 @@ cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launc
 }
 
 cudaError_t launch_resolve(const float *accum, float *fb, int start_block, int n_slots, int width, int height, float inv_spp,
-                           float blend, cudaStream_t stream, long long *launches) {
+                           float blend, cudaStream_t stream, long long *launches, Profiler *prof) {
     int threads = 256;
     int blocks = (n_slots + threads - 1) / threads;
+    if (prof) prof->begin(KC_RESOLVE, stream);
     k_resolve<<<blocks, threads, 0, stream>>>(accum, reinterpret_cast<float4 *>(fb), start_block, n_slots, width, height,
                                              inv_spp, blend);
+    if (prof) prof->end(KC_RESOLVE, stream);
     if (launches) (*launches)++;
     return cudaGetLastError();
 }

@@ -1,6 +1,8 @@
 // dr_kernels.h - host-visible launch interface of the device kernels (no torch types).
 #pragma once
 #include <cuda_runtime.h>
+#include <utility>
+#include <vector>
 #include "../../include/dr_api.h"
 #include "dr_device.cuh"
 
@@ -30,12 +32,37 @@ struct WaveDesc {
     void *ctrl;
 };
 
+// Kernel classes for per-class timing.
+enum KernelClass { KC_CAMERA = 0, KC_TRACE = 1, KC_SHADE = 2, KC_SHADOW = 3, KC_RESOLVE = 4, KC_COUNT = 5 };
+
+// CUDA-event timing of kernel launches on their own stream, accumulated per kernel class.
+class Profiler {
+  public:
+    bool enabled = false;
+    ~Profiler();
+    void begin(int cls, cudaStream_t s);
+    void end(int cls, cudaStream_t s);
+    // Waits for the recorded events, adds their elapsed times to ms[] and recycles them.
+    cudaError_t harvest();
+    void reset();
+    double ms[KC_COUNT] = {0, 0, 0, 0, 0};
+    long long launches[KC_COUNT] = {0, 0, 0, 0, 0};
+
+  private:
+    cudaEvent_t take();
+    std::vector<cudaEvent_t> pool_;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending_;
+    cudaEvent_t open_[KC_COUNT] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+};
+
 size_t ctrl_bytes();
 
 cudaError_t launch_cast(const drd::Scene &S, const float *o, const float *d, const int *ignore, int n, int clip, int *hit_tri,
                         float *hit_t, int *nbox, int *ntri, cudaStream_t stream, long long *launches);
-cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launches);
+// counters (nullable): 6 x u64 = {trace rays, trace box tests, trace tri tests, shadow casts, shadow box tests, shadow tri tests}
+cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launches, Profiler *prof,
+                        unsigned long long *counters);
 cudaError_t launch_resolve(const float *accum, float *fb, int start_block, int n_slots, int width, int height, float inv_spp,
-                           float blend, cudaStream_t stream, long long *launches);
+                           float blend, cudaStream_t stream, long long *launches, Profiler *prof);
 
 }  // namespace drk

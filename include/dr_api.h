@@ -241,6 +241,31 @@ int32_t dr_block_count(int32_t width, int32_t height);
 /* Kernel launches issued by this renderer since creation (for launch accounting). */
 int64_t dr_renderer_launch_count(const dr_renderer *r);
 
+/* ---- instrumentation ---------------------------------------------------------------------
+ * Kernel classes timed with CUDA events recorded on the launch stream around each launch. */
+#define DR_KERNEL_CAMERA 0
+#define DR_KERNEL_TRACE 1
+#define DR_KERNEL_SHADE 2
+#define DR_KERNEL_SHADOW 3
+#define DR_KERNEL_RESOLVE 4
+#define DR_KERNEL_CLASSES 5
+
+/* Enables (1) or disables (0) per-class event timing for subsequent dr_render_blocks calls and
+ * clears the accumulated times. */
+dr_status dr_renderer_set_profiling(dr_renderer *r, int32_t enable);
+
+/* Waits for the recorded events and returns, per kernel class, the summed launch durations in
+ * milliseconds and the number of timed launches (arrays of DR_KERNEL_CLASSES; either may be NULL). */
+dr_status dr_renderer_kernel_times(dr_renderer *r, double *ms, int64_t *launches);
+
+/* Counting pass: while enabled, trace and shadow kernels also count, per cast, the reference's
+ * child-box slab tests and triangle tests (see dr_cast_counted).  Slower; never on a timed path. */
+dr_status dr_renderer_set_counting(dr_renderer *r, int32_t enable);
+
+/* Accumulated counts since counting was enabled (synchronises the device): counts[6] =
+ * {extension rays, their box tests, their triangle tests, shadow casts, their box tests, their triangle tests}. */
+dr_status dr_renderer_counters(dr_renderer *r, int64_t *counts);
+
 #ifdef __cplusplus
 }
 #endif

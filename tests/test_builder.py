@@ -1,0 +1,77 @@
+"""Host octree builder of the product vs the oracle's restatement of Octree::build: identical trees
+(node boxes bit for bit, split decisions, leaf triangle lists in order)."""
+import numpy as np
+import pytest
+
+import dumbray_gb300 as dr
+from dumbray_gb300 import scenes
+import _oracle as O
+
+
+def _same_tree(tris, **kw):
+    st, box, child, leaf, refs = dr.build_octree_host(tris, **kw)
+    cb, cc, ct = dr.canonical_tree(box, child, leaf, refs)
+    osc = O.OracleScene(tris)
+    ob, oc, ot = osc.canonical()
+    assert len(cb) == len(ob) == osc.node_count() == st["nodes"]
+    assert np.array_equal(cc, oc)
+    assert np.array_equal(ct, ot)
+    assert np.array_equal(cb.view(np.int32), ob.view(np.int32))
+    return st
+
+
+@pytest.mark.parametrize("level", [1, 3, 5])
+def test_builder_matches_oracle_displaced_icosphere(level):
+    tris = np.concatenate([scenes.displaced_icosphere(level, 0.1, 1), scenes.box((3, 3, 3), inward=True)])
+    _same_tree(tris)
+
+
+def test_builder_matches_oracle_c1_geometry():
+    st = _same_tree(scenes.box_and_icosphere(5)["tris"])
+    assert st["depth"] <= 24
+
+
+def test_builder_thread_count_does_not_change_tree():
+    tris = scenes.displaced_icosphere(4, 0.1, 3)
+    a = dr.build_octree_host(tris, threads=1)
+    b = dr.build_octree_host(tris, threads=7)
+    for x, y in zip(a[1:], b[1:]):
+        assert np.array_equal(np.asarray(x).view(np.int32), np.asarray(y).view(np.int32))
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 8, 9])
+def test_builder_tiny_scenes(n):
+    rng = np.random.default_rng(n)
+    tris = rng.uniform(-1, 1, size=(n, 3, 3)).astype(np.float32)
+    st = _same_tree(tris)
+    if n < 8:
+        assert st["nodes"] == 1 and st["leaves"] == 1  # root stays a leaf below the split threshold
+
+
+def test_builder_degenerate_and_duplicate_triangles():
+    rng = np.random.default_rng(5)
+    t = rng.uniform(-1, 1, size=(200, 3, 3)).astype(np.float32)
+    t[10:30] = t[10]                 # duplicates
+    t[40:60, 2] = t[40:60, 1]        # zero-area (two equal vertices)
+    t[60:70, :, 1] = 0.25            # coplanar with an axis plane
+    _same_tree(t)
+
+
+def test_builder_all_triangles_identical():
+    t = np.tile(np.array([[[0, 0, 0], [1, 0, 0], [0, 1, 0]]], np.float32), (50, 1, 1))
+    st = _same_tree(t)
+    assert st["refs"] >= 50
+
+
+def test_empty_scene_builds():
+    st, box, child, leaf, refs = dr.build_octree_host(np.zeros((0, 3, 3), np.float32))
+    assert st["refs"] == 0
+
+
+def test_builder_parameters_match_oracle_defaults():
+    tris = scenes.displaced_icosphere(3, 0.1, 1)
+    a = dr.build_octree_host(tris)
+    b = dr.build_octree_host(tris, max_depth=24, split_threshold=8)
+    assert a[0] == b[0]
+    shallow = dr.build_octree_host(tris, max_depth=2)
+    assert shallow[0]["depth"] <= 2

@@ -1,0 +1,129 @@
+"""dr_cast on the GPU against the oracle and the reference's golden vectors: hit triangle index
+bit-exact and t bit-exact (the device predicate uses explicitly rounded arithmetic), so the tie
+budget of 1e-5 of rays and the 1e-5 relative t tolerance are met with zero slack used."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+import dumbray_gb300 as dr
+from dumbray_gb300 import scenes
+import _oracle as O
+
+GOLD = Path(__file__).resolve().parent / "golden"
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_cast(scene, o, d, cuda, ignore=None, cull=True, counted=False):
+    to = torch.from_numpy(np.ascontiguousarray(o, np.float32)).to(cuda)
+    td = torch.from_numpy(np.ascontiguousarray(d, np.float32)).to(cuda)
+    ti = None if ignore is None else torch.from_numpy(np.ascontiguousarray(ignore, np.int32)).to(cuda)
+    out = dr.cast(scene, to, td, ignore=ti, cull_backfaces=cull, counted=counted)
+    torch.cuda.synchronize()
+    return [x.cpu().numpy() for x in out]
+
+
+def _assert_same(idx, t, ref_idx, ref_t):
+    assert np.array_equal(idx, ref_idx), f"{(idx != ref_idx).sum()} index mismatches"
+    hit = ref_idx >= 0
+    assert np.array_equal(t[hit].view(np.int32), ref_t[hit].view(np.int32))
+    assert np.all(t[~hit] == np.finfo(np.float32).max)
+
+
+@pytest.mark.parametrize("fixture,culls", [("cast_small.npz", (1, 0)), ("cast_c1.npz", (1,))])
+def test_cast_matches_reference_golden(cuda, fixture, culls):
+    g = np.load(GOLD / fixture)
+    sc = dr.Scene(g["tris"])
+    assert sc.stats()["nodes"] == int(g["nodes"])
+    for cull in culls:
+        idx, t = _gpu_cast(sc, g["o"], g["d"], cuda, cull=bool(cull))
+        _assert_same(idx, t, g[f"idx_cull{cull}"], g[f"t_cull{cull}"])
+
+
+@pytest.mark.parametrize("level,seed", [(3, 1), (5, 2), (6, 3)])
+def test_cast_matches_oracle_incoherent_and_primary(cuda, level, seed):
+    tris = np.concatenate([scenes.displaced_icosphere(level, 0.1, seed), scenes.box((3, 3, 3), inward=True)])
+    sc = dr.Scene(tris)
+    osc = O.OracleScene(tris)
+    o1, d1 = scenes.incoherent_rays(30000, -1.3, 1.3, seed=seed)
+    o2, d2 = scenes.primary_rays(96, 64, 50.0, (0.2, 0.5, -2.8), (0.0, 0.0, 0.0))
+    o, d = np.concatenate([o1, o2]), np.concatenate([d1, d2])
+    d[::13, 2] = 0.0
+    for cull in (True, False):
+        idx, t = _gpu_cast(sc, o, d, cuda, cull=cull)
+        oi, ot, _, _ = osc.cast(o, d, cull=cull)
+        _assert_same(idx, t, oi, ot)
+
+
+def test_cast_counters_equal_reference_traversal(cuda):
+    """Box tests follow the reference's sequential child scan (it stops at the returning child);
+    triangle tests are identical.  These are the C_box / C_tri of the bytes-per-ray formula."""
+    tris = np.concatenate([scenes.displaced_icosphere(5, 0.1, 1), scenes.box((3, 3, 3), inward=True)])
+    sc = dr.Scene(tris)
+    osc = O.OracleScene(tris)
+    o, d = scenes.incoherent_rays(20000, -1.2, 1.2, seed=7)
+    idx, t, nb, nt = _gpu_cast(sc, o, d, cuda, counted=True)
+    oi, ot, onb, ont = osc.cast(o, d)
+    _assert_same(idx, t, oi, ot)
+    assert np.array_equal(nt, ont)
+    assert np.array_equal(nb, onb)
+
+
+def test_cast_ignore_triangle_is_validator(cuda):
+    """ignore_tri plays validateNotSameAsObject: re-casting from each hit point, ignoring the hit
+    triangle, equals the oracle with the same restriction."""
+    tris = np.concatenate([scenes.displaced_icosphere(4, 0.1, 5), scenes.box((3, 3, 3), inward=True)])
+    sc = dr.Scene(tris)
+    osc = O.OracleScene(tris)
+    o, d = scenes.incoherent_rays(8000, -1.2, 1.2, seed=8)
+    idx, t = _gpu_cast(sc, o, d, cuda, cull=False)
+    hit = idx >= 0
+    p = (o + d * t[:, None])[hit].astype(np.float32)
+    rng = np.random.default_rng(0)
+    nd = rng.normal(size=p.shape).astype(np.float32)
+    ig = idx[hit]
+    i2, t2 = _gpu_cast(sc, p, nd, cuda, ignore=ig, cull=False)
+    oi, ot, _, _ = osc.cast(p, nd, ignore=ig, cull=False)
+    _assert_same(i2, t2, oi, ot)
+    assert not np.any(i2 == ig)
+
+
+@pytest.mark.parametrize("n", [1, 5, 9])
+def test_cast_tiny_scenes_and_root_leaf(cuda, n):
+    rng = np.random.default_rng(n)
+    tris = rng.uniform(-1, 1, size=(n, 3, 3)).astype(np.float32)
+    sc = dr.Scene(tris)
+    osc = O.OracleScene(tris)
+    o, d = scenes.incoherent_rays(5000, -1, 1, seed=n)
+    for cull in (True, False):
+        idx, t = _gpu_cast(sc, o, d, cuda, cull=cull)
+        oi, ot, _, _ = osc.cast(o, d, cull=cull)
+        _assert_same(idx, t, oi, ot)
+
+
+def test_cast_empty_scene_and_empty_batch(cuda):
+    sc = dr.Scene(np.zeros((0, 3, 3), np.float32))
+    o, d = scenes.incoherent_rays(100, -1, 1, seed=1)
+    idx, t = _gpu_cast(sc, o, d, cuda)
+    assert np.all(idx == -1)
+    sc2 = dr.Scene(scenes.icosphere(1))
+    idx, t = _gpu_cast(sc2, o[:0], d[:0], cuda)
+    assert idx.shape == (0,)
+
+
+def test_cast_degenerate_geometry(cuda):
+    rng = np.random.default_rng(5)
+    t = rng.uniform(-1, 1, size=(300, 3, 3)).astype(np.float32)
+    t[10:30] = t[10]
+    t[40:60, 2] = t[40:60, 1]
+    t[60:70, :, 1] = 0.25
+    sc = dr.Scene(t)
+    osc = O.OracleScene(t)
+    o, d = scenes.incoherent_rays(20000, -1.2, 1.2, seed=3)
+    o[::5, 1] = 0.25
+    d[::9, 1] = 0.0
+    for cull in (True, False):
+        idx, tt = _gpu_cast(sc, o, d, cuda, cull=cull)
+        oi, ot, _, _ = osc.cast(o, d, cull=cull)
+        _assert_same(idx, tt, oi, ot)

@@ -1,0 +1,192 @@
+"""dr_render_blocks on the GPU.
+
+Reference semantics: same scene, same counter-based random numbers -> the GPU and the oracle
+follow the same paths, so images agree per pixel up to float rounding of transcendentals
+(tolerance stated per test), and both agree statistically with the reference DumbRenderer.
+Physical mode: agreement with the FP64 oracle within 1% relative RMSE."""
+from pathlib import Path
+import sys
+
+import numpy as np
+import pytest
+import torch
+
+import dumbray_gb300 as dr
+from dumbray_gb300 import scenes
+import _oracle as O
+
+GOLD = Path(__file__).resolve().parent / "golden"
+sys.path.insert(0, str(GOLD))
+from make_golden import render_scene  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_render(scene, cam, p, cuda, fb=None, start=0, end=None):
+    nb = dr.block_count(p.width, p.height)
+    end = nb if end is None else end
+    if fb is None:
+        fb = dr.new_frame_buffer(p.width, p.height, cuda)
+    r = dr.Renderer(1 << 16)
+    r.render_blocks(scene, cam, fb, start, end, p)
+    torch.cuda.synchronize()
+    return fb, r
+
+
+def _compare(gpu, ora, tol_rel=2e-3, max_bad_frac=0.02, mean_tol=5e-3):
+    """Per-pixel: |gpu - oracle| <= tol_rel * max(|oracle|, 0.01) for all but max_bad_frac of the
+    channels (paths may split where a transcendental rounds differently); image means within mean_tol."""
+    gpu = gpu[..., :3].astype(np.float64)
+    ora = ora[..., :3].astype(np.float64)
+    assert np.isfinite(gpu).all()
+    bad = np.abs(gpu - ora) > tol_rel * np.maximum(np.abs(ora), 0.01)
+    assert bad.mean() <= max_bad_frac, f"{bad.mean():.4f} of channels differ"
+    m = max(abs(ora.mean()), 1e-6)
+    assert abs(gpu.mean() - ora.mean()) / m <= mean_tol, (gpu.mean(), ora.mean())
+
+
+def _ref_scene(kind, light="spherical"):
+    tris, mat, mats, lights, cam = render_scene(kind)
+    if light == "soft":
+        lights = [dr.soft_directional_light((1.2, 1.2, 1.2), (0.25, -1.0, 0.3), 3.0, 0.05)]
+    elif light == "directional":
+        lights = [dr.directional_light((1.0, 0.9, 0.8), (0.2, -1.0, 0.1), 3.0)]
+    elif light == "two":
+        lights = lights + [dr.soft_directional_light((0.5, 0.5, 0.8), (-0.3, -1.0, 0.2), 3.0, 0.02)]
+    return tris, mat, mats, lights, cam
+
+
+@pytest.mark.parametrize("kind", ["diffuse", "metal", "ss"])
+@pytest.mark.parametrize("light", ["spherical", "soft", "directional", "two"])
+def test_reference_mode_matches_oracle(cuda, kind, light):
+    tris, mat, mats, lights, cam = _ref_scene(kind, light)
+    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights)
+    osc = O.OracleScene(tris, mat_id=mat, materials=mats, lights=lights)
+    p = dr.render_params(40, 28, dr.MODE_REFERENCE, samples=(2, 3), max_bounces=3, seed=5)
+    fb, _ = _gpu_render(sc, cam, p, cuda)
+    gpu = dr.blockmajor_to_image(fb, 40, 28)
+    ora = dr.blockmajor_to_image(osc.render_blocks(cam, p), 40, 28)
+    _compare(gpu, ora)
+
+
+@pytest.mark.parametrize("lens", [dr.LENS_DEFAULT_PERSPECTIVE, dr.LENS_SIMPLE_STOCHASTIC, dr.LENS_SPHERICAL_SEGMENT])
+@pytest.mark.parametrize("boxing", [dr.BOXING_HEIGHT, dr.BOXING_WIDTH, dr.BOXING_MIN, dr.BOXING_MAX])
+def test_reference_lenses_and_boxing(cuda, lens, boxing):
+    tris, mat, mats, lights, _ = _ref_scene("diffuse")
+    cam = dr.camera(lens, position=(0.0, 0.0, -0.95), angle=(70.0, 50.0), focal_distance=2.0, softness=0.01,
+                    filter=(1.0, 0.9, 0.8))
+    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights)
+    osc = O.OracleScene(tris, mat_id=mat, materials=mats, lights=lights)
+    p = dr.render_params(33, 19, dr.MODE_REFERENCE, samples=(2, 2), max_bounces=2, boxing=boxing, seed=9)
+    fb, _ = _gpu_render(sc, cam, p, cuda)
+    _compare(dr.blockmajor_to_image(fb, 33, 19), dr.blockmajor_to_image(osc.render_blocks(cam, p), 33, 19))
+
+
+@pytest.mark.parametrize("cull", [True, False])
+@pytest.mark.parametrize("bounces", [0, 1, 5])
+def test_reference_cull_and_bounce_limit(cuda, cull, bounces):
+    tris, mat, mats, lights, cam = _ref_scene("ss")
+    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights)
+    osc = O.OracleScene(tris, mat_id=mat, materials=mats, lights=lights)
+    p = dr.render_params(24, 24, dr.MODE_REFERENCE, samples=(2, 2), max_bounces=bounces, cull_backfaces=cull, seed=3)
+    fb, _ = _gpu_render(sc, cam, p, cuda)
+    _compare(dr.blockmajor_to_image(fb, 24, 24), dr.blockmajor_to_image(osc.render_blocks(cam, p), 24, 24))
+
+
+def test_block_range_and_progressive_blend(cuda):
+    """Blocks outside [start, end) are untouched; iteration k blends with weight 1/k like
+    blendBlockPixelColor (DumbRenderer.cu:64, BlockBasedFrameBuffer.impl.cuh:152-156)."""
+    tris, mat, mats, lights, cam = _ref_scene("diffuse")
+    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights)
+    osc = O.OracleScene(tris, mat_id=mat, materials=mats, lights=lights)
+    W, H = 48, 40
+    nb = dr.block_count(W, H)
+    rng = np.random.default_rng(0)
+    init = rng.uniform(0, 1, size=(nb * 128, 4)).astype(np.float32)
+    fb = torch.from_numpy(init.copy()).to(cuda)
+    ofb = init.copy()
+    for it in (1, 2, 3):
+        p = dr.render_params(W, H, dr.MODE_REFERENCE, samples=(1, 2), max_bounces=2, iteration=it, seed=4)
+        _gpu_render(sc, cam, p, cuda, fb=fb, start=3, end=nb - 2)
+        osc.render_blocks(cam, p, fb=ofb, start=3, end=nb - 2)
+    g = fb.cpu().numpy()
+    assert np.array_equal(g[: 3 * 128], init[: 3 * 128])
+    assert np.array_equal(g[(nb - 2) * 128:], init[(nb - 2) * 128:])
+    _compare(dr.blockmajor_to_image(g, W, H), dr.blockmajor_to_image(ofb, W, H))
+
+
+@pytest.mark.parametrize("kind", ["diffuse", "metal", "ss"])
+def test_gpu_matches_reference_renderer_statistically(cuda, kind):
+    """8 GPU runs (1024 spp each) vs 4 reference DumbRenderer runs (golden fixture, 512 iterations
+    each): MSE of the run means within 1.5x of the predicted variance, image means within 4 SE."""
+    from _stats import compare_runs
+    g = np.load(GOLD / f"render_{kind}.npz")
+    size, bounces = int(g["size"]), int(g["bounces"])
+    tris, mat, mats, lights, cam = render_scene(kind)
+    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights)
+    runs = []
+    for seed in range(100, 108):
+        p = dr.render_params(size, size, dr.MODE_REFERENCE, samples=(32, 32), max_bounces=bounces, seed=seed)
+        fb, _ = _gpu_render(sc, cam, p, cuda)
+        runs.append(dr.blockmajor_to_image(fb, size, size))
+    compare_runs(runs, g["runs"])
+
+
+def _phys_scene(level=3):
+    c = scenes.box_and_icosphere(level)
+    mats = [dr.lambert((0.7, 0.7, 0.7)), dr.lambert((0.7, 0.1, 0.1)), dr.lambert((0.0, 0.0, 0.0), emission=(10.0, 10.0, 10.0))]
+    return c["tris"], c["mat_id"], mats
+
+
+@pytest.mark.parametrize("lens,angle", [(dr.LENS_PINHOLE, 60.0), (dr.LENS_FISHEYE, 170.0), (dr.LENS_SPHERICAL, 120.0)])
+def test_physical_mode_matches_fp64_oracle(cuda, lens, angle):
+    tris, mat, mats = _phys_scene(3)
+    sc = dr.Scene(tris, mat_id=mat, materials=mats)
+    osc = O.OracleScene(tris, mat_id=mat, materials=mats)
+    cam = dr.camera(lens, position=(0.0, 0.0, -0.99), angle=(angle, angle * 0.6))
+    p = dr.render_params(32, 32, dr.MODE_PHYSICAL, samples=(4, 4), max_bounces=4, seed=2)
+    fb, _ = _gpu_render(sc, cam, p, cuda)
+    gpu = dr.blockmajor_to_image(fb, 32, 32)[..., :3].astype(np.float64)
+    ora = dr.blockmajor_to_image(osc.render_blocks(cam, p), 32, 32)[..., :3].astype(np.float64)
+    rel_rmse = np.sqrt(np.mean((gpu - ora) ** 2)) / max(ora.mean(), 1e-6)
+    assert rel_rmse <= 0.01, rel_rmse
+
+
+def test_physical_materials_and_per_triangle_params(cuda):
+    """Lambert / mirror / glossy with per-triangle albedo, roughness and emission overrides."""
+    c = scenes.box_and_icosphere(3)
+    tris = c["tris"]
+    n = len(tris)
+    h = scenes.tri_hash_u32(np.arange(n), 1) % 100
+    mat = np.where(h < 60, 0, np.where(h < 85, 1, 2)).astype(np.int32)
+    mats = [dr.lambert(), dr.mirror(), dr.glossy(roughness=0.2)]
+    rng = np.random.default_rng(1)
+    albedo = rng.uniform(0.2, 0.8, size=(n, 3)).astype(np.float32)
+    rough = rng.uniform(0.05, 0.4, size=n).astype(np.float32)
+    emission = np.zeros((n, 3), np.float32)
+    lo = c["n_room"] + c["n_sphere"]
+    emission[lo:] = 10.0
+    mat[lo:] = 0
+    sc = dr.Scene(tris, mat_id=mat, materials=mats)
+    sc.set_triangle_params(albedo, emission, rough)
+    osc = O.OracleScene(tris, mat_id=mat, materials=mats)
+    osc.set_triangle_params(albedo, emission, rough)
+    cam = dr.camera(dr.LENS_PINHOLE, position=(0.0, 0.0, -0.99), angle=60.0)
+    p = dr.render_params(32, 32, dr.MODE_PHYSICAL, samples=(4, 4), max_bounces=6, seed=8)
+    fb, _ = _gpu_render(sc, cam, p, cuda)
+    gpu = dr.blockmajor_to_image(fb, 32, 32)[..., :3].astype(np.float64)
+    ora = dr.blockmajor_to_image(osc.render_blocks(cam, p), 32, 32)[..., :3].astype(np.float64)
+    assert np.sqrt(np.mean((gpu - ora) ** 2)) / max(ora.mean(), 1e-6) <= 0.01
+
+
+def test_render_argument_errors(cuda):
+    tris, mat, mats, lights, cam = _ref_scene("diffuse")
+    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights)
+    fb = dr.new_frame_buffer(16, 16, cuda)
+    r = dr.Renderer(1 << 12)
+    with pytest.raises(dr.DumbRayError):
+        r.render_blocks(sc, cam, fb, 0, 99, dr.render_params(16, 16))
+    with pytest.raises(dr.DumbRayError):
+        r.render_blocks(sc, cam, fb, 0, 2, dr.render_params(16, 16, mode=dr.MODE_PHYSICAL))  # reference lens in physical mode
+    with pytest.raises(dr.DumbRayError):
+        r.render_blocks(sc, cam, fb, 0, 2, dr.render_params(16, 16, max_bounces=65))
