@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--wave", type=int, default=1 << 22)
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer e2e pass (profiling cases)")
+    ap.add_argument("--no-count", action="store_true", help="skip the traversal-counting pass (profiling cases)")
     return ap.parse_args()
 
 
@@ -236,6 +238,8 @@ def run_ours(a):
     value = world * paths_per_frame * a.steps / (ms / 1e3) / 1e6
 
     # e2e through the public API with host buffers (pinned), copies inside the timed region
+    if a.no_e2e:
+        a.steps_e2e = 0
     host_fb = torch.zeros(fb.shape, dtype=torch.float32).pin_memory()
     host_out = torch.zeros(fb.shape, dtype=torch.float32).pin_memory()
     torch.cuda.synchronize()
@@ -243,7 +247,7 @@ def run_ours(a):
         torch.distributed.barrier()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
-    for i in range(a.steps):
+    for i in range(0 if a.no_e2e else a.steps):
         fb.copy_(host_fb, non_blocking=True)
         rend.render_blocks(scene, cam, fb, 0, nb, params(a.warmup + a.steps + i), stream)
         host_out.copy_(fb, non_blocking=True)
@@ -254,14 +258,17 @@ def run_ours(a):
         t = torch.tensor([ms_e2e], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms_e2e = float(t.item())
-    e2e = world * paths_per_frame * a.steps / (ms_e2e / 1e3) / 1e6
+    e2e = world * paths_per_frame * a.steps / (ms_e2e / 1e3) / 1e6 if not a.no_e2e else None
     fb_bytes = fb.numel() * 4
 
     # counting pass (untimed): reference traversal counts of the extension rays of one frame
-    rend.set_counting(True)
-    rend.render_blocks(scene, cam, fb, 0, nb, params(0), stream)
-    cnt = rend.counters()
-    rend.set_counting(False)
+    if a.no_count:
+        cnt = dict(trace_rays=0, trace_box=0, trace_tri=0, shadow_casts=0, shadow_box=0, shadow_tri=0)
+    else:
+        rend.set_counting(True)
+        rend.render_blocks(scene, cam, fb, 0, nb, params(0), stream)
+        cnt = rend.counters()
+        rend.set_counting(False)
     c_box = cnt["trace_box"] / max(1, cnt["trace_rays"])
     c_tri = cnt["trace_tri"] / max(1, cnt["trace_rays"])
     bytes_per_ray = 40.0 + 32.0 * c_box + 36.0 * c_tri
@@ -281,7 +288,7 @@ def run_ours(a):
                    "lens": a.lens, "mode": "physical", "wave_paths": a.wave, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (scene ~0.3 GB, wavefront queues ~2 GB), no flush",
                    "scene_build_s": round(build_s, 2)},
-        "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": fb_bytes, "d2h_bytes_per_step": fb_bytes},
+        "e2e": {"value": None if e2e is None else round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": fb_bytes, "d2h_bytes_per_step": fb_bytes},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None, "kernel": "k_trace",
