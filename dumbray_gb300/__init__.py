@@ -511,3 +511,17 @@ def image_to_blockmajor(img: np.ndarray) -> np.ndarray:
     pad = np.zeros((bh * BLOCK_H, bw * BLOCK_W, img.shape[2]), img.dtype)
     pad[:h, :w] = img
     return np.ascontiguousarray(pad.reshape(bh, BLOCK_H, bw, BLOCK_W, -1).transpose(0, 2, 1, 3, 4).reshape(-1, img.shape[2]))
+
+
+def render_blocks_noalloc(scene: Scene, cam: DrCamera, fb, start_block: int, end_block: int, params: DrRenderParams,
+                          stream=None):
+    """dr_render_blocks_noalloc: the same render as Renderer.render_blocks for callers that cannot
+    allocate device memory while rendering (e.g. inside a CUDA stream capture); uses the library's
+    fixed 16 MiB device scratch array, at most 2048 blocks per call, calls on different streams race."""
+    L = lib()
+    fn = L.dr_render_blocks_noalloc
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                   ctypes.c_void_p]
+    check(fn(scene.handle, ctypes.byref(cam), _ptr(fb), int(start_block), int(end_block), ctypes.byref(params),
+             _stream_ptr(stream)))

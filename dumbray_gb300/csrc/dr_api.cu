@@ -14,6 +14,7 @@
 #include "../../include/dr_api.h"
 #include "dr_kernels.h"
 #include "octree_build.h"
+#include "dr_internal.h"
 
 namespace {
 
@@ -603,3 +604,7 @@ dr_status dr_render_blocks(dr_renderer *r, const dr_scene *sc, const dr_camera *
 }
 
 }  // extern "C"
+
+const drd::Scene *dr_internal_scene_device(const dr_scene *scene) { return scene ? &scene->dev : nullptr; }
+
+void dr_internal_set_error(const char *msg) { g_err = msg ? msg : ""; }

@@ -235,6 +235,21 @@ void dr_renderer_destroy(dr_renderer *r);
 dr_status dr_render_blocks(dr_renderer *r, const dr_scene *scene, const dr_camera *camera, float *fb_blockmajor,
                            int32_t start_block, int32_t end_block, const dr_render_params *params, void *stream);
 
+/* Allocation-free variant of dr_render_blocks.  It has no counterpart in the reference: it exists
+ * for callers that cannot allocate device memory while they render (a host rendering inside a CUDA
+ * stream capture, a plugin host whose device memory belongs to another pool, a latency-critical
+ * thread that must not let cudaMalloc/cudaFree synchronise the device).  Same arguments, results
+ * and blending as dr_render_blocks, but no dr_renderer: the scratch is one file-scope device array
+ * of DR_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until process exit.
+ * At most DR_NOALLOC_MAX_BLOCKS blocks per call (more returns DR_E_CAPACITY).  All calls share the
+ * array: calls whose work overlaps on the GPU race, so issue them on one stream.  The first call on
+ * a device looks up the array's address with that device current; make it before any stream
+ * capture starts.  Calls no cudaMalloc, cudaFree or allocating library routine. */
+#define DR_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+#define DR_NOALLOC_MAX_BLOCKS 2048
+dr_status dr_render_blocks_noalloc(const dr_scene *scene, const dr_camera *camera, float *fb_blockmajor,
+                                   int32_t start_block, int32_t end_block, const dr_render_params *params, void *stream);
+
 /* Number of blocks of a width x height image (ceil(W/8) * ceil(H/16)). */
 int32_t dr_block_count(int32_t width, int32_t height);
 
