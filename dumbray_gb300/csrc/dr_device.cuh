@@ -95,26 +95,50 @@ __device__ __forceinline__ bool slab_hit(float lx, float ly, float lz, float hx,
     return mn != FLT_MAX;
 }
 
+// One edge condition of Triangle::containsVertex (Triangle.impl.h:292-302):
+//     rn(rn(X / rn(sqrt(P))) + S) >= rn(Y / rn(sqrt(Q)))
+// with X = e.px, P = px.px, Y = -(e.f), Q = f.f (all exactly rounded dot products).
+// Decided first with rsqrtf (documented max error 2 ulp): the fast left and right sides differ from
+// the exactly rounded ones by at most ~3 ulp each, so a difference D outside the margin
+// M = 2^-19 (|L| + |R| + S) (about 16 ulp) has the same sign as the exact difference; inside the
+// margin, or for inf/NaN operands, the exact IEEE expression is evaluated.  Results are therefore
+// bit-identical to the reference's host arithmetic while the common case avoids two IEEE divisions
+// and two IEEE square roots.
+__device__ __forceinline__ bool edge_ok(f3 e, f3 px, f3 f) {
+    const float S = 32 * kEps;
+    const float X = xdot(e, px), P = xdot(px, px), Y = -xdot(e, f), Q = xdot(f, f);
+    const float Lf = __fadd_rn(__fmul_rn(X, rsqrtf(P)), S);
+    const float Rf = __fmul_rn(Y, rsqrtf(Q));
+    const float D = __fsub_rn(Lf, Rf);
+    const float M = 1.9073486328125e-06f * (fabsf(Lf) + fabsf(Rf) + S);
+    if (D > M) return true;
+    if (D < -M) return false;
+    return __fadd_rn(__fdiv_rn(X, __fsqrt_rn(P)), S) >= __fdiv_rn(Y, __fsqrt_rn(Q));
+}
+
 // Triangle::containsVertex (Triangle.impl.h:283-302)
 __device__ __forceinline__ bool contains_vertex(f3 a, f3 b, f3 c, f3 p) {
     if (xeq(a, b) || xeq(b, c) || xeq(c, a)) return false;
     if (xeq(p, a) || xeq(p, b) || xeq(p, c)) return true;
-    const float S = 32 * kEps;
     f3 ab = xsub(b, a), bc = xsub(c, b), ca = xsub(a, c);
-    f3 ax = xsub(p, a), bx = xsub(p, b), cx = xsub(p, c);
-    if (!(__fadd_rn(__fdiv_rn(xdot(ab, ax), xmag(ax)), S) >= __fdiv_rn(-xdot(ab, ca), xmag(ca)))) return false;
-    if (!(__fadd_rn(__fdiv_rn(xdot(bc, bx), xmag(bx)), S) >= __fdiv_rn(-xdot(bc, ab), xmag(ab)))) return false;
-    return __fadd_rn(__fdiv_rn(xdot(ca, cx), xmag(cx)), S) >= __fdiv_rn(-xdot(ca, bc), xmag(bc));
+    if (!edge_ok(ab, xsub(p, a), ca)) return false;
+    if (!edge_ok(bc, xsub(p, b), ab)) return false;
+    return edge_ok(ca, xsub(p, c), bc);
 }
 
-// Triangle::cast (Triangle.impl.h:334-348)
-__device__ __forceinline__ bool tri_cast(f3 a, f3 b, f3 c, f3 o, f3 d, bool clip, float &dist, f3 &hp) {
+// Triangle::cast (Triangle.impl.h:334-348), with the caller's strict-min and validator checks
+// (castInLeaf, Octree.impl.cuh:596-603) moved ahead of the containment test: a triangle whose
+// distance is not below `best`, or that is the ignored object, cannot change the leaf's result,
+// so skipping its containment test leaves every result unchanged.
+__device__ __forceinline__ bool tri_cast_better(f3 a, f3 b, f3 c, int id, f3 o, f3 d, bool clip, int ignore, float best,
+                                                float &dist, f3 &hp) {
     f3 n = xcross(xsub(b, a), xsub(c, a));
     float dp = xdot(xsub(a, o), n);
     if (clip && (dp < -kEps)) return false;
     float dirp = xdot(d, n);
     if (__fmul_rn(dp, dirp) <= 0.0f) return false;
     float distance = __fdiv_rn(dp, dirp);
+    if (!(distance < best) || id == ignore) return false;
     f3 hv = xadd(o, xmul(d, distance));
     if (!contains_vertex(a, b, c, hv)) return false;
     dist = distance;
@@ -143,9 +167,11 @@ __device__ __forceinline__ bool cast_leaf(const Scene &S, int first, int count, 
         float dist;
         f3 hp;
         ntri++;
-        bool ok = tri_cast(f3of(A), f3of(B), f3of(C), o, d, clip, dist, hp);
-        if (ok && id == ignore) ok = false;
-        if (ok && dist < best) { best = dist; bp = hp; bi = id; }
+        if (tri_cast_better(f3of(A), f3of(B), f3of(C), id, o, d, clip, ignore, best, dist, hp)) {
+            best = dist;
+            bp = hp;
+            bi = id;
+        }
     }
     if (best != FLT_MAX && bp.x >= lx && bp.y >= ly && bp.z >= lz && bp.x <= hx && bp.y <= hy && bp.z <= hz) {
         h.tri = bi;

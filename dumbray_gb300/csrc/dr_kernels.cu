@@ -16,6 +16,7 @@
 // sequence with no host synchronisation.
 #include "dr_kernels.h"
 #include "dr_shading.cuh"
+#include "dr_trace.cuh"
 
 #include <cstdio>
 
@@ -42,24 +43,44 @@ __device__ __forceinline__ int warp_fetch(int *counter) {
 }
 
 // ---------------------------------------------------------------------------------------------
-template <bool COUNT>
-__global__ void __launch_bounds__(256) k_cast(Scene S, const float *__restrict__ o, const float *__restrict__ d,
-                                              const int *__restrict__ ignore, int n, int clip, int *__restrict__ hit_tri,
-                                              float *__restrict__ hit_t, int *__restrict__ nbox, int *__restrict__ ntri) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        f3 ro = mkf3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
-        f3 rd = mkf3(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
-        int ign = ignore ? ignore[i] : -1;
-        Hit h;
-        int nb = 0, nt = 0;
-        cast_closest<COUNT>(S, ro, rd, clip != 0, ign, h, nb, nt);
+// dr_cast source: warp w of the grid owns rays [w * kChunk, (w + 1) * kChunk).
+struct BatchSource {
+    const float *o, *d;
+    const int *ignore;
+    int *hit_tri, *nbox, *ntri;
+    float *hit_t;
+    int n;
+    bool given;
+    __device__ __forceinline__ bool next(int &b, int &e) {
+        if (given) return false;
+        given = true;
+        int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+        b = w * kChunk;
+        e = min(b + kChunk, n);
+        return b < n;
+    }
+    __device__ __forceinline__ void load(int i, f3 &ro, f3 &rd, int &ign) {
+        ro = mkf3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
+        rd = mkf3(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
+        ign = ignore ? ignore[i] : -1;
+    }
+    __device__ __forceinline__ void store(int i, const Hit &h, int nb, int nt) {
         hit_tri[i] = h.tri;
         hit_t[i] = h.tri >= 0 ? h.t : FLT_MAX;
-        if (COUNT) {
+        if (nbox) {
             nbox[i] = nb;
             ntri[i] = nt;
         }
     }
+};
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_cast(Scene S, const float *__restrict__ o, const float *__restrict__ d,
+                                              const int *__restrict__ ignore, int n, int clip, int *__restrict__ hit_tri,
+                                              float *__restrict__ hit_t, int *__restrict__ nbox, int *__restrict__ ntri) {
+    uint32_t stack[kStack];
+    BatchSource src{o, d, ignore, hit_tri, COUNT ? nbox : nullptr, COUNT ? ntri : nullptr, hit_t, n, false};
+    trace_persistent<COUNT>(S, clip != 0, src, stack);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -240,26 +261,63 @@ __global__ void __launch_bounds__(256) k_camera(WaveArgs A) {
     }
 }
 
+// Chunked work fetch from a device counter (warp-uniform).  The chunk shrinks with the queue:
+// about 4 chunks per resident warp (152 SMs x 24 warps), between 32 and kChunk rays, so short
+// queues (late bounces, shadow queues) still spread over every resident warp.
+__device__ __forceinline__ int chunk_for(int n) { return max(32, min(kChunk, (n / (152 * 24 * 4)) & ~31)); }
+__device__ __forceinline__ bool fetch_chunk(int *counter, int n, int chunk, int &b, int &e) {
+    int base = 0;
+    if ((threadIdx.x & 31u) == 0) base = atomicAdd(counter, chunk);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base >= n) return false;
+    b = base;
+    e = min(base + chunk, n);
+    return true;
+}
+
+struct TraceSource {
+    Queue Q;
+    float2 *hits;
+    int *fetch;
+    int n, chunk;
+    long long rays, nb, nt;
+    __device__ __forceinline__ bool next(int &b, int &e) { return fetch_chunk(fetch, n, chunk, b, e); }
+    __device__ __forceinline__ void load(int i, f3 &o, f3 &d, int &ign) {
+        float4 p0 = Q.p0[i], p1 = Q.p1[i];
+        o = f3of(p0);
+        d = f3of(p1);
+        ign = Q.p3[i].x;
+    }
+    __device__ __forceinline__ void store(int i, const Hit &h, int b_, int t_) {
+        hits[i] = make_float2(__int_as_float(h.tri), h.t);
+        rays++;
+        nb += b_;
+        nt += t_;
+    }
+};
+
+__device__ __forceinline__ void count_add64(unsigned long long *c, long long rays, long long nb, long long nt) {
+    for (int off = 16; off > 0; off >>= 1) {
+        rays += __shfl_xor_sync(0xFFFFFFFFu, rays, off);
+        nb += __shfl_xor_sync(0xFFFFFFFFu, nb, off);
+        nt += __shfl_xor_sync(0xFFFFFFFFu, nt, off);
+    }
+    if ((threadIdx.x & 31u) == 0) {
+        atomicAdd(c, (unsigned long long)rays);
+        atomicAdd(c + 1, (unsigned long long)nb);
+        atomicAdd(c + 2, (unsigned long long)nt);
+    }
+}
+
 template <bool COUNT>
 __global__ void __launch_bounds__(256) k_trace(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
-    const Queue Q = A.q[b & 1];
     const int n = *((volatile int *)&C->ray_count[b]);
     const bool clip = A.mode == DR_MODE_REFERENCE ? (A.clip != 0) : false;
-    for (;;) {
-        int base = warp_fetch(&C->fetch_trace[b]);
-        if (base >= n) break;
-        int i = base + (int)lane_id();
-        int nb = 0, nt = 0;
-        if (i < n) {
-            float4 p0 = Q.p0[i], p1 = Q.p1[i];
-            int4 p3 = Q.p3[i];
-            Hit h;
-            cast_closest<COUNT>(A.S, f3of(p0), f3of(p1), clip, p3.x, h, nb, nt);
-            A.hits[i] = make_float2(__int_as_float(h.tri), h.t);
-        }
-        if (COUNT) count_add(A.counters, i < n ? 1 : 0, nb, nt);
-    }
+    uint32_t stack[kStack];
+    TraceSource src{A.q[b & 1], A.hits, &C->fetch_trace[b], n, chunk_for(n), 0, 0, 0};
+    trace_persistent<COUNT>(A.S, clip, src, stack);
+    if (COUNT) count_add64(A.counters, src.rays, src.nb, src.nt);
 }
 
 // Reference semantics: one layer of DumbRenderer's state machine, with the layer gather folded
@@ -552,27 +610,45 @@ __global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
     }
 }
 
-// Physical visibility: closest hit from the shading point toward the light point (segment
-// length 1 in units of the direction), ignoring the shading triangle; visible if nothing but
-// the light triangle is hit before t = 0.999.
+// Physical visibility: closest hit from the shading point toward the sampled light point
+// (direction = light point - shading point, so the light is at t = 1), ignoring the shading
+// triangle; visible if nothing but the light triangle is hit before t = 0.999.
+struct ShadowPhysSource {
+    ShadowQ sq;
+    float *accum;
+    int *fetch;
+    int n, chunk;
+    long long rays, nb, nt;
+    __device__ __forceinline__ bool next(int &b, int &e) { return fetch_chunk(fetch, n, chunk, b, e); }
+    __device__ __forceinline__ void load(int i, f3 &o, f3 &d, int &ign) {
+        o = f3of(sq.s0[i]);
+        d = f3of(sq.s1[i]);
+        ign = __float_as_int(sq.s2[i].w);
+    }
+    __device__ __forceinline__ void store(int i, const Hit &h, int b_, int t_) {
+        int light_tri = __float_as_int(sq.s1[i].w);
+        bool vis = (h.tri < 0) || (h.tri == light_tri) || !(h.t < 0.999f);
+        if (vis) {
+            float4 s4 = sq.s4[i];
+            accum_add(accum, __float_as_int(sq.s0[i].w), mkc(s4.x, s4.y, s4.z));
+        }
+        rays++;
+        nb += b_;
+        nt += t_;
+    }
+};
+
+// Physical visibility: closest hit from the shading point toward the sampled light point
+// (direction = light point - shading point, so the light is at t = 1), ignoring the shading
+// triangle; visible if nothing but the light triangle is hit before t = 0.999.
 template <bool COUNT>
 __global__ void __launch_bounds__(256) k_shadow_phys(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const int n = *((volatile int *)&C->shadow_count[b]);
-    for (;;) {
-        int base = warp_fetch(&C->fetch_shadow[b]);
-        if (base >= n) break;
-        int i = base + (int)lane_id();
-        int nb = 0, nt = 0;
-        if (i < n) {
-            float4 s0 = A.sq.s0[i], s1 = A.sq.s1[i], s2 = A.sq.s2[i], s4 = A.sq.s4[i];
-            Hit h;
-            cast_closest<COUNT>(A.S, f3of(s0), f3of(s1), false, __float_as_int(s2.w), h, nb, nt);
-            bool vis = (h.tri < 0) || (h.tri == __float_as_int(s1.w)) || !(h.t < 0.999f);
-            if (vis) accum_add(A.accum, __float_as_int(s0.w), mkc(s4.x, s4.y, s4.z));
-        }
-        if (COUNT) count_add(A.counters + 3, i < n ? 1 : 0, nb, nt);
-    }
+    uint32_t stack[kStack];
+    ShadowPhysSource src{A.sq, A.accum, &C->fetch_shadow[b], n, chunk_for(n), 0, 0, 0};
+    trace_persistent<COUNT>(A.S, false, src, stack);
+    if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
 }
 
 // Accumulators -> frame buffer: set (blend >= 1) or blend like blendBlockPixelColor.
@@ -620,7 +696,8 @@ cudaError_t launch_cast(const Scene &S, const float *o, const float *d, const in
                         float *hit_t, int *nbox, int *ntri, cudaStream_t stream, long long *launches) {
     if (n <= 0) return cudaSuccess;
     int threads = 128;
-    int blocks = (n + threads - 1) / threads;
+    int per_block = (threads / 32) * kChunk;
+    int blocks = (n + per_block - 1) / per_block;
     if (nbox || ntri)
         k_cast<true><<<blocks, threads, 0, stream>>>(S, o, d, ignore, n, clip, hit_tri, hit_t, nbox, ntri);
     else
