@@ -79,8 +79,9 @@ __global__ void __launch_bounds__(128) k_cast(Scene S, const float *__restrict__
                                               const int *__restrict__ ignore, int n, int clip, int *__restrict__ hit_tri,
                                               float *__restrict__ hit_t, int *__restrict__ nbox, int *__restrict__ ntri) {
     uint32_t stack[kStack];
+    __shared__ WarpLeafSlots slots[4];
     BatchSource src{o, d, ignore, hit_tri, COUNT ? nbox : nullptr, COUNT ? ntri : nullptr, hit_t, n, false};
-    trace_persistent<COUNT>(S, clip != 0, src, stack);
+    trace_persistent<COUNT>(S, clip != 0, src, stack, slots[threadIdx.x >> 5]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -315,8 +316,9 @@ __global__ void __launch_bounds__(256) k_trace(WaveArgs A, int b) {
     const int n = *((volatile int *)&C->ray_count[b]);
     const bool clip = A.mode == DR_MODE_REFERENCE ? (A.clip != 0) : false;
     uint32_t stack[kStack];
+    __shared__ WarpLeafSlots slots[8];
     TraceSource src{A.q[b & 1], A.hits, &C->fetch_trace[b], n, chunk_for(n), 0, 0, 0};
-    trace_persistent<COUNT>(A.S, clip, src, stack);
+    trace_persistent<COUNT>(A.S, clip, src, stack, slots[threadIdx.x >> 5]);
     if (COUNT) count_add64(A.counters, src.rays, src.nb, src.nt);
 }
 
@@ -646,8 +648,9 @@ __global__ void __launch_bounds__(256) k_shadow_phys(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const int n = *((volatile int *)&C->shadow_count[b]);
     uint32_t stack[kStack];
+    __shared__ WarpLeafSlots slots[8];
     ShadowPhysSource src{A.sq, A.accum, &C->fetch_shadow[b], n, chunk_for(n), 0, 0, 0};
-    trace_persistent<COUNT>(A.S, false, src, stack);
+    trace_persistent<COUNT>(A.S, false, src, stack, slots[threadIdx.x >> 5]);
     if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
 }
 

@@ -7,6 +7,11 @@
 //     most one 8-child group test, or entering a leaf) or one triangle test.  A lane never waits
 //     for another lane's whole leaf or whole descent; per-ray costs range over three orders of
 //     magnitude on displaced meshes (p99 ~1,700 triangle tests against a mean of ~120);
+//   * leaf work is shared by the whole warp: the pending (ray, triangle) tests of all lanes that hold
+//     a leaf are numbered with a warp prefix sum and handed out 32 per round, one per lane; the
+//     tester reads the owner's ray through shuffles and posts (distance, list position) to the
+//     owner's slot with a 64-bit atomicMin, so the owner keeps the smallest distance and, among
+//     equal distances, the earliest triangle in list order - exactly castInLeaf's strict-min scan;
 //   * a lane whose ray is finished takes the next ray of the warp's current chunk at once.  Chunks
 //     are handed out by the caller's Source (an atomic counter for queues whose size is only known
 //     on the device, a fixed range for plain batches).
@@ -65,8 +70,15 @@ __device__ __forceinline__ int lane_start(const Scene &S, LaneRay &L) {
 //   bool next(int &begin, int &end)           warp-uniform; false when no work is left
 //   void load(int i, f3 &o, f3 &d, int &ignore)
 //   void store(int i, const Hit &h, int nbox, int ntri)
+// Per-warp shared scratch of the cooperative leaf rounds.
+struct WarpLeafSlots {
+    unsigned long long key[32];
+    int incl[32];
+};
+
 template <bool COUNT, class Source>
-__device__ __forceinline__ void trace_persistent(const Scene &S, bool clip, Source &src, uint32_t *stack) {
+__device__ __forceinline__ void trace_persistent(const Scene &S, bool clip, Source &src, uint32_t *stack,
+                                                 WarpLeafSlots &ws) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lt_mask = (1u << lane) - 1u;
     int c_next = 0, c_end = 0;
@@ -136,37 +148,79 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, bool clip, Sour
                     L.sp = 0;
                 }
             }
-        } else if (mode == kLeaf) {
-            // ---- one triangle test of the current leaf (castInLeaf)
-            if (L.r < L.r_end) {
-                const float4 *lt = S.leaf_tris + 3 * (size_t)L.r;
+        }
+        // ---- one cooperative round of leaf triangle tests (castInLeaf)
+        int pending = (mode == kLeaf) ? (L.r_end - L.r) : 0;
+        int incl = pending;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            int v = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+            if ((int)lane >= off) incl += v;
+        }
+        const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        if (total > 0) {
+            ws.incl[lane] = incl;
+            ws.key[lane] = ~0ull;
+            __syncwarp();
+            // task `lane` belongs to the first lane whose inclusive count exceeds it
+            int owner = 0;
+            if ((int)lane < total) {
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (ws.incl[owner + step - 1] <= (int)lane) owner += step;
+            } else {
+                owner = (int)lane;
+            }
+            const int owner_excl = ws.incl[owner] - __shfl_sync(0xFFFFFFFFu, pending, owner);
+            const float ox = __shfl_sync(0xFFFFFFFFu, L.o.x, owner), oy = __shfl_sync(0xFFFFFFFFu, L.o.y, owner),
+                        oz = __shfl_sync(0xFFFFFFFFu, L.o.z, owner);
+            const float dx = __shfl_sync(0xFFFFFFFFu, L.d.x, owner), dy = __shfl_sync(0xFFFFFFFFu, L.d.y, owner),
+                        dz = __shfl_sync(0xFFFFFFFFu, L.d.z, owner);
+            const int ign = __shfl_sync(0xFFFFFFFFu, L.ignore, owner);
+            const float obest = __shfl_sync(0xFFFFFFFFu, L.best, owner);
+            const int owner_r = __shfl_sync(0xFFFFFFFFu, L.r, owner);
+            if ((int)lane < total) {
+                const int pos = owner_r + ((int)lane - owner_excl);
+                const float4 *lt = S.leaf_tris + 3 * (size_t)pos;
                 float4 A = __ldg(lt), B = __ldg(lt + 1), C = __ldg(lt + 2);
                 float dist;
                 f3 hp;
-                if (COUNT) L.nt++;
-                if (tri_cast_better(f3of(A), f3of(B), f3of(C), __float_as_int(A.w), L.o, L.d, clip, L.ignore, L.best, dist, hp)) {
-                    L.best = dist;
-                    L.bp = hp;
-                    L.bi = __float_as_int(A.w);
-                }
-                L.r++;
+                if (tri_cast_better(f3of(A), f3of(B), f3of(C), __float_as_int(A.w), mkf3(ox, oy, oz), mkf3(dx, dy, dz), clip, ign,
+                                    obest, dist, hp))
+                    atomicMin(&ws.key[owner], ((unsigned long long)__float_as_uint(dist) << 32) | (unsigned)pos);
             }
-            if (L.r >= L.r_end) {
-                if (L.best != FLT_MAX && L.bp.x >= L.lx && L.bp.y >= L.ly && L.bp.z >= L.lz && L.bp.x <= L.hx &&
-                    L.bp.y <= L.hy && L.bp.z <= L.hz) {
-                    if (COUNT) {
-                        L.nb -= 7 - L.kleaf;
-                        for (int s = 0; s < L.sp; s++) L.nb -= 7 - (int)((stack[s] >> 8) & 7u);
-                    }
-                    Hit h;
-                    h.tri = L.bi;
-                    h.t = L.best;
-                    h.p = L.bp;
-                    src.store(cur_i, h, L.nb, L.nt);
-                    mode = kIdle;
-                } else {
-                    mode = kTrav;
+            __syncwarp();
+            if (mode == kLeaf) {
+                const int excl = incl - pending;
+                const int done = max(0, min(pending, 32 - excl));
+                if (COUNT) L.nt += done;
+                L.r += done;
+                const unsigned long long k = ws.key[lane];
+                if (k != ~0ull) {
+                    const float dist = __uint_as_float((unsigned)(k >> 32));
+                    const int pos = (int)(k & 0xFFFFFFFFull);
+                    L.best = dist;
+                    L.bi = __float_as_int(__ldg(S.leaf_tris + 3 * (size_t)pos).w);
+                    L.bp = xadd(L.o, xmul(L.d, dist));
                 }
+            }
+            __syncwarp();
+        }
+        if (mode == kLeaf && L.r >= L.r_end) {
+            if (L.best != FLT_MAX && L.bp.x >= L.lx && L.bp.y >= L.ly && L.bp.z >= L.lz && L.bp.x <= L.hx && L.bp.y <= L.hy &&
+                L.bp.z <= L.hz) {
+                if (COUNT) {
+                    L.nb -= 7 - L.kleaf;
+                    for (int s = 0; s < L.sp; s++) L.nb -= 7 - (int)((stack[s] >> 8) & 7u);
+                }
+                Hit h;
+                h.tri = L.bi;
+                h.t = L.best;
+                h.p = L.bp;
+                src.store(cur_i, h, L.nb, L.nt);
+                mode = kIdle;
+            } else {
+                mode = kTrav;
             }
         }
     }
