@@ -208,8 +208,13 @@ def run_ours(a):
         return dr.render_params(W, H, dr.MODE_PHYSICAL, samples=(sx, sy), max_bounces=a.depth,
                                 iteration=1 + rank * 100000 + it, seed=1234)
 
+    first_ms = None
     for i in range(a.warmup):
+        w0 = time.time()
         rend.render_blocks(scene, cam, fb, 0, nb, params(i), stream)
+        if i == 0:
+            torch.cuda.synchronize()
+            first_ms = (time.time() - w0) * 1e3
     torch.cuda.synchronize()
     # timed region: device-resident inputs
     if world > 1:
@@ -296,6 +301,7 @@ def run_ours(a):
                      "c_box": round(c_box, 2), "c_tri": round(c_tri, 2),
                      "launch_ms_avg": round(trace_ms / max(1, trace_launches), 4)},
         "kernel_ms_per_step": {k: round(v[0] / a.steps, 2) for k, v in ktimes.items()},
+        "first_frame_ms": None if first_ms is None else round(first_ms, 1),
         "rays_per_frame": {"extension": cnt["trace_rays"], "shadow": cnt["shadow_casts"]},
         "mrays_per_s": round((cnt["trace_rays"] + cnt["shadow_casts"]) * a.steps / (ms / 1e3) / 1e6, 1),
     }

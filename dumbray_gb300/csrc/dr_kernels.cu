@@ -311,7 +311,7 @@ __device__ __forceinline__ void count_add64(unsigned long long *c, long long ray
 }
 
 template <bool COUNT>
-__global__ void __launch_bounds__(256) k_trace(WaveArgs A, int b) {
+__global__ void __launch_bounds__(256, 3) k_trace(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const int n = *((volatile int *)&C->ray_count[b]);
     const bool clip = A.mode == DR_MODE_REFERENCE ? (A.clip != 0) : false;
@@ -644,7 +644,7 @@ struct ShadowPhysSource {
 // (direction = light point - shading point, so the light is at t = 1), ignoring the shading
 // triangle; visible if nothing but the light triangle is hit before t = 0.999.
 template <bool COUNT>
-__global__ void __launch_bounds__(256) k_shadow_phys(WaveArgs A, int b) {
+__global__ void __launch_bounds__(256, 3) k_shadow_phys(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const int n = *((volatile int *)&C->shadow_count[b]);
     uint32_t stack[kStack];

@@ -8,7 +8,7 @@
 //     for another lane's whole leaf or whole descent; per-ray costs range over three orders of
 //     magnitude on displaced meshes (p99 ~1,700 triangle tests against a mean of ~120);
 //   * leaf work is shared by the whole warp: the pending (ray, triangle) tests of all lanes that hold
-//     a leaf are numbered with a warp prefix sum and handed out 32 per round, one per lane; the
+//     a leaf are numbered with a warp prefix sum and handed out 64 per round, two per lane; the
 //     tester reads the owner's ray through shuffles and posts (distance, list position) to the
 //     owner's slot with a 64-bit atomicMin, so the owner keeps the smallest distance and, among
 //     equal distances, the earliest triangle in list order - exactly castInLeaf's strict-min scan;
@@ -162,37 +162,57 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, bool clip, Sour
             ws.incl[lane] = incl;
             ws.key[lane] = ~0ull;
             __syncwarp();
-            // task `lane` belongs to the first lane whose inclusive count exceeds it
-            int owner = 0;
-            if ((int)lane < total) {
+            // tasks `lane` and `lane + 32` of this round; task t belongs to the first lane whose
+            // inclusive count exceeds t.  Both triangles are loaded before either is tested.
+            const int t0 = (int)lane, t1 = (int)lane + 32;
+            int own0 = (int)lane, own1 = (int)lane;
+            if (t0 < total) {
+                own0 = 0;
 #pragma unroll
                 for (int step = 16; step > 0; step >>= 1)
-                    if (ws.incl[owner + step - 1] <= (int)lane) owner += step;
-            } else {
-                owner = (int)lane;
+                    if (ws.incl[own0 + step - 1] <= t0) own0 += step;
             }
-            const int owner_excl = ws.incl[owner] - __shfl_sync(0xFFFFFFFFu, pending, owner);
-            const float ox = __shfl_sync(0xFFFFFFFFu, L.o.x, owner), oy = __shfl_sync(0xFFFFFFFFu, L.o.y, owner),
-                        oz = __shfl_sync(0xFFFFFFFFu, L.o.z, owner);
-            const float dx = __shfl_sync(0xFFFFFFFFu, L.d.x, owner), dy = __shfl_sync(0xFFFFFFFFu, L.d.y, owner),
-                        dz = __shfl_sync(0xFFFFFFFFu, L.d.z, owner);
-            const int ign = __shfl_sync(0xFFFFFFFFu, L.ignore, owner);
-            const float obest = __shfl_sync(0xFFFFFFFFu, L.best, owner);
-            const int owner_r = __shfl_sync(0xFFFFFFFFu, L.r, owner);
-            if ((int)lane < total) {
-                const int pos = owner_r + ((int)lane - owner_excl);
-                const float4 *lt = S.leaf_tris + 3 * (size_t)pos;
-                float4 A = __ldg(lt), B = __ldg(lt + 1), C = __ldg(lt + 2);
-                float dist;
-                f3 hp;
-                if (tri_cast_better(f3of(A), f3of(B), f3of(C), __float_as_int(A.w), mkf3(ox, oy, oz), mkf3(dx, dy, dz), clip, ign,
-                                    obest, dist, hp))
-                    atomicMin(&ws.key[owner], ((unsigned long long)__float_as_uint(dist) << 32) | (unsigned)pos);
+            if (t1 < total) {
+                own1 = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (ws.incl[own1 + step - 1] <= t1) own1 += step;
+            }
+            const int excl0 = ws.incl[own0] - __shfl_sync(0xFFFFFFFFu, pending, own0);
+            const int excl1 = ws.incl[own1] - __shfl_sync(0xFFFFFFFFu, pending, own1);
+            const int r0 = __shfl_sync(0xFFFFFFFFu, L.r, own0), r1 = __shfl_sync(0xFFFFFFFFu, L.r, own1);
+            const int pos0 = r0 + (t0 - excl0), pos1 = r1 + (t1 - excl1);
+            float4 A0, B0, C0, A1, B1, C1;
+            if (t0 < total) {
+                const float4 *lt = S.leaf_tris + 3 * (size_t)pos0;
+                A0 = __ldg(lt); B0 = __ldg(lt + 1); C0 = __ldg(lt + 2);
+            }
+            if (t1 < total) {
+                const float4 *lt = S.leaf_tris + 3 * (size_t)pos1;
+                A1 = __ldg(lt); B1 = __ldg(lt + 1); C1 = __ldg(lt + 2);
+            }
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int own = q ? own1 : own0;
+                const float ox = __shfl_sync(0xFFFFFFFFu, L.o.x, own), oy = __shfl_sync(0xFFFFFFFFu, L.o.y, own),
+                            oz = __shfl_sync(0xFFFFFFFFu, L.o.z, own);
+                const float dx = __shfl_sync(0xFFFFFFFFu, L.d.x, own), dy = __shfl_sync(0xFFFFFFFFu, L.d.y, own),
+                            dz = __shfl_sync(0xFFFFFFFFu, L.d.z, own);
+                const int ign = __shfl_sync(0xFFFFFFFFu, L.ignore, own);
+                const float obest = __shfl_sync(0xFFFFFFFFu, L.best, own);
+                if ((q ? t1 : t0) < total) {
+                    const float4 A = q ? A1 : A0, B = q ? B1 : B0, C = q ? C1 : C0;
+                    float dist;
+                    f3 hp;
+                    if (tri_cast_better(f3of(A), f3of(B), f3of(C), __float_as_int(A.w), mkf3(ox, oy, oz), mkf3(dx, dy, dz), clip,
+                                        ign, obest, dist, hp))
+                        atomicMin(&ws.key[own], ((unsigned long long)__float_as_uint(dist) << 32) | (unsigned)(q ? pos1 : pos0));
+                }
             }
             __syncwarp();
             if (mode == kLeaf) {
                 const int excl = incl - pending;
-                const int done = max(0, min(pending, 32 - excl));
+                const int done = max(0, min(pending, 64 - excl));
                 if (COUNT) L.nt += done;
                 L.r += done;
                 const unsigned long long k = ws.key[lane];
