@@ -66,6 +66,11 @@ class DrRenderParams(ctypes.Structure):
                 ("seed", ctypes.c_uint32)]
 
 
+class DrBatchItem(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("camera", DrCamera), ("params", DrRenderParams), ("fb", ctypes.c_void_p),
+                ("start_block", ctypes.c_int32), ("end_block", ctypes.c_int32)]
+
+
 class DumbRayError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"dumbray_gb300 status {status}: {message}")
@@ -128,6 +133,18 @@ def lib() -> ctypes.CDLL:
     L.dr_renderer_set_counting.argtypes = [vp, i32]
     L.dr_renderer_counters.restype = i32
     L.dr_renderer_counters.argtypes = [vp, vp]
+    L.dr_render_adjoint.restype = i32
+    L.dr_render_adjoint.argtypes = [vp, vp, vp, vp, i32, i32, vp, vp, vp, vp]
+    L.dr_batch_create.restype = i32
+    L.dr_batch_create.argtypes = [vp, i32, P(vp)]
+    L.dr_batch_set_iteration.restype = i32
+    L.dr_batch_set_iteration.argtypes = [vp, i32]
+    L.dr_batch_render.restype = i32
+    L.dr_batch_render.argtypes = [vp, vp, i32, vp]
+    L.dr_batch_paths.restype = i64
+    L.dr_batch_paths.argtypes = [vp]
+    L.dr_batch_destroy.restype = None
+    L.dr_batch_destroy.argtypes = [vp]
     L.dr_render_blocks.restype = i32
     L.dr_render_blocks.argtypes = [vp, vp, vp, vp, i32, i32, vp, vp]
     _lib = L
@@ -317,6 +334,12 @@ class Scene:
         check(lib().dr_scene_export_tree(self.handle, box.ctypes.data, child.ctypes.data, leaf.ctypes.data, refs.ctypes.data))
         return box, child, leaf, refs[: s["refs"]]
 
+    def triangle_params_device(self):
+        """(albedo_ptr, emission_ptr): device float[n][3] arrays the kernels read (writable in place)."""
+        a, e = ctypes.c_void_p(), ctypes.c_void_p()
+        check(lib().dr_scene_triangle_params_device(self.handle, ctypes.byref(a), ctypes.byref(e)))
+        return a.value, e.value
+
     def set_triangle_params(self, albedo=None, emission=None, roughness=None):
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float32) for a in (albedo, emission, roughness)]
         check(lib().dr_scene_set_triangle_params(self.handle, *[None if a is None else a.ctypes.data for a in arrs]))
@@ -447,6 +470,52 @@ class Renderer:
             pass
 
 
+    def render_adjoint(self, scene: Scene, cam: DrCamera, dl_dfb, start_block: int, end_block: int, params: DrRenderParams,
+                       grad_albedo, grad_emission, stream=None):
+        """dr_render_adjoint: adds dL/d albedo and dL/d emission (CUDA float32 [n,3]) for dL/dI = dl_dfb."""
+        check(lib().dr_render_adjoint(self._h, scene.handle, ctypes.byref(cam), _ptr(dl_dfb), int(start_block), int(end_block),
+                                      ctypes.byref(params), _ptr(grad_albedo), _ptr(grad_emission), _stream_ptr(stream)))
+
+
+class Batch:
+    """Many render jobs sharing the same waves (dr_batch); optionally replayed as one CUDA graph."""
+
+    def __init__(self, jobs):
+        """jobs: sequence of (scene, camera, params, fb_tensor, start_block, end_block)."""
+        self._keep = list(jobs)
+        arr = (DrBatchItem * len(self._keep))()
+        for i, (scene, cam, params, fb, s0, s1) in enumerate(self._keep):
+            arr[i].scene = scene.handle.value
+            arr[i].camera = cam
+            arr[i].params = params
+            arr[i].fb = _ptr(fb)
+            arr[i].start_block = s0
+            arr[i].end_block = s1
+        h = ctypes.c_void_p()
+        check(lib().dr_batch_create(ctypes.addressof(arr), len(self._keep), ctypes.byref(h)))
+        self._h = h
+
+    def paths(self) -> int:
+        return int(lib().dr_batch_paths(self._h))
+
+    def set_iteration(self, iteration: int):
+        check(lib().dr_batch_set_iteration(self._h, int(iteration)))
+
+    def render(self, renderer: "Renderer", use_graph: bool = True, stream=None):
+        check(lib().dr_batch_render(renderer.handle, self._h, 1 if use_graph else 0, _stream_ptr(stream)))
+
+    def close(self):
+        if self._h is not None:
+            lib().dr_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class BlockRenderer:
     """Host mirror of DumbRenderer's block-renderer interface (DumbRenderer.cuh:9-64): the same
     configuration setters and a ``render_blocks_gpu`` that renders a block range of a device frame
@@ -525,3 +594,54 @@ def render_blocks_noalloc(scene: Scene, cam: DrCamera, fb, start_block: int, end
                    ctypes.c_void_p]
     check(fn(scene.handle, ctypes.byref(cam), _ptr(fb), int(start_block), int(end_block), ctypes.byref(params),
              _stream_ptr(stream)))
+
+
+def render_differentiable(scene: Scene, cam: DrCamera, params: DrRenderParams, albedo, emission, renderer=None):
+    """Physical-mode render as a differentiable function of per-triangle albedo and emission
+    (CUDA float32 [n,3] tensors): returns the block-major [blocks*128, 4] image; its backward pass is
+    the path-replay adjoint (dr_render_adjoint) with the same random numbers.  The parameters are
+    copied into the scene's device arrays before rendering; the emissive-triangle sampling table
+    keeps the emitter set and powers the scene was created with (sampling pdfs are constants)."""
+    import torch
+
+    class _Render(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, alb, emi):
+            a_ptr, e_ptr = scene.triangle_params_device()
+            n = scene.n
+            # write the parameters in place (device -> device copies on the current stream)
+            at = torch.cuda.current_stream()
+            _copy_into(a_ptr, alb.detach().contiguous().float(), n)
+            _copy_into(e_ptr, emi.detach().contiguous().float(), n)
+            r = renderer if renderer is not None else Renderer(1 << 20)
+            fb = new_frame_buffer(params.width, params.height, alb.device)
+            r.render_blocks(scene, cam, fb, 0, block_count(params.width, params.height), params, at)
+            ctx.r = r
+            return fb
+
+        @staticmethod
+        def backward(ctx, g):
+            g = g.contiguous().float()
+            ga = torch.zeros((scene.n, 3), dtype=torch.float32, device=g.device)
+            ge = torch.zeros((scene.n, 3), dtype=torch.float32, device=g.device)
+            ctx.r.render_adjoint(scene, cam, g, 0, block_count(params.width, params.height), params, ga, ge)
+            return ga, ge
+
+    return _Render.apply(albedo, emission)
+
+
+class _DeviceArray:
+    """A raw device allocation exposed through the CUDA array interface (zero-copy torch view)."""
+
+    def __init__(self, ptr: int, shape, typestr="<f4"):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr), False), "version": 3}
+
+
+def device_view(ptr: int, shape, device="cuda"):
+    """torch view of device memory owned by the library (e.g. a scene's albedo / emission arrays)."""
+    import torch
+    return torch.as_tensor(_DeviceArray(ptr, shape), device=device)
+
+
+def _copy_into(dst_ptr: int, src, n: int):
+    device_view(dst_ptr, (n, 3), src.device).copy_(src)

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <string>
 #include <thread>
+#include <atomic>
 #include <vector>
 
 #include "../../include/dr_api.h"
@@ -26,6 +27,9 @@ dr_status fail(dr_status s, const std::string &msg) {
 }
 dr_status cuda_fail(cudaError_t e, const char *where) {
     g_err = std::string(where) + ": " + cudaGetErrorString(e);
+    // Reset the runtime's last-error slot: a non-sticky error reported through the status code must
+    // not surface again in the caller's next cudaGetLastError() check.
+    (void)cudaGetLastError();
     return DR_E_CUDA;
 }
 
@@ -66,8 +70,9 @@ struct dr_scene {
     float4 *shade = nullptr;
     int *emissive = nullptr;
     float *emissive_cdf = nullptr;
-    float *albedo_dev = nullptr;         // views for dr_scene_triangle_params_device
+    float *albedo_dev = nullptr;         // per-triangle albedo / emission read by the kernels
     float *emission_dev = nullptr;
+    float *light_pdf_dev = nullptr;
 
     ~dr_scene() {
         for (void *p : allocs) cudaFree(p);
@@ -76,6 +81,7 @@ struct dr_scene {
         cudaFree(emissive_cdf);
         cudaFree(albedo_dev);
         cudaFree(emission_dev);
+        cudaFree(light_pdf_dev);
     }
 };
 
@@ -97,9 +103,21 @@ struct dr_renderer {
     drk::Profiler prof;
     unsigned long long *counters = nullptr;
     bool counting = false;
+    int *prefix = nullptr;          // adjoint: per-path vertex triangles
+    int prefix_paths = 0;
+    // Identifies the current set of scratch buffers: a new value at creation and whenever a buffer a
+    // captured batch graph points into is reallocated (process-unique, so a renderer created at
+    // the address of a destroyed one never matches a graph captured for the old one).
+    unsigned long long scratch_id = next_scratch_id();
+
+    static unsigned long long next_scratch_id() {
+        static std::atomic<unsigned long long> counter{0};
+        return ++counter;
+    }
 
     ~dr_renderer() {
         cudaFree(counters);
+        cudaFree(prefix);
         for (int k = 0; k < 2; k++) {
             for (int j = 0; j < 3; j++) cudaFree(q[k][j]);
             cudaFree(q3[k]);
@@ -113,24 +131,22 @@ struct dr_renderer {
 
 namespace {
 
-// Per-triangle shading records and the emissive-triangle sampling table (physical mode).
+// Per-triangle shading records and the emissive-triangle sampling table (physical mode): triangles
+// are picked by emitted power (sum of rgb radiance x area), a point uniformly by area, so the area
+// pdf of a point of emitter i is (r+g+b)_i / total power.
 dr_status upload_shading(dr_scene *sc) {
     const int64_t n = sc->n;
-    std::vector<float4> shade(2 * n);
+    std::vector<float4> shade(n);
+    std::vector<float> light_pdf(n, 0.0f);
     std::vector<int> em;
     std::vector<float> cdf;
     double total = 0.0;
     for (int64_t i = 0; i < n; i++) {
         int type = sc->mats.empty() ? DR_MAT_LAMBERT : sc->mats[sc->mat_id[i]].type;
-        shade[2 * i] = make_float4(sc->albedo[3 * i], sc->albedo[3 * i + 1], sc->albedo[3 * i + 2], sc->roughness[i]);
-        float4 e;
-        e.x = sc->emission[3 * i];
-        e.y = sc->emission[3 * i + 1];
-        e.z = sc->emission[3 * i + 2];
-        int bits = type;
-        std::memcpy(&e.w, &bits, 4);
-        shade[2 * i + 1] = e;
-        float esum = e.x + e.y + e.z;
+        float tbits;
+        std::memcpy(&tbits, &type, 4);
+        shade[i] = make_float4(sc->roughness[i], tbits, 0.0f, 0.0f);
+        float esum = sc->emission[3 * i] + sc->emission[3 * i + 1] + sc->emission[3 * i + 2];
         if (esum > 0.0f) {
             const float *p = &sc->xyz[9 * i];
             double ux = p[3] - p[0], uy = p[4] - p[1], uz = p[5] - p[2];
@@ -142,23 +158,34 @@ dr_status upload_shading(dr_scene *sc) {
             cdf.push_back((float)total);
         }
     }
+    for (size_t k = 0; k < em.size(); k++) {
+        int i = em[k];
+        float esum = sc->emission[3 * i] + sc->emission[3 * i + 1] + sc->emission[3 * i + 2];
+        light_pdf[i] = (float)((double)esum / total);
+    }
     cudaFree(sc->shade);
     cudaFree(sc->emissive);
     cudaFree(sc->emissive_cdf);
     cudaFree(sc->albedo_dev);
     cudaFree(sc->emission_dev);
+    cudaFree(sc->light_pdf_dev);
     sc->shade = nullptr;
     sc->emissive = nullptr;
     sc->emissive_cdf = nullptr;
     sc->albedo_dev = nullptr;
     sc->emission_dev = nullptr;
+    sc->light_pdf_dev = nullptr;
     cudaError_t e = upload(&sc->shade, shade.data(), shade.size());
     if (e == cudaSuccess) e = upload(&sc->emissive, em.data(), em.size());
     if (e == cudaSuccess) e = upload(&sc->emissive_cdf, cdf.data(), cdf.size());
     if (e == cudaSuccess) e = upload(&sc->albedo_dev, sc->albedo.data(), sc->albedo.size());
     if (e == cudaSuccess) e = upload(&sc->emission_dev, sc->emission.data(), sc->emission.size());
+    if (e == cudaSuccess) e = upload(&sc->light_pdf_dev, light_pdf.data(), light_pdf.size());
     if (e != cudaSuccess) return cuda_fail(e, "upload shading");
     sc->dev.shade = sc->shade;
+    sc->dev.albedo = sc->albedo_dev;
+    sc->dev.emission = sc->emission_dev;
+    sc->dev.light_pdf = sc->light_pdf_dev;
     sc->dev.emissive = sc->emissive;
     sc->dev.emissive_cdf = sc->emissive_cdf;
     sc->dev.n_emissive = (int)em.size();
@@ -513,72 +540,73 @@ dr_status dr_renderer_counters(dr_renderer *r, int64_t *counts) {
     return DR_OK;
 }
 
-dr_status dr_render_blocks(dr_renderer *r, const dr_scene *sc, const dr_camera *cam, float *fb, int32_t start_block,
-                           int32_t end_block, const dr_render_params *p, void *stream_ptr) {
-    if (!r || !sc || !cam || !fb || !p) return fail(DR_E_ARG, "dr_render_blocks: NULL argument");
-    if (p->mode != DR_MODE_REFERENCE && p->mode != DR_MODE_PHYSICAL) return fail(DR_E_ARG, "dr_render_blocks: bad mode");
-    if (p->width <= 0 || p->height <= 0) return fail(DR_E_ARG, "dr_render_blocks: bad resolution");
+// Validates one render job and fills its Item (everything but the slot / path offsets).
+static dr_status make_item(const dr_scene *sc, const dr_camera *cam, float *fb, int32_t start_block, int32_t end_block,
+                           const dr_render_params *p, const char *who, drk::Item &I) {
+    if (!sc || !cam || !fb || !p) return fail(DR_E_ARG, std::string(who) + ": NULL argument");
+    if (p->mode != DR_MODE_REFERENCE && p->mode != DR_MODE_PHYSICAL) return fail(DR_E_ARG, std::string(who) + ": bad mode");
+    if (p->width <= 0 || p->height <= 0) return fail(DR_E_ARG, std::string(who) + ": bad resolution");
     const int nblocks = dr_block_count(p->width, p->height);
-    if (start_block < 0 || end_block > nblocks || start_block > end_block) return fail(DR_E_ARG, "dr_render_blocks: bad block range");
-    if (p->max_bounces < 0 || p->max_bounces > 64) return fail(DR_E_ARG, "dr_render_blocks: max_bounces must be in [0, 64]");
-    if (p->boxing < 0 || p->boxing > 3) return fail(DR_E_ARG, "dr_render_blocks: bad boxing mode");
-    if (cam->lens < 0 || cam->lens > DR_LENS_SPHERICAL) return fail(DR_E_ARG, "dr_render_blocks: bad lens");
-    const bool ref_lens = cam->lens <= DR_LENS_SPHERICAL_SEGMENT;
-    if ((p->mode == DR_MODE_REFERENCE) != ref_lens)
-        return fail(DR_E_ARG, "dr_render_blocks: lens does not belong to the render mode");
-    if (start_block == end_block) return DR_OK;
-    cudaStream_t stream = (cudaStream_t)stream_ptr;
+    if (start_block < 0 || end_block > nblocks || start_block > end_block)
+        return fail(DR_E_ARG, std::string(who) + ": bad block range");
+    if (p->max_bounces < 0 || p->max_bounces > 64) return fail(DR_E_ARG, std::string(who) + ": max_bounces must be in [0, 64]");
+    if (p->boxing < 0 || p->boxing > 3) return fail(DR_E_ARG, std::string(who) + ": bad boxing mode");
+    if (cam->lens < 0 || cam->lens > DR_LENS_SPHERICAL) return fail(DR_E_ARG, std::string(who) + ": bad lens");
+    if ((p->mode == DR_MODE_REFERENCE) != (cam->lens <= DR_LENS_SPHERICAL_SEGMENT))
+        return fail(DR_E_ARG, std::string(who) + ": lens does not belong to the render mode");
     const int fx = std::max(1, p->samples_x), fy = std::max(1, p->samples_y);
-    const int spp = fx * fy;
-    const int n_slots = (end_block - start_block) * DR_BLOCK_W * DR_BLOCK_H;
-    const int per_path_shadow = (p->mode == DR_MODE_REFERENCE) ? std::max(1, sc->dev.n_lights) : 1;
-    long long wave = std::min<long long>(r->capacity, (long long)r->shadow_capacity / per_path_shadow);
-    wave = std::max<long long>(32, (wave / 32) * 32);
-
-    if (r->accum_slots < (size_t)n_slots) {
-        cudaFree(r->accum);
-        r->accum = nullptr;
-        r->accum_slots = 0;
-        cudaError_t e = cudaMalloc((void **)&r->accum, sizeof(float4) * (size_t)n_slots);
-        if (e != cudaSuccess) return cuda_fail(e, "dr_render_blocks: accumulator");
-        r->accum_slots = (size_t)n_slots;
-    }
-    cudaError_t e = cudaMemsetAsync(r->accum, 0, sizeof(float4) * (size_t)n_slots, stream);
-    if (e != cudaSuccess) return cuda_fail(e, "dr_render_blocks: memset");
-
-    drk::WaveDesc W;
-    W.scene = sc->dev;
-    W.camera = *cam;
+    std::memset(&I, 0, sizeof(I));
+    I.S = sc->dev;
+    I.camera = *cam;
     {
         float angle = cam->angle[0];
         if (angle < 1.0f) angle = 1.0f;
         else if (angle > 179.0f) angle = 179.0f;
         float radian = (angle / (2 * 57.29577951308233f));
-        W.cam_x = 0.5f / std::tan(radian);
+        I.cam_x = 0.5f / std::tan(radian);
     }
-    W.mode = p->mode;
-    W.width = p->width;
-    W.height = p->height;
-    W.fsaa_x = fx;
-    W.fsaa_y = fy;
-    W.spp = spp;
-    W.max_bounces = p->max_bounces;
-    W.clip = p->cull_backfaces;
+    I.mode = p->mode;
+    I.width = p->width;
+    I.height = p->height;
+    I.fsaa_x = fx;
+    I.fsaa_y = fy;
+    I.spp = fx * fy;
+    I.max_bounces = p->max_bounces;
+    I.clip = p->cull_backfaces;
     {
         float w = (float)p->width, h = (float)p->height;
-        float ps = 1.0f;
+        float ps;
         if (p->boxing == DR_BOXING_HEIGHT) ps = 1.0f / h;
         else if (p->boxing == DR_BOXING_WIDTH) ps = 1.0f / w;
         else if (p->boxing == DR_BOXING_MIN) ps = 1.0f / ((h <= w) ? h : w);
         else ps = 1.0f / ((h >= w) ? h : w);
-        W.pixel_size = ps;
-        W.pdx = ps / (float)fx;
-        W.pdy = ps / (float)fy;
+        I.pixel_size = ps;
+        I.pdx = ps / (float)fx;
+        I.pdy = ps / (float)fy;
     }
-    W.seed = p->seed;
-    W.sample_base = (uint32_t)((p->iteration < 1 ? 0 : p->iteration - 1) * spp);
-    W.start_block = start_block;
-    W.n_slots = n_slots;
+    I.seed = p->seed;
+    I.sample_base = (uint32_t)((p->iteration < 1 ? 0 : p->iteration - 1) * I.spp);
+    I.start_block = start_block;
+    I.n_slots = (end_block - start_block) * DR_BLOCK_W * DR_BLOCK_H;
+    I.fb = fb;
+    I.inv_spp = 1.0f / (float)I.spp;
+    I.blend = (p->iteration <= 1) ? 1.0f : (1.0f / (float)p->iteration);
+    return DR_OK;
+}
+
+static dr_status ensure_accum(dr_renderer *r, size_t slots) {
+    if (r->accum_slots >= slots) return DR_OK;
+    cudaFree(r->accum);
+    r->accum = nullptr;
+    r->accum_slots = 0;
+    cudaError_t e = cudaMalloc((void **)&r->accum, sizeof(float4) * std::max<size_t>(slots, 1));
+    if (e != cudaSuccess) return cuda_fail(e, "accumulator");
+    r->accum_slots = slots;
+    r->scratch_id = dr_renderer::next_scratch_id();
+    return DR_OK;
+}
+
+static void wave_buffers(dr_renderer *r, drk::WaveDesc &W) {
     for (int k = 0; k < 2; k++) {
         W.q_p0[k] = r->q[k][0];
         W.q_p1[k] = r->q[k][1];
@@ -589,19 +617,267 @@ dr_status dr_render_blocks(dr_renderer *r, const dr_scene *sc, const dr_camera *
     for (int j = 0; j < 5; j++) W.s[j] = r->s[j];
     W.accum = r->accum;
     W.ctrl = r->ctrl;
-    const long long total = (long long)n_slots * spp;
+    W.prefix = r->prefix;
+}
+
+// Issues the waves (and the resolve unless adjoint) of `total` paths over `total_slots` slots.
+static dr_status run_waves(dr_renderer *r, drk::WaveDesc &W, long long total, long long wave, int total_slots, cudaStream_t stream,
+                           drk::Profiler *prof, bool count, bool resolve) {
+    cudaError_t e = cudaMemsetAsync(r->accum, 0, sizeof(float4) * (size_t)std::max(total_slots, 1), stream);
+    if (e != cudaSuccess) return cuda_fail(e, "render: clear accumulator");
     for (long long b = 0; b < total; b += wave) {
         W.wave_begin = b;
         W.wave_count = (int)std::min<long long>(wave, total - b);
-        e = drk::launch_wave(W, stream, &r->launches, &r->prof, r->counting ? r->counters : nullptr);
-        if (e != cudaSuccess) return cuda_fail(e, "dr_render_blocks: wave");
+        e = drk::launch_wave(W, stream, &r->launches, prof, count ? r->counters : nullptr);
+        if (e != cudaSuccess) return cuda_fail(e, "render: wave");
     }
-    const float blend = (p->iteration <= 1) ? 1.0f : (1.0f / (float)p->iteration);
-    e = drk::launch_resolve(r->accum, fb, start_block, n_slots, p->width, p->height, 1.0f / (float)spp, blend, stream, &r->launches,
-                             &r->prof);
-    if (e != cudaSuccess) return cuda_fail(e, "dr_render_blocks: resolve");
+    if (resolve) {
+        e = drk::launch_resolve(W, total_slots, stream, &r->launches, prof);
+        if (e != cudaSuccess) return cuda_fail(e, "render: resolve");
+    }
     return DR_OK;
 }
+
+static long long wave_size(const dr_renderer *r, int lights_per_path, long long cap) {
+    long long wave = std::min<long long>(std::min<long long>(r->capacity, cap), (long long)r->shadow_capacity / std::max(1, lights_per_path));
+    return std::max<long long>(32, (wave / 32) * 32);
+}
+
+dr_status dr_render_blocks(dr_renderer *r, const dr_scene *sc, const dr_camera *cam, float *fb, int32_t start_block,
+                           int32_t end_block, const dr_render_params *p, void *stream_ptr) {
+    if (!r) return fail(DR_E_ARG, "dr_render_blocks: NULL argument");
+    drk::WaveDesc W;
+    std::memset(&W, 0, sizeof(W));
+    dr_status st = make_item(sc, cam, fb, start_block, end_block, p, "dr_render_blocks", W.inl);
+    if (st != DR_OK) return st;
+    if (start_block == end_block) return DR_OK;
+    cudaStream_t stream = (cudaStream_t)stream_ptr;
+    const drk::Item &I = W.inl;
+    st = ensure_accum(r, (size_t)I.n_slots);
+    if (st != DR_OK) return st;
+    W.items = nullptr;
+    W.n_items = 1;
+    W.mode = I.mode;
+    W.max_bounces = I.max_bounces;
+    W.adjoint = false;
+    wave_buffers(r, W);
+    const int lights = (I.mode == DR_MODE_REFERENCE) ? I.S.n_lights : 1;
+    return run_waves(r, W, (long long)I.n_slots * I.spp, wave_size(r, lights, 1LL << 40), I.n_slots, stream, &r->prof, r->counting,
+                     true);
+}
+
+dr_status dr_render_adjoint(dr_renderer *r, const dr_scene *sc, const dr_camera *cam, const float *dl_dfb, int32_t start_block,
+                            int32_t end_block, const dr_render_params *p, float *grad_albedo, float *grad_emission,
+                            void *stream_ptr) {
+    if (!r || !dl_dfb || !grad_albedo || !grad_emission) return fail(DR_E_ARG, "dr_render_adjoint: NULL argument");
+    drk::WaveDesc W;
+    std::memset(&W, 0, sizeof(W));
+    dr_status st = make_item(sc, cam, const_cast<float *>(dl_dfb), start_block, end_block, p, "dr_render_adjoint", W.inl);
+    if (st != DR_OK) return st;
+    if (p->mode != DR_MODE_PHYSICAL) return fail(DR_E_ARG, "dr_render_adjoint: only the physical mode is differentiable");
+    if (p->max_bounces + 1 > drd::kAdjDepth) return fail(DR_E_ARG, "dr_render_adjoint: too many bounces");
+    if (start_block == end_block) return DR_OK;
+    cudaStream_t stream = (cudaStream_t)stream_ptr;
+    drk::Item &I = W.inl;
+    I.fb = nullptr;
+    I.dl_dfb = dl_dfb;
+    I.grad_albedo = grad_albedo;
+    I.grad_emission = grad_emission;
+    const long long cap = 1LL << 20;  // paths per adjoint wave: bounds the prefix buffer to ~280 MB
+    const long long wave = wave_size(r, 1, cap);
+    if (r->prefix_paths < wave) {
+        cudaFree(r->prefix);
+        r->prefix = nullptr;
+        r->prefix_paths = 0;
+        cudaError_t e = cudaMalloc((void **)&r->prefix, sizeof(int) * (size_t)wave * drd::kAdjDepth);
+        if (e != cudaSuccess) return cuda_fail(e, "dr_render_adjoint: prefix buffer");
+        r->prefix_paths = (int)wave;
+    }
+    st = ensure_accum(r, (size_t)I.n_slots);
+    if (st != DR_OK) return st;
+    W.items = nullptr;
+    W.n_items = 1;
+    W.mode = I.mode;
+    W.max_bounces = I.max_bounces;
+    W.adjoint = true;
+    wave_buffers(r, W);
+    return run_waves(r, W, (long long)I.n_slots * I.spp, wave, I.n_slots, stream, &r->prof, false, false);
+}
+
+}  // extern "C"
+
+// ---- batches ------------------------------------------------------------------------------------
+struct dr_batch {
+    std::vector<drk::Item> items;
+    drk::Item *items_dev = nullptr;
+    long long total_paths = 0;
+    int total_slots = 0;
+    int mode = 0, max_bounces = 0, max_lights = 1;
+    std::vector<const dr_scene *> scenes;
+    std::vector<dr_render_params> params;
+    unsigned long long graph_scratch = 0;   // scratch_id of the renderer the graph was captured with
+    long long graph_wave = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long graph_launches = 0;
+    // Captures run on this private stream: the caller's stream may be the legacy default stream,
+    // which cannot be captured.  The instantiated graph is launched on the caller's stream.
+    cudaStream_t capture_stream = nullptr;
+    cudaEvent_t done = nullptr;   // recorded after each render: the job table is in use until it fires
+
+    void drop_graph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        graph_scratch = 0;
+    }
+    ~dr_batch() {
+        drop_graph();
+        if (capture_stream) cudaStreamDestroy(capture_stream);
+        if (done) cudaEventDestroy(done);
+        cudaFree(items_dev);
+    }
+};
+
+extern "C" {
+
+dr_status dr_batch_create(const dr_batch_item *items, int32_t n, dr_batch **out) {
+    if (!out) return fail(DR_E_ARG, "dr_batch_create: out is NULL");
+    *out = nullptr;
+    if (!items || n <= 0) return fail(DR_E_ARG, "dr_batch_create: empty batch");
+    dr_batch *b = new (std::nothrow) dr_batch();
+    if (!b) return fail(DR_E_NOMEM, "dr_batch_create: out of host memory");
+    b->items.resize(n);
+    long long path = 0;
+    long long slot = 0;
+    for (int i = 0; i < n; i++) {
+        const dr_batch_item &it = items[i];
+        dr_status st = make_item(it.scene, &it.camera, it.fb, it.start_block, it.end_block, &it.params, "dr_batch_create", b->items[i]);
+        if (st != DR_OK) {
+            delete b;
+            return st;
+        }
+        if (i > 0 && it.params.mode != items[0].params.mode) {
+            delete b;
+            return fail(DR_E_ARG, "dr_batch_create: all jobs of a batch must use the same render mode");
+        }
+        drk::Item &I = b->items[i];
+        I.slot_begin = (int)slot;
+        I.path_begin = path;
+        slot += I.n_slots;
+        path += (long long)I.n_slots * I.spp;
+        b->max_bounces = std::max(b->max_bounces, I.max_bounces);
+        if (I.mode == DR_MODE_REFERENCE) b->max_lights = std::max(b->max_lights, I.S.n_lights);
+        b->scenes.push_back(it.scene);
+        b->params.push_back(it.params);
+    }
+    if (slot > (1LL << 30)) {
+        delete b;
+        return fail(DR_E_CAPACITY, "dr_batch_create: more than 2^30 pixel slots");
+    }
+    b->mode = items[0].params.mode;
+    b->total_paths = path;
+    b->total_slots = (int)slot;
+    cudaError_t e = upload(&b->items_dev, b->items.data(), b->items.size());
+    if (e != cudaSuccess) {
+        delete b;
+        return cuda_fail(e, "dr_batch_create: job table");
+    }
+    *out = b;
+    return DR_OK;
+}
+
+dr_status dr_batch_set_iteration(dr_batch *b, int32_t iteration) {
+    if (!b) return fail(DR_E_ARG, "dr_batch_set_iteration: batch is NULL");
+    for (size_t i = 0; i < b->items.size(); i++) {
+        drk::Item &I = b->items[i];
+        I.sample_base = (uint32_t)((iteration < 1 ? 0 : iteration - 1) * I.spp);
+        I.blend = (iteration <= 1) ? 1.0f : (1.0f / (float)iteration);
+    }
+    cudaError_t e = b->done ? cudaEventSynchronize(b->done) : cudaSuccess;   // previous render finished with the table
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->items_dev, b->items.data(), sizeof(drk::Item) * b->items.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "dr_batch_set_iteration");
+    return DR_OK;
+}
+
+dr_status dr_batch_render(dr_renderer *r, dr_batch *b, int32_t use_graph, void *stream_ptr) {
+    if (!r || !b) return fail(DR_E_ARG, "dr_batch_render: NULL argument");
+    cudaStream_t stream = (cudaStream_t)stream_ptr;
+    dr_status st = ensure_accum(r, (size_t)b->total_slots);
+    if (st != DR_OK) return st;
+    drk::WaveDesc W;
+    std::memset(&W, 0, sizeof(W));
+    W.inl = b->items[0];
+    W.items = b->items_dev;
+    W.n_items = (int)b->items.size();
+    W.mode = b->mode;
+    W.max_bounces = b->max_bounces;
+    W.adjoint = false;
+    wave_buffers(r, W);
+    const long long wave = wave_size(r, b->mode == DR_MODE_REFERENCE ? b->max_lights : 1, 1LL << 40);
+    if (!b->done) {
+        cudaError_t e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            b->done = nullptr;
+            return cuda_fail(e, "dr_batch_render: event");
+        }
+    }
+    if (!use_graph) {
+        st = run_waves(r, W, b->total_paths, wave, b->total_slots, stream, &r->prof, r->counting, true);
+        if (st == DR_OK) cudaEventRecord(b->done, stream);
+        return st;
+    }
+    if (b->exec == nullptr || b->graph_scratch != r->scratch_id || b->graph_wave != wave) {
+        b->drop_graph();
+        cudaError_t e = cudaSuccess;
+        if (!b->capture_stream) e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return cuda_fail(e, "dr_batch_render: capture stream");
+        cudaStream_t cs = b->capture_stream;
+        e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_fail(e, "dr_batch_render: begin capture");
+        long long launches = r->launches;
+        st = run_waves(r, W, b->total_paths, wave, b->total_slots, cs, nullptr, false, true);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(cs, &g);   // always ends the capture, also after a failed launch
+        r->launches = launches;
+        if (st != DR_OK || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            (void)cudaGetLastError();
+            return st != DR_OK ? st : cuda_fail(e, "dr_batch_render: end capture");
+        }
+        e = cudaGraphInstantiate(&b->exec, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            b->exec = nullptr;
+            return cuda_fail(e, "dr_batch_render: instantiate");
+        }
+        b->graph = g;
+        b->graph_scratch = r->scratch_id;
+        b->graph_wave = wave;
+        size_t nodes = 0;
+        cudaGraphGetNodes(g, nullptr, &nodes);
+        b->graph_launches = 0;
+        // kernel nodes only (the accumulator clear is a memset node)
+        std::vector<cudaGraphNode_t> list(nodes);
+        if (nodes && cudaGraphGetNodes(g, list.data(), &nodes) == cudaSuccess) {
+            for (size_t k = 0; k < nodes; k++) {
+                cudaGraphNodeType t;
+                if (cudaGraphNodeGetType(list[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) b->graph_launches++;
+            }
+        }
+    }
+    cudaError_t e = cudaGraphLaunch(b->exec, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "dr_batch_render: graph launch");
+    cudaEventRecord(b->done, stream);
+    r->launches += b->graph_launches;
+    return DR_OK;
+}
+
+int64_t dr_batch_paths(const dr_batch *b) { return b ? b->total_paths : 0; }
+
+void dr_batch_destroy(dr_batch *b) { delete b; }
 
 }  // extern "C"
 

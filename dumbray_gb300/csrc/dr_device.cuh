@@ -46,9 +46,12 @@ struct Scene {
     const int *mat_id;
     const Material *mats;
     const Light *lights;
-    const float4 *shade;        // physical: [2n] {albedo.rgb, roughness}, {emission.rgb, type bits}
+    const float4 *shade;        // physical: [n] {roughness, type bits, -, -}
+    const float *albedo;        // physical: [n][3] (writable in place by an optimiser)
+    const float *emission;      // physical: [n][3] (writable in place; sampling tables are not rebuilt)
+    const float *light_pdf;     // physical: [n] area pdf of picking a point of this triangle by NEE
     const int *emissive;        // emissive triangle ids
-    const float *emissive_cdf;  // inclusive prefix sums of power
+    const float *emissive_cdf;  // inclusive prefix sums of power (at table build time)
     float root_lo[3], root_hi[3];
     int root_child;             // 0 = root split (children are nodes 0..7), -1 = root is a leaf
     int root_leaf_first, root_leaf_count;
@@ -183,9 +186,9 @@ __device__ __forceinline__ bool cast_leaf(const Scene &S, int first, int count, 
 }
 
 // Tests the 8 children of a group; bit k of the result = child (order ^ k) is hit.
-__device__ __forceinline__ unsigned test_group(const Scene &S, int group, int order, f3 o, f3 inv) {
+__device__ __forceinline__ unsigned test_group(const float4 *nodes, int group, int order, f3 o, f3 inv) {
     unsigned m = 0;
-    const float4 *g = S.nodes + 16 * (size_t)group;
+    const float4 *g = nodes + 16 * (size_t)group;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
         int c = order ^ k;
@@ -215,7 +218,7 @@ __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool cl
     // stack entry: group << 11 | position taken << 8 | remaining hit mask (visit order)
     uint32_t stack[kStack];
     int sp = 0;
-    uint32_t cur = test_group(S, 0, order, o, inv);
+    uint32_t cur = test_group(S.nodes, 0, order, o, inv);
     if (COUNT) nbox += 8;
     for (;;) {
         uint32_t m = cur & 0xFFu;
@@ -241,7 +244,7 @@ __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool cl
         } else {
             if (sp >= kStack) return false;  // unreachable for trees of depth <= 24
             stack[sp++] = (cur & ~(7u << 8)) | ((uint32_t)k << 8);
-            cur = ((uint32_t)(w >> 3) << 11) | test_group(S, w >> 3, order, o, inv);
+            cur = ((uint32_t)(w >> 3) << 11) | test_group(S.nodes, w >> 3, order, o, inv);
             if (COUNT) nbox += 8;
         }
     }

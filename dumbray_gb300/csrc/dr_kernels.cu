@@ -6,14 +6,16 @@
 //   k_shade_ref       DumbRenderer layer step (DumbRenderer.cu:249-443) as one forward path step:
 //                     indirect request, light photons -> shadow queue, next ray -> next queue
 //   k_shadow_ref      light -> point visibility with the reference's transparency re-casts
-//   k_shade_phys      physical path step (emission + MIS, NEE -> shadow queue, BSDF sample)
-//   k_shadow_phys     point -> light visibility
+//   k_shade_phys      physical path step (emission + MIS, NEE -> shadow queue, BSDF sample);
+//                     in the adjoint pass it also scatters gradients of emission hits
+//   k_shadow_phys     point -> light visibility; in the adjoint pass it scatters NEE gradients
 //   k_resolve         accumulators -> BlockBasedFrameBuffer<8,16> set / blend (BlockBasedFrameBuffer.impl.cuh:149-156)
 //
 // Wavefront design: queues are structure-of-arrays of float4/int4 records in HBM; work is pulled by
 // persistent warps through one atomic per warp; outputs are compacted with a warp ballot and one
 // atomic per warp.  Queue counts live in a device control block, so a whole wave is a fixed launch
-// sequence with no host synchronisation.
+// sequence with no host synchronisation (and can be captured in a CUDA graph).  Every path record
+// carries the index of its render job, so the paths of many scenes can share a wave (batches).
 #include "dr_kernels.h"
 #include "dr_shading.cuh"
 #include "dr_trace.cuh"
@@ -21,6 +23,8 @@
 #include <cstdio>
 
 namespace drd {
+
+using drk::Item;
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
@@ -42,15 +46,49 @@ __device__ __forceinline__ int warp_fetch(int *counter) {
     return __shfl_sync(0xFFFFFFFFu, base, 0);
 }
 
+// Chunked work fetch from a device counter (warp-uniform).  The chunk shrinks with the queue:
+// about 4 chunks per resident warp (152 SMs x 24 warps), between 32 and kChunk rays, so short
+// queues (late bounces, shadow queues) still spread over every resident warp.
+__device__ __forceinline__ int chunk_for(int n) { return max(32, min(kChunk, (n / (152 * 24 * 4)) & ~31)); }
+__device__ __forceinline__ bool fetch_chunk(int *counter, int n, int chunk, int &b, int &e) {
+    int base = 0;
+    if ((threadIdx.x & 31u) == 0) base = atomicAdd(counter, chunk);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base >= n) return false;
+    b = base;
+    e = min(base + chunk, n);
+    return true;
+}
+
+__device__ __forceinline__ void count_add64(unsigned long long *c, long long rays, long long nb, long long nt) {
+    for (int off = 16; off > 0; off >>= 1) {
+        rays += __shfl_xor_sync(0xFFFFFFFFu, rays, off);
+        nb += __shfl_xor_sync(0xFFFFFFFFu, nb, off);
+        nt += __shfl_xor_sync(0xFFFFFFFFu, nt, off);
+    }
+    if ((threadIdx.x & 31u) == 0) {
+        atomicAdd(c, (unsigned long long)rays);
+        atomicAdd(c + 1, (unsigned long long)nb);
+        atomicAdd(c + 2, (unsigned long long)nt);
+    }
+}
+
+__device__ __forceinline__ void accum_add(float *acc, int slot, c3 c) {
+    if (c.r != 0.0f) atomicAdd(acc + 4 * slot, c.r);
+    if (c.g != 0.0f) atomicAdd(acc + 4 * slot + 1, c.g);
+    if (c.b != 0.0f) atomicAdd(acc + 4 * slot + 2, c.b);
+}
+
 // ---------------------------------------------------------------------------------------------
-// dr_cast source: warp w of the grid owns rays [w * kChunk, (w + 1) * kChunk).
+// dr_cast: warp w of the grid owns rays [w * kChunk, (w + 1) * kChunk) of one scene.
 struct BatchSource {
     const float *o, *d;
     const int *ignore;
     int *hit_tri, *nbox, *ntri;
     float *hit_t;
     int n;
-    bool given;
+    bool given, cull;
+    const Scene *scene0;  // unused: single-scene source
     __device__ __forceinline__ bool next(int &b, int &e) {
         if (given) return false;
         given = true;
@@ -59,11 +97,15 @@ struct BatchSource {
         e = min(b + kChunk, n);
         return b < n;
     }
-    __device__ __forceinline__ void load(int i, f3 &ro, f3 &rd, int &ign) {
+    __device__ __forceinline__ void load(int i, f3 &ro, f3 &rd, int &ign, int &job) {
         ro = mkf3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
         rd = mkf3(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
         ign = ignore ? ignore[i] : -1;
+        job = 0;
     }
+    // single-scene source: never asked for a per-job scene (MULTI = false)
+    __device__ __forceinline__ const Scene &scene(int) { return *scene0; }
+    __device__ __forceinline__ bool clip(int) { return cull; }
     __device__ __forceinline__ void store(int i, const Hit &h, int nb, int nt) {
         hit_tri[i] = h.tri;
         hit_t[i] = h.tri >= 0 ? h.t : FLT_MAX;
@@ -80,14 +122,12 @@ __global__ void __launch_bounds__(128) k_cast(Scene S, const float *__restrict__
                                               float *__restrict__ hit_t, int *__restrict__ nbox, int *__restrict__ ntri) {
     uint32_t stack[kStack];
     __shared__ WarpLeafSlots slots[4];
-    BatchSource src{o, d, ignore, hit_tri, COUNT ? nbox : nullptr, COUNT ? ntri : nullptr, hit_t, n, false};
-    trace_persistent<COUNT>(S, clip != 0, src, stack, slots[threadIdx.x >> 5]);
+    BatchSource src{o, d, ignore, hit_tri, COUNT ? nbox : nullptr, COUNT ? ntri : nullptr, hit_t, n, false, clip != 0, &S};
+    trace_persistent<COUNT, false>(S, src, stack, slots[threadIdx.x >> 5]);
 }
 
 // ---------------------------------------------------------------------------------------------
 // Wave control block (int slots, zeroed at the start of every wave).
-//   ray_count[b]   rays in the queue consumed at bounce b
-//   fetch_trace[b], fetch_shade[b], fetch_shadow[b], shadow_count[b]
 struct Ctrl {
     int ray_count[kMaxBounceSlots];
     int shadow_count[kMaxBounceSlots];
@@ -99,60 +139,39 @@ struct Ctrl {
 };
 
 // Ray queue record (64 B, 4 x 16 B SoA planes):
-//   p0 = {o.xyz, pixel slot}   p1 = {d.xyz, sample index}   p2 = {throughput.rgb, prev pdf}
-//   p3 = {prev triangle, flags (bit0 = prev delta), pixel id, unused}
+//   p0 = {o.xyz, accumulator slot}   p1 = {d.xyz, sample index}   p2 = {throughput.rgb, prev pdf}
+//   p3 = {prev triangle, flags (bit 0 = prev vertex delta; bits 1.. = path index in the wave), pixel id, job}
 struct Queue {
     float4 *p0, *p1, *p2;
     int4 *p3;
 };
 // Hit record: {tri, t}
-// Shadow record (80 B): s0 = {origin.xyz, pixel slot}, s1 = {dir.xyz, target tri}, s2 = {target point.xyz, ignore tri},
-//                       s3 = {light colour rgb, -}, s4 = {contribution rgb, -}
+// Shadow record (80 B): s0 = {origin.xyz, accumulator slot}, s1 = {dir.xyz, target / light tri},
+//   s2 = {target point.xyz, ignore tri}, s3 = {light colour rgb | adjoint: path index, vertex, -}, s4 = {contribution rgb, job}
 struct ShadowQ {
     float4 *s0, *s1, *s2, *s3, *s4;
 };
 
 struct WaveArgs {
-    Scene S;
-    dr_camera cam;
-    float cam_x;            // 0.5 / tan(fov/2) for the reference pinhole lenses
-    int mode;
-    int width, height;
-    int fsaa_x, fsaa_y;
-    int spp;
+    Item inl;
+    const Item *items;
+    int n_items;
     int max_bounces;
-    int clip;
-    float pixel_size, pdx, pdy;
-    uint32_t seed;
-    uint32_t sample_base;
-    int start_block;
-    int n_slots;            // pixel slots in the block range (blocks * 128)
     long long wave_begin;   // first path index of this wave
     int wave_count;         // paths in this wave
     Queue q[2];
     float2 *hits;
     ShadowQ sq;
-    float *accum;           // [n_slots][4]
+    float *accum;           // [total slots][4]
     Ctrl *ctrl;
     unsigned long long *counters;  // counting pass only
+    int *prefix;                   // adjoint pass only
 };
 
-// Warp-sum of per-lane traversal counts into the 64-bit counters (counting pass only).
-__device__ __forceinline__ void count_add(unsigned long long *c, int rays, int nb, int nt) {
-    unsigned r = __reduce_add_sync(0xFFFFFFFFu, (unsigned)rays);
-    unsigned b = __reduce_add_sync(0xFFFFFFFFu, (unsigned)nb);
-    unsigned t = __reduce_add_sync(0xFFFFFFFFu, (unsigned)nt);
-    if (lane_id() == 0) {
-        atomicAdd(c, (unsigned long long)r);
-        atomicAdd(c + 1, (unsigned long long)b);
-        atomicAdd(c + 2, (unsigned long long)t);
-    }
-}
-
-__device__ __forceinline__ void accum_add(float *acc, int slot, c3 c) {
-    if (c.r != 0.0f) atomicAdd(acc + 4 * slot, c.r);
-    if (c.g != 0.0f) atomicAdd(acc + 4 * slot + 1, c.g);
-    if (c.b != 0.0f) atomicAdd(acc + 4 * slot + 2, c.b);
+template <bool MULTI>
+__device__ __forceinline__ const Item &job_of(const WaveArgs &A, int job) {
+    if (MULTI) return A.items[job];
+    return A.inl;
 }
 
 __device__ __forceinline__ f3 cam_to_world(const dr_camera &c, f3 d) {
@@ -161,24 +180,24 @@ __device__ __forceinline__ f3 cam_to_world(const dr_camera &c, f3 d) {
 }
 
 // Lens sample for one path.  Returns false for pixels that produce no ray.
-__device__ inline bool lens_ray(const WaveArgs &A, int x, int y, int s, uint32_t key, f3 &o, f3 &d, c3 &filter) {
-    const dr_camera &c = A.cam;
+__device__ inline bool lens_ray(const Item &I, int x, int y, int s, uint32_t key, f3 &o, f3 &d, c3 &filter) {
+    const dr_camera &c = I.camera;
     filter = mkc(1, 1, 1);
-    if (A.mode == DR_MODE_REFERENCE) {
-        int fi = s / A.fsaa_y, fj = s - fi * A.fsaa_y;
-        float px = ((float)x - ((float)A.width / 2.0f)) * A.pixel_size;
-        float py = (((float)A.height / 2.0f) - (float)y) * A.pixel_size;
-        float sx = px + (((float)fi) + 0.5f) * A.pdx;
-        float sy = py + (((float)fj) + 0.5f) * A.pdy;
-        float ox = A.pdx / 2.0f, oy = A.pdy / 2.0f;
+    if (I.mode == DR_MODE_REFERENCE) {
+        int fi = s / I.fsaa_y, fj = s - fi * I.fsaa_y;
+        float px = ((float)x - ((float)I.width / 2.0f)) * I.pixel_size;
+        float py = (((float)I.height / 2.0f) - (float)y) * I.pixel_size;
+        float sx = px + (((float)fi) + 0.5f) * I.pdx;
+        float sy = py + (((float)fj) + 0.5f) * I.pdy;
+        float ox = I.pdx / 2.0f, oy = I.pdy / 2.0f;
         if (c.lens == DR_LENS_DEFAULT_PERSPECTIVE) {
             o = f3{0, 0, 0};
-            d = norm3(f3{sx, sy, A.cam_x});
+            d = norm3(f3{sx, sy, I.cam_x});
         } else if (c.lens == DR_LENS_SIMPLE_STOCHASTIC) {
             float jx = (rnd(key, kLensBounce, 0) * (ox - (-ox))) + (-ox);
             float jy = (rnd(key, kLensBounce, 1) * (oy - (-oy))) + (-oy);
             o = f3{0, 0, 0};
-            d = f3{sx + jx, sy + jy, A.cam_x};
+            d = f3{sx + jx, sy + jy, I.cam_x};
         } else {
             float jx = (rnd(key, kLensBounce, 0) * (ox - (-ox))) + (-ox);
             float jy = (rnd(key, kLensBounce, 1) * (oy - (-oy))) + (-oy);
@@ -195,8 +214,8 @@ __device__ inline bool lens_ray(const WaveArgs &A, int x, int y, int s, uint32_t
         }
     } else {
         float jx = rnd(key, kLensBounce, 0), jy = rnd(key, kLensBounce, 1);
-        float sx = ((float)x + jx - 0.5f * (float)A.width) / (float)A.height;
-        float sy = (0.5f * (float)A.height - ((float)y + jy)) / (float)A.height;
+        float sx = ((float)x + jx - 0.5f * (float)I.width) / (float)I.height;
+        float sy = (0.5f * (float)I.height - ((float)y + jy)) / (float)I.height;
         f3 dl;
         const float PI = 3.14159265358979f;
         if (c.lens == DR_LENS_FISHEYE) {
@@ -211,9 +230,8 @@ __device__ inline bool lens_ray(const WaveArgs &A, int x, int y, int s, uint32_t
             float v = sy * (c.angle[1] * PI / 180.0f);
             dl = f3{sinf(h) * cosf(v), sinf(v), cosf(h) * cosf(v)};
         } else {
-            dl = norm3(f3{sx, sy, A.cam_x});
+            dl = norm3(f3{sx, sy, I.cam_x});
         }
-        o = f3{0, 0, 0};
         d = norm3(cam_to_world(c, dl));
         o = f3{c.position[0], c.position[1], c.position[2]};
         return true;
@@ -223,6 +241,20 @@ __device__ inline bool lens_ray(const WaveArgs &A, int x, int y, int s, uint32_t
     return true;
 }
 
+// The job owning global path index g (jobs sorted by path_begin).
+template <bool MULTI>
+__device__ __forceinline__ int job_of_path(const WaveArgs &A, long long g) {
+    if (!MULTI) return 0;
+    int lo = 0, hi = A.n_items - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (A.items[mid].path_begin <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <bool MULTI>
 __global__ void __launch_bounds__(256) k_camera(WaveArgs A) {
     Ctrl *C = A.ctrl;
     for (;;) {
@@ -232,23 +264,27 @@ __global__ void __launch_bounds__(256) k_camera(WaveArgs A) {
         bool valid = i < A.wave_count;
         f3 o = f3{0, 0, 0}, d = f3{0, 0, 1};
         c3 filt = mkc(0, 0, 0);
-        int slot = 0, pixel = 0;
+        int slot = 0, pixel = 0, job = 0;
         uint32_t sample = 0;
         if (valid) {
             long long g = A.wave_begin + i;
-            int s = (int)(g / A.n_slots);
-            slot = (int)(g - (long long)s * A.n_slots);
-            int blk = A.start_block + slot / (DR_BLOCK_W * DR_BLOCK_H);
-            int pid = slot % (DR_BLOCK_W * DR_BLOCK_H);
-            int bw = (A.width + DR_BLOCK_W - 1) / DR_BLOCK_W;
+            job = job_of_path<MULTI>(A, g);
+            const Item &I = job_of<MULTI>(A, job);
+            long long lp = g - I.path_begin;
+            int s = (int)(lp / I.n_slots);
+            int lslot = (int)(lp - (long long)s * I.n_slots);
+            slot = I.slot_begin + lslot;
+            int blk = I.start_block + lslot / (DR_BLOCK_W * DR_BLOCK_H);
+            int pid = lslot % (DR_BLOCK_W * DR_BLOCK_H);
+            int bw = (I.width + DR_BLOCK_W - 1) / DR_BLOCK_W;
             int by = blk / bw, bx = blk - by * bw;
             int x = bx * DR_BLOCK_W + (pid % DR_BLOCK_W), y = by * DR_BLOCK_H + pid / DR_BLOCK_W;
-            valid = (x < A.width) && (y < A.height);
+            valid = (x < I.width) && (y < I.height);
             if (valid) {
-                pixel = y * A.width + x;
-                sample = A.sample_base + (uint32_t)s;
-                uint32_t key = path_key(A.seed, (uint32_t)pixel, sample);
-                valid = lens_ray(A, x, y, s, key, o, d, filt);
+                pixel = y * I.width + x;
+                sample = I.sample_base + (uint32_t)s;
+                uint32_t key = path_key(I.seed, (uint32_t)pixel, sample);
+                valid = lens_ray(I, x, y, s, key, o, d, filt);
             }
         }
         int w = warp_alloc(&C->ray_count[0], valid);
@@ -257,37 +293,32 @@ __global__ void __launch_bounds__(256) k_camera(WaveArgs A) {
             Q.p0[w] = make_float4(o.x, o.y, o.z, __int_as_float(slot));
             Q.p1[w] = make_float4(d.x, d.y, d.z, __uint_as_float(sample));
             Q.p2[w] = make_float4(filt.r, filt.g, filt.b, 0.0f);
-            Q.p3[w] = make_int4(-1, 1, pixel, 0);
+            Q.p3[w] = make_int4(-1, 1 | (i << 1), pixel, job);
         }
     }
 }
 
-// Chunked work fetch from a device counter (warp-uniform).  The chunk shrinks with the queue:
-// about 4 chunks per resident warp (152 SMs x 24 warps), between 32 and kChunk rays, so short
-// queues (late bounces, shadow queues) still spread over every resident warp.
-__device__ __forceinline__ int chunk_for(int n) { return max(32, min(kChunk, (n / (152 * 24 * 4)) & ~31)); }
-__device__ __forceinline__ bool fetch_chunk(int *counter, int n, int chunk, int &b, int &e) {
-    int base = 0;
-    if ((threadIdx.x & 31u) == 0) base = atomicAdd(counter, chunk);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (base >= n) return false;
-    b = base;
-    e = min(base + chunk, n);
-    return true;
-}
-
+template <bool MULTI>
 struct TraceSource {
+    const WaveArgs *A;
     Queue Q;
     float2 *hits;
     int *fetch;
     int n, chunk;
     long long rays, nb, nt;
     __device__ __forceinline__ bool next(int &b, int &e) { return fetch_chunk(fetch, n, chunk, b, e); }
-    __device__ __forceinline__ void load(int i, f3 &o, f3 &d, int &ign) {
+    __device__ __forceinline__ void load(int i, f3 &o, f3 &d, int &ign, int &job) {
         float4 p0 = Q.p0[i], p1 = Q.p1[i];
+        int4 p3 = Q.p3[i];
         o = f3of(p0);
         d = f3of(p1);
-        ign = Q.p3[i].x;
+        ign = p3.x;
+        job = p3.w;
+    }
+    __device__ __forceinline__ const Scene &scene(int job) { return job_of<MULTI>(*A, job).S; }
+    __device__ __forceinline__ bool clip(int job) {
+        const Item &I = job_of<MULTI>(*A, job);
+        return I.mode == DR_MODE_REFERENCE && I.clip != 0;
     }
     __device__ __forceinline__ void store(int i, const Hit &h, int b_, int t_) {
         hits[i] = make_float2(__int_as_float(h.tri), h.t);
@@ -297,36 +328,22 @@ struct TraceSource {
     }
 };
 
-__device__ __forceinline__ void count_add64(unsigned long long *c, long long rays, long long nb, long long nt) {
-    for (int off = 16; off > 0; off >>= 1) {
-        rays += __shfl_xor_sync(0xFFFFFFFFu, rays, off);
-        nb += __shfl_xor_sync(0xFFFFFFFFu, nb, off);
-        nt += __shfl_xor_sync(0xFFFFFFFFu, nt, off);
-    }
-    if ((threadIdx.x & 31u) == 0) {
-        atomicAdd(c, (unsigned long long)rays);
-        atomicAdd(c + 1, (unsigned long long)nb);
-        atomicAdd(c + 2, (unsigned long long)nt);
-    }
-}
-
-template <bool COUNT>
+template <bool COUNT, bool MULTI>
 __global__ void __launch_bounds__(256, 3) k_trace(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const int n = *((volatile int *)&C->ray_count[b]);
-    const bool clip = A.mode == DR_MODE_REFERENCE ? (A.clip != 0) : false;
     uint32_t stack[kStack];
     __shared__ WarpLeafSlots slots[8];
-    TraceSource src{A.q[b & 1], A.hits, &C->fetch_trace[b], n, chunk_for(n), 0, 0, 0};
-    trace_persistent<COUNT>(A.S, clip, src, stack, slots[threadIdx.x >> 5]);
+    TraceSource<MULTI> src{&A, A.q[b & 1], A.hits, &C->fetch_trace[b], n, chunk_for(n), 0, 0, 0};
+    trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5]);
     if (COUNT) count_add64(A.counters, src.rays, src.nb, src.nt);
 }
 
 // Reference semantics: one layer of DumbRenderer's state machine, with the layer gather folded
 // into a forward throughput (getReflectedColor is linear in the photon colour).
+template <bool MULTI>
 __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
-    const Scene &S = A.S;
     const Queue Q = A.q[b & 1];
     const Queue N = A.q[(b + 1) & 1];
     const int n = *((volatile int *)&C->ray_count[b]);
@@ -337,7 +354,7 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
         bool active = i < n;
         int tri = -1;
         float4 p0, p1, p2;
-        int4 p3;
+        int4 p3 = make_int4(0, 0, 0, 0);
         float t = 0.0f;
         if (active) {
             float2 h = A.hits[i];
@@ -349,6 +366,8 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
             p3 = Q.p3[i];
         }
         active = active && tri >= 0;
+        const Item &I = job_of<MULTI>(A, p3.w);
+        const Scene &S = I.S;
         bool child = false;
         f3 hp = f3{0, 0, 0}, cd = f3{0, 0, 0};
         c3 thr = mkc(0, 0, 0);
@@ -357,8 +376,8 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
             f3 o = f3of(p0), d = f3of(p1);
             hp = xadd(o, xmul(d, t));
             thr = mkc(p2.x, p2.y, p2.z);
-            key = path_key(A.seed, (uint32_t)p3.z, __float_as_uint(p1.w));
-            if (b < A.max_bounces) {
+            key = path_key(I.seed, (uint32_t)p3.z, __float_as_uint(p1.w));
+            if (b < I.max_bounces) {
                 const Material &m = S.mats[__ldg(S.mat_id + tri)];
                 TriV v = load_tri(S.tris, tri), nt = load_tri(S.nrms, tri);
                 int ctype = 0;
@@ -369,18 +388,19 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
                 }
                 if (child) {
                     c3 w = ref_reflect(S, tri, hp, neg3(cd), neg3(d), false, ctype);
-                    child = true;
-                    // throughput of the child layer
-                    p2 = make_float4(thr.r * w.r, thr.g * w.g, thr.b * w.b, 0.0f);
+                    p2 = make_float4(thr.r * w.r, thr.g * w.g, thr.b * w.b, 0.0f);  // throughput of the child layer
                 }
             }
         }
-        // light photons: one shadow record per light
-        for (int li = 0; li < S.n_lights; li++) {
+        // light photons: one shadow record per light of the path's scene
+        const int n_lights = MULTI ? 16 : A.inl.S.n_lights;
+        for (int li = 0; li < n_lights; li++) {
+            const bool has = active && li < S.n_lights;
+            if (MULTI && !__any_sync(0xFFFFFFFFu, has)) break;
             bool emit = false;
             f3 lo, ld;
             c3 lc, contrib;
-            if (active) {
+            if (has) {
                 light_photon(S.lights[li], hp, key, (uint32_t)b, li, lo, ld, lc);
                 c3 r = ref_reflect(S, tri, hp, ld, neg3(f3of(p1)), true, 0);
                 contrib = cmul(thr, r);
@@ -388,11 +408,11 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
             }
             int w = warp_alloc(&C->shadow_count[b], emit);
             if (emit) {
-                A.sq.s0[w] = make_float4(lo.x, lo.y, lo.z, __int_as_float(__float_as_int(p0.w)));
+                A.sq.s0[w] = make_float4(lo.x, lo.y, lo.z, p0.w);
                 A.sq.s1[w] = make_float4(ld.x, ld.y, ld.z, __int_as_float(tri));
                 A.sq.s2[w] = make_float4(hp.x, hp.y, hp.z, __int_as_float(-1));
                 A.sq.s3[w] = make_float4(lc.r, lc.g, lc.b, 0.0f);
-                A.sq.s4[w] = make_float4(contrib.r, contrib.g, contrib.b, 0.0f);
+                A.sq.s4[w] = make_float4(contrib.r, contrib.g, contrib.b, __int_as_float(p3.w));
             }
         }
         int w = warp_alloc(&C->ray_count[b + 1], child);
@@ -400,7 +420,7 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
             N.p0[w] = make_float4(hp.x, hp.y, hp.z, p0.w);
             N.p1[w] = make_float4(cd.x, cd.y, cd.z, p1.w);
             N.p2[w] = p2;
-            N.p3[w] = make_int4(tri, 0, p3.z, 0);
+            N.p3[w] = make_int4(tri, p3.y & ~1, p3.z, p3.w);
         }
     }
 }
@@ -408,12 +428,10 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
 // Reference light visibility (DumbRenderer.cu:361-428): cast from the light sample toward the
 // point; it counts if the first hit is the shaded triangle or lies within sqrt(8 eps) of the
 // point; otherwise the blocker's reflected colour decides whether the photon continues.
-template <bool COUNT>
+template <bool COUNT, bool MULTI>
 __global__ void __launch_bounds__(256) k_shadow_ref(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
-    const Scene &S = A.S;
     const int n = *((volatile int *)&C->shadow_count[b]);
-    const bool clip = A.clip != 0;
     for (;;) {
         int base = warp_fetch(&C->fetch_shadow[b]);
         if (base >= n) break;
@@ -421,6 +439,9 @@ __global__ void __launch_bounds__(256) k_shadow_ref(WaveArgs A, int b) {
         int casts = 0, nb = 0, nt = 0;
         if (i < n) {
             float4 s0 = A.sq.s0[i], s1 = A.sq.s1[i], s2 = A.sq.s2[i], s3 = A.sq.s3[i], s4 = A.sq.s4[i];
+            const Item &I = job_of<MULTI>(A, __float_as_int(s4.w));
+            const Scene &S = I.S;
+            const bool clip = I.clip != 0;
             f3 lo = f3of(s0), ld = f3of(s1), hp = f3of(s2);
             int target = __float_as_int(s1.w);
             int slot = __float_as_int(s0.w);
@@ -444,14 +465,39 @@ __global__ void __launch_bounds__(256) k_shadow_ref(WaveArgs A, int b) {
                 } else break;
             }
         }
-        if (COUNT) count_add(A.counters + 3, casts, nb, nt);
+        if (COUNT) count_add64(A.counters + 3, casts, nb, nt);
     }
 }
 
-// Physical path step.
+// Adjoint helpers: dL/dI of the pixel behind an accumulator slot, divided by spp (the pixel is the
+// mean of its samples).
+__device__ __forceinline__ c3 pixel_adjoint(const Item &I, int slot) {
+    int lslot = slot - I.slot_begin;
+    const float4 g = __ldg(reinterpret_cast<const float4 *>(I.dl_dfb) + (size_t)I.start_block * (DR_BLOCK_W * DR_BLOCK_H) + lslot);
+    return mkc(g.x * I.inv_spp, g.y * I.inv_spp, g.z * I.inv_spp);
+}
+// A contribution c (per channel) carrying the albedo factors of path vertices prefix[0..last]:
+// d c / d albedo_k = c / albedo_k for each such vertex (every material scales the throughput, and
+// the NEE BSDF, linearly by its albedo).
+__device__ __forceinline__ void scatter_albedo(const Item &I, const int *pre, int last, c3 delta, c3 c) {
+    const float gr = delta.r * c.r, gg = delta.g * c.g, gb = delta.b * c.b;
+    if (gr == 0.0f && gg == 0.0f && gb == 0.0f) return;
+    for (int j = 0; j <= last; j++) {
+        int k = pre[j];
+        const float *a = I.S.albedo + 3 * (size_t)k;
+        float ar = __ldg(a), ag = __ldg(a + 1), ab = __ldg(a + 2);
+        float *g = I.grad_albedo + 3 * (size_t)k;
+        if (ar > 1e-8f && gr != 0.0f) atomicAdd(g, gr / ar);
+        if (ag > 1e-8f && gg != 0.0f) atomicAdd(g + 1, gg / ag);
+        if (ab > 1e-8f && gb != 0.0f) atomicAdd(g + 2, gb / ab);
+    }
+}
+
+// Physical path step.  ADJ: adjoint pass (no image; gradients of emission hits are scattered here,
+// vertex triangles are recorded for the NEE gradients scattered by k_shadow_phys).
+template <bool MULTI, bool ADJ>
 __global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
-    const Scene &S = A.S;
     const Queue Q = A.q[b & 1];
     const Queue N = A.q[(b + 1) & 1];
     const int n = *((volatile int *)&C->ray_count[b]);
@@ -462,7 +508,7 @@ __global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
         bool active = i < n;
         int tri = -1;
         float4 p0, p1, p2;
-        int4 p3;
+        int4 p3 = make_int4(0, 0, 0, 0);
         float t = 0.0f;
         if (active) {
             float2 h = A.hits[i];
@@ -474,6 +520,8 @@ __global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
             p3 = Q.p3[i];
         }
         active = active && tri >= 0;
+        const Item &I = job_of<MULTI>(A, p3.w);
+        const Scene &S = I.S;
         bool emit_shadow = false, child = false;
         f3 hp = f3{0, 0, 0}, sdir = f3{0, 0, 0}, nd = f3{0, 0, 0};
         c3 scontrib = mkc(0, 0, 0), thr = mkc(0, 0, 0);
@@ -481,37 +529,50 @@ __global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
         float new_pdf = 0.0f;
         int new_delta = 0;
         int slot = 0;
+        const int path = p3.y >> 1;
         if (active) {
             slot = __float_as_int(p0.w);
             f3 o = f3of(p0), d = f3of(p1);
             hp = xadd(o, xmul(d, t));
             thr = mkc(p2.x, p2.y, p2.z);
-            uint32_t key = path_key(A.seed, (uint32_t)p3.z, __float_as_uint(p1.w));
+            uint32_t key = path_key(I.seed, (uint32_t)p3.z, __float_as_uint(p1.w));
             TriV v = load_tri(S.tris, tri);
             f3 outward = tri_normal(v);
             f3 ng = norm3(outward);
             f3 wo = neg3(d);
             if (dot3(ng, wo) < 0) ng = neg3(ng);
-            float4 sh0 = __ldg(S.shade + 2 * (size_t)tri), sh1 = __ldg(S.shade + 2 * (size_t)tri + 1);
+            float4 sh = __ldg(S.shade + tri);
+            const float *emp = S.emission + 3 * (size_t)tri;
+            c3 em = mkc(__ldg(emp), __ldg(emp + 1), __ldg(emp + 2));
             // emission (one-sided, outward side)
-            if (sh1.x + sh1.y + sh1.z > 0.0f) {
+            if (em.r + em.g + em.b > 0.0f) {
                 f3 out = norm3(outward);
                 float cosl = dot3(out, wo);
                 if (cosl > 0) {
                     float w = 1.0f;
                     if (!(p3.y & 1) && S.emissive_total > 0) {
-                        float area = tri_area(v);
-                        float pl = ((sh1.x + sh1.y + sh1.z) * area) / S.emissive_total / area;
-                        float pls = pl * (t * t * sqr3(d)) / cosl;
+                        float pls = __ldg(S.light_pdf + tri) * (t * t * sqr3(d)) / cosl;
                         w = mis2(p2.w, pls);
                     }
-                    accum_add(A.accum, slot, mkc(thr.r * sh1.x * w, thr.g * sh1.y * w, thr.b * sh1.z * w));
+                    c3 c = mkc(thr.r * em.r * w, thr.g * em.g * w, thr.b * em.b * w);
+                    if (ADJ) {
+                        c3 delta = pixel_adjoint(I, slot);
+                        float *g = I.grad_emission + 3 * (size_t)tri;
+                        if (delta.r != 0.0f) atomicAdd(g, delta.r * thr.r * w);
+                        if (delta.g != 0.0f) atomicAdd(g + 1, delta.g * thr.g * w);
+                        if (delta.b != 0.0f) atomicAdd(g + 2, delta.b * thr.b * w);
+                        if (b > 0) scatter_albedo(I, A.prefix + (size_t)path * kAdjDepth, b - 1, delta, c);
+                    } else {
+                        accum_add(A.accum, slot, c);
+                    }
                 }
             }
-            if (b < A.max_bounces) {
-                int mt = __float_as_int(sh1.w);
-                c3 alb = mkc(sh0.x, sh0.y, sh0.z);
-                float alpha = fmaxf(sh0.w, 1e-3f);
+            if (ADJ) A.prefix[(size_t)path * kAdjDepth + b] = tri;
+            if (b < I.max_bounces) {
+                int mt = __float_as_int(sh.y);
+                const float *ap = S.albedo + 3 * (size_t)tri;
+                c3 alb = mkc(__ldg(ap), __ldg(ap + 1), __ldg(ap + 2));
+                float alpha = fmaxf(sh.x, 1e-3f);
                 if (mt != DR_MAT_MIRROR && S.n_emissive > 0) {
                     float u = rnd(key, (uint32_t)b, 3) * S.emissive_total;
                     int lo = 0, hi = S.n_emissive - 1;
@@ -533,10 +594,9 @@ __global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
                     float cosl = -dot3(lout, wi);
                     float cosi = dot3(ng, wi);
                     if (cosl > 0 && cosi > 0) {
-                        float4 le = __ldg(S.shade + 2 * (size_t)li + 1);
-                        float area = tri_area(lt);
-                        float pl = ((le.x + le.y + le.z) * area) / S.emissive_total / area;
-                        float pls = pl * dist2 / cosl;
+                        const float *lep = S.emission + 3 * (size_t)li;
+                        c3 le = mkc(__ldg(lep), __ldg(lep + 1), __ldg(lep + 2));
+                        float pls = __ldg(S.light_pdf + li) * dist2 / cosl;
                         c3 f;
                         float pb;
                         if (mt == DR_MAT_GLOSSY) {
@@ -553,7 +613,7 @@ __global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
                         }
                         float w = mis2(pls, pb);
                         float k = cosi / pls * w;
-                        scontrib = mkc(thr.r * f.r * le.x * k, thr.g * f.g * le.y * k, thr.b * f.b * le.z * k);
+                        scontrib = mkc(thr.r * f.r * le.r * k, thr.g * f.g * le.g * k, thr.b * f.b * le.b * k);
                         emit_shadow = (scontrib.r + scontrib.g + scontrib.b) > 0.0f;
                         sdir = ldv;
                         light_tri = li;
@@ -600,39 +660,58 @@ __global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
             A.sq.s0[ws] = make_float4(hp.x, hp.y, hp.z, __int_as_float(slot));
             A.sq.s1[ws] = make_float4(sdir.x, sdir.y, sdir.z, __int_as_float(light_tri));
             A.sq.s2[ws] = make_float4(0.f, 0.f, 0.f, __int_as_float(tri));
-            A.sq.s4[ws] = make_float4(scontrib.r, scontrib.g, scontrib.b, 0.0f);
+            if (ADJ) A.sq.s3[ws] = make_float4(__int_as_float(path), __int_as_float(b), 0.0f, 0.0f);
+            A.sq.s4[ws] = make_float4(scontrib.r, scontrib.g, scontrib.b, __int_as_float(p3.w));
         }
         int w = warp_alloc(&C->ray_count[b + 1], child);
         if (child) {
             N.p0[w] = make_float4(hp.x, hp.y, hp.z, p0.w);
             N.p1[w] = make_float4(nd.x, nd.y, nd.z, p1.w);
             N.p2[w] = make_float4(thr.r, thr.g, thr.b, new_pdf);
-            N.p3[w] = make_int4(tri, new_delta, p3.z, 0);
+            N.p3[w] = make_int4(tri, (p3.y & ~1) | new_delta, p3.z, p3.w);
         }
     }
 }
 
-// Physical visibility: closest hit from the shading point toward the sampled light point
-// (direction = light point - shading point, so the light is at t = 1), ignoring the shading
-// triangle; visible if nothing but the light triangle is hit before t = 0.999.
+template <bool MULTI, bool ADJ>
 struct ShadowPhysSource {
+    const WaveArgs *A;
     ShadowQ sq;
     float *accum;
     int *fetch;
     int n, chunk;
     long long rays, nb, nt;
     __device__ __forceinline__ bool next(int &b, int &e) { return fetch_chunk(fetch, n, chunk, b, e); }
-    __device__ __forceinline__ void load(int i, f3 &o, f3 &d, int &ign) {
+    __device__ __forceinline__ void load(int i, f3 &o, f3 &d, int &ign, int &job) {
         o = f3of(sq.s0[i]);
         d = f3of(sq.s1[i]);
         ign = __float_as_int(sq.s2[i].w);
+        job = __float_as_int(sq.s4[i].w);
     }
+    __device__ __forceinline__ const Scene &scene(int job) { return job_of<MULTI>(*A, job).S; }
+    __device__ __forceinline__ bool clip(int) { return false; }
     __device__ __forceinline__ void store(int i, const Hit &h, int b_, int t_) {
         int light_tri = __float_as_int(sq.s1[i].w);
         bool vis = (h.tri < 0) || (h.tri == light_tri) || !(h.t < 0.999f);
         if (vis) {
             float4 s4 = sq.s4[i];
-            accum_add(accum, __float_as_int(sq.s0[i].w), mkc(s4.x, s4.y, s4.z));
+            c3 c = mkc(s4.x, s4.y, s4.z);
+            int slot = __float_as_int(sq.s0[i].w);
+            if (ADJ) {
+                const Item &I = job_of<MULTI>(*A, __float_as_int(s4.w));
+                float4 s3 = sq.s3[i];
+                int path = __float_as_int(s3.x), vtx = __float_as_int(s3.y);
+                c3 delta = pixel_adjoint(I, slot);
+                const float *lep = I.S.emission + 3 * (size_t)light_tri;
+                float lr = __ldg(lep), lg = __ldg(lep + 1), lb = __ldg(lep + 2);
+                float *g = I.grad_emission + 3 * (size_t)light_tri;
+                if (lr > 0.0f && delta.r != 0.0f) atomicAdd(g, delta.r * c.r / lr);
+                if (lg > 0.0f && delta.g != 0.0f) atomicAdd(g + 1, delta.g * c.g / lg);
+                if (lb > 0.0f && delta.b != 0.0f) atomicAdd(g + 2, delta.b * c.b / lb);
+                scatter_albedo(I, A->prefix + (size_t)path * kAdjDepth, vtx, delta, c);
+            } else {
+                accum_add(accum, slot, c);
+            }
         }
         rays++;
         nb += b_;
@@ -643,31 +722,46 @@ struct ShadowPhysSource {
 // Physical visibility: closest hit from the shading point toward the sampled light point
 // (direction = light point - shading point, so the light is at t = 1), ignoring the shading
 // triangle; visible if nothing but the light triangle is hit before t = 0.999.
-template <bool COUNT>
+template <bool COUNT, bool MULTI, bool ADJ>
 __global__ void __launch_bounds__(256, 3) k_shadow_phys(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const int n = *((volatile int *)&C->shadow_count[b]);
     uint32_t stack[kStack];
     __shared__ WarpLeafSlots slots[8];
-    ShadowPhysSource src{A.sq, A.accum, &C->fetch_shadow[b], n, chunk_for(n), 0, 0, 0};
-    trace_persistent<COUNT>(A.S, false, src, stack, slots[threadIdx.x >> 5]);
+    ShadowPhysSource<MULTI, ADJ> src{&A, A.sq, A.accum, &C->fetch_shadow[b], n, chunk_for(n), 0, 0, 0};
+    trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5]);
     if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
 }
 
 // Accumulators -> frame buffer: set (blend >= 1) or blend like blendBlockPixelColor.
-__global__ void k_resolve(const float *__restrict__ accum, float4 *__restrict__ fb, int start_block, int n_slots, int width,
-                          int height, float inv_spp, float blend) {
+template <bool MULTI>
+__global__ void k_resolve(WaveArgs A, int total_slots) {
     int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= n_slots) return;
-    int blk = start_block + slot / (DR_BLOCK_W * DR_BLOCK_H);
-    int pid = slot % (DR_BLOCK_W * DR_BLOCK_H);
-    int bw = (width + DR_BLOCK_W - 1) / DR_BLOCK_W;
+    if (slot >= total_slots) return;
+    int job = 0;
+    if (MULTI) {
+        int lo = 0, hi = A.n_items - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (A.items[mid].slot_begin <= slot) lo = mid;
+            else hi = mid - 1;
+        }
+        job = lo;
+    }
+    const Item &I = job_of<MULTI>(A, job);
+    int lslot = slot - I.slot_begin;
+    if (lslot >= I.n_slots) return;
+    int blk = I.start_block + lslot / (DR_BLOCK_W * DR_BLOCK_H);
+    int pid = lslot % (DR_BLOCK_W * DR_BLOCK_H);
+    int bw = (I.width + DR_BLOCK_W - 1) / DR_BLOCK_W;
     int by = blk / bw, bx = blk - by * bw;
     int x = bx * DR_BLOCK_W + (pid % DR_BLOCK_W), y = by * DR_BLOCK_H + pid / DR_BLOCK_W;
-    if (x >= width || y >= height) return;
-    float4 a = reinterpret_cast<const float4 *>(accum)[slot];
-    float4 c = make_float4(a.x * inv_spp, a.y * inv_spp, a.z * inv_spp, 1.0f);
+    if (x >= I.width || y >= I.height) return;
+    float4 a = reinterpret_cast<const float4 *>(A.accum)[slot];
+    float4 c = make_float4(a.x * I.inv_spp, a.y * I.inv_spp, a.z * I.inv_spp, 1.0f);
+    float4 *fb = reinterpret_cast<float4 *>(I.fb);
     size_t at = (size_t)blk * (DR_BLOCK_W * DR_BLOCK_H) + pid;
+    const float blend = I.blend;
     if (blend >= 1.0f) fb[at] = c;
     else {
         float4 old = fb[at];
@@ -760,27 +854,11 @@ void Profiler::reset() {
     }
 }
 
-cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launches, Profiler *prof,
-                        unsigned long long *counters) {
-    WaveArgs A;
-    A.S = W.scene;
-    A.cam = W.camera;
-    A.cam_x = W.cam_x;
-    A.mode = W.mode;
-    A.width = W.width;
-    A.height = W.height;
-    A.fsaa_x = W.fsaa_x;
-    A.fsaa_y = W.fsaa_y;
-    A.spp = W.spp;
+static void fill_args(const WaveDesc &W, WaveArgs &A, unsigned long long *counters) {
+    A.inl = W.inl;
+    A.items = W.items;
+    A.n_items = W.n_items;
     A.max_bounces = W.max_bounces;
-    A.clip = W.clip;
-    A.pixel_size = W.pixel_size;
-    A.pdx = W.pdx;
-    A.pdy = W.pdy;
-    A.seed = W.seed;
-    A.sample_base = W.sample_base;
-    A.start_block = W.start_block;
-    A.n_slots = W.n_slots;
     A.wave_begin = W.wave_begin;
     A.wave_count = W.wave_count;
     for (int k = 0; k < 2; k++) {
@@ -798,48 +876,65 @@ cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launc
     A.accum = W.accum;
     A.ctrl = reinterpret_cast<Ctrl *>(W.ctrl);
     A.counters = counters;
-    const bool count = counters != nullptr;
-    cudaError_t e = cudaMemsetAsync(W.ctrl, 0, sizeof(Ctrl), stream);
-    if (e != cudaSuccess) return e;
+    A.prefix = W.prefix;
+}
+
+template <bool MULTI>
+static void launch_wave_t(const WaveDesc &W, const WaveArgs &A, cudaStream_t stream, Profiler &P, bool count, long long &nl) {
     const int grid = sm_count() * 8;
-    long long nl = 0;
-    Profiler dummy;
-    Profiler &P = prof ? *prof : dummy;
     P.begin(KC_CAMERA, stream);
-    k_camera<<<grid, 256, 0, stream>>>(A);
+    k_camera<MULTI><<<grid, 256, 0, stream>>>(A);
     P.end(KC_CAMERA, stream);
     nl++;
     for (int b = 0; b <= W.max_bounces; b++) {
         P.begin(KC_TRACE, stream);
-        if (count) k_trace<true><<<grid, 256, 0, stream>>>(A, b);
-        else k_trace<false><<<grid, 256, 0, stream>>>(A, b);
+        if (count) k_trace<true, MULTI><<<grid, 256, 0, stream>>>(A, b);
+        else k_trace<false, MULTI><<<grid, 256, 0, stream>>>(A, b);
         P.end(KC_TRACE, stream);
         P.begin(KC_SHADE, stream);
-        if (W.mode == DR_MODE_REFERENCE) k_shade_ref<<<grid, 256, 0, stream>>>(A, b);
-        else k_shade_phys<<<grid, 256, 0, stream>>>(A, b);
+        if (W.mode == DR_MODE_REFERENCE) k_shade_ref<MULTI><<<grid, 256, 0, stream>>>(A, b);
+        else if (W.adjoint) k_shade_phys<MULTI, true><<<grid, 256, 0, stream>>>(A, b);
+        else k_shade_phys<MULTI, false><<<grid, 256, 0, stream>>>(A, b);
         P.end(KC_SHADE, stream);
         P.begin(KC_SHADOW, stream);
         if (W.mode == DR_MODE_REFERENCE) {
-            if (count) k_shadow_ref<true><<<grid, 256, 0, stream>>>(A, b);
-            else k_shadow_ref<false><<<grid, 256, 0, stream>>>(A, b);
+            if (count) k_shadow_ref<true, MULTI><<<grid, 256, 0, stream>>>(A, b);
+            else k_shadow_ref<false, MULTI><<<grid, 256, 0, stream>>>(A, b);
+        } else if (W.adjoint) {
+            k_shadow_phys<false, MULTI, true><<<grid, 256, 0, stream>>>(A, b);
         } else {
-            if (count) k_shadow_phys<true><<<grid, 256, 0, stream>>>(A, b);
-            else k_shadow_phys<false><<<grid, 256, 0, stream>>>(A, b);
+            if (count) k_shadow_phys<true, MULTI, false><<<grid, 256, 0, stream>>>(A, b);
+            else k_shadow_phys<false, MULTI, false><<<grid, 256, 0, stream>>>(A, b);
         }
         P.end(KC_SHADOW, stream);
         nl += 3;
     }
+}
+
+cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launches, Profiler *prof,
+                        unsigned long long *counters) {
+    WaveArgs A;
+    fill_args(W, A, counters);
+    cudaError_t e = cudaMemsetAsync(W.ctrl, 0, sizeof(Ctrl), stream);
+    if (e != cudaSuccess) return e;
+    long long nl = 0;
+    Profiler dummy;
+    Profiler &P = prof ? *prof : dummy;
+    if (W.items) launch_wave_t<true>(W, A, stream, P, counters != nullptr, nl);
+    else launch_wave_t<false>(W, A, stream, P, counters != nullptr, nl);
     if (launches) *launches += nl;
     return cudaGetLastError();
 }
 
-cudaError_t launch_resolve(const float *accum, float *fb, int start_block, int n_slots, int width, int height, float inv_spp,
-                           float blend, cudaStream_t stream, long long *launches, Profiler *prof) {
+cudaError_t launch_resolve(const WaveDesc &W, int total_slots, cudaStream_t stream, long long *launches, Profiler *prof) {
+    WaveArgs A;
+    fill_args(W, A, nullptr);
     int threads = 256;
-    int blocks = (n_slots + threads - 1) / threads;
+    int blocks = (total_slots + threads - 1) / threads;
+    if (blocks == 0) return cudaSuccess;
     if (prof) prof->begin(KC_RESOLVE, stream);
-    k_resolve<<<blocks, threads, 0, stream>>>(accum, reinterpret_cast<float4 *>(fb), start_block, n_slots, width, height,
-                                             inv_spp, blend);
+    if (W.items) k_resolve<true><<<blocks, threads, 0, stream>>>(A, total_slots);
+    else k_resolve<false><<<blocks, threads, 0, stream>>>(A, total_slots);
     if (prof) prof->end(KC_RESOLVE, stream);
     if (launches) (*launches)++;
     return cudaGetLastError();

@@ -8,20 +8,38 @@
 
 namespace drd {
 constexpr int kMaxBounceSlots = 68;  // bounce limit 64 (DUMB_RENDERER_BOUNCE_LIMIT) + camera + spare
+constexpr int kAdjDepth = 66;        // prefix slots per path in the adjoint pass (bounces 0..64)
 }
 
 namespace drk {
 
-// One wave of the wavefront renderer: paths [wave_begin, wave_begin + wave_count) of the
-// (sample-major, block-major pixel slot) path space of one dr_render_blocks call.
-struct WaveDesc {
-    drd::Scene scene;
+// One render job of a wave: a scene, a camera, a block range of a frame buffer and the render
+// parameters.  A plain dr_render_blocks call is a single job passed inline in the kernel
+// arguments; a batch keeps a table of jobs in device memory and every path record carries the
+// index of its job, so the paths of many scenes share the same waves.
+struct Item {
+    drd::Scene S;
     dr_camera camera;
-    float cam_x;
+    float cam_x;                 // 0.5 / tan(fov / 2) for the pinhole lenses
     int mode, width, height, fsaa_x, fsaa_y, spp, max_bounces, clip;
     float pixel_size, pdx, pdy;
     uint32_t seed, sample_base;
     int start_block, n_slots;
+    int slot_begin;              // first pixel slot of this job in the shared accumulator
+    long long path_begin;        // first path index of this job in the wave path space
+    float *fb;                   // block-major float4 frame buffer
+    float inv_spp, blend;
+    const float *dl_dfb;         // adjoint: dL/dI, block-major float4 (null outside the adjoint pass)
+    float *grad_albedo;          // adjoint: dL/d albedo, float[n][3]
+    float *grad_emission;        // adjoint: dL/d emission, float[n][3]
+};
+
+// One wave: paths [wave_begin, wave_begin + wave_count) of the path space of all jobs.
+struct WaveDesc {
+    Item inl;                    // the job when items == nullptr
+    const Item *items;           // device job table (batches) or nullptr
+    int n_items;
+    int mode, max_bounces;
     long long wave_begin;
     int wave_count;
     float4 *q_p0[2], *q_p1[2], *q_p2[2];
@@ -30,6 +48,8 @@ struct WaveDesc {
     float4 *s[5];
     float *accum;
     void *ctrl;
+    int *prefix;                 // adjoint: [wave capacity][kAdjDepth] triangle of each path vertex
+    bool adjoint;
 };
 
 // Kernel classes for per-class timing.
@@ -62,7 +82,7 @@ cudaError_t launch_cast(const drd::Scene &S, const float *o, const float *d, con
 // counters (nullable): 6 x u64 = {trace rays, trace box tests, trace tri tests, shadow casts, shadow box tests, shadow tri tests}
 cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launches, Profiler *prof,
                         unsigned long long *counters);
-cudaError_t launch_resolve(const float *accum, float *fb, int start_block, int n_slots, int width, int height, float inv_spp,
-                           float blend, cudaStream_t stream, long long *launches, Profiler *prof);
+// Frame-buffer resolve of all jobs: `total_slots` pixel slots of the shared accumulator.
+cudaError_t launch_resolve(const WaveDesc &W, int total_slots, cudaStream_t stream, long long *launches, Profiler *prof);
 
 }  // namespace drk

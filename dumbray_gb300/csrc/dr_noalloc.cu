@@ -22,6 +22,7 @@
 //   * the first call on a device looks up the array's device address (cudaGetSymbolAddress) with
 //     that device current and caches it; make that first call before any stream capture begins.
 #include <algorithm>
+#include <cstring>
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -120,23 +121,25 @@ extern "C" dr_status dr_render_blocks_noalloc(const dr_scene *sc, const dr_camer
     if (e != cudaSuccess) return nfail(DR_E_CUDA, std::string("dr_render_blocks_noalloc: clear: ") + cudaGetErrorString(e));
 
     drk::WaveDesc W;
-    W.scene = *S;
-    W.camera = *cam;
+    std::memset(&W, 0, sizeof(W));
+    drk::Item &I = W.inl;
+    I.S = *S;
+    I.camera = *cam;
     {
         float angle = cam->angle[0];
         if (angle < 1.0f) angle = 1.0f;
         else if (angle > 179.0f) angle = 179.0f;
         float radian = (angle / (2 * 57.29577951308233f));
-        W.cam_x = 0.5f / std::tan(radian);
+        I.cam_x = 0.5f / std::tan(radian);
     }
-    W.mode = p->mode;
-    W.width = p->width;
-    W.height = p->height;
-    W.fsaa_x = fx;
-    W.fsaa_y = fy;
-    W.spp = spp;
-    W.max_bounces = p->max_bounces;
-    W.clip = p->cull_backfaces;
+    I.mode = p->mode;
+    I.width = p->width;
+    I.height = p->height;
+    I.fsaa_x = fx;
+    I.fsaa_y = fy;
+    I.spp = spp;
+    I.max_bounces = p->max_bounces;
+    I.clip = p->cull_backfaces;
     {
         float w = (float)p->width, h = (float)p->height;
         float ps;
@@ -144,14 +147,22 @@ extern "C" dr_status dr_render_blocks_noalloc(const dr_scene *sc, const dr_camer
         else if (p->boxing == DR_BOXING_WIDTH) ps = 1.0f / w;
         else if (p->boxing == DR_BOXING_MIN) ps = 1.0f / ((h <= w) ? h : w);
         else ps = 1.0f / ((h >= w) ? h : w);
-        W.pixel_size = ps;
-        W.pdx = ps / (float)fx;
-        W.pdy = ps / (float)fy;
+        I.pixel_size = ps;
+        I.pdx = ps / (float)fx;
+        I.pdy = ps / (float)fy;
     }
-    W.seed = p->seed;
-    W.sample_base = (uint32_t)((p->iteration < 1 ? 0 : p->iteration - 1) * spp);
-    W.start_block = start_block;
-    W.n_slots = n_slots;
+    I.seed = p->seed;
+    I.sample_base = (uint32_t)((p->iteration < 1 ? 0 : p->iteration - 1) * spp);
+    I.start_block = start_block;
+    I.n_slots = n_slots;
+    I.fb = fb;
+    I.inv_spp = 1.0f / (float)spp;
+    I.blend = (p->iteration <= 1) ? 1.0f : (1.0f / (float)p->iteration);
+    W.items = nullptr;
+    W.n_items = 1;
+    W.mode = p->mode;
+    W.max_bounces = p->max_bounces;
+    W.adjoint = false;
     for (int k = 0; k < 2; k++) {
         W.q_p0[k] = reinterpret_cast<float4 *>(base + kOffQueues + (4 * k + 0) * kQueuePlane);
         W.q_p1[k] = reinterpret_cast<float4 *>(base + kOffQueues + (4 * k + 1) * kQueuePlane);
@@ -162,6 +173,7 @@ extern "C" dr_status dr_render_blocks_noalloc(const dr_scene *sc, const dr_camer
     for (int j = 0; j < 5; j++) W.s[j] = reinterpret_cast<float4 *>(base + kOffShadow + j * kShadowPlane);
     W.accum = accum;
     W.ctrl = base + kOffCtrl;
+    W.prefix = nullptr;
     long long launches = 0;
     const long long total = (long long)n_slots * spp;
     for (long long b = 0; b < total; b += wave) {
@@ -170,9 +182,7 @@ extern "C" dr_status dr_render_blocks_noalloc(const dr_scene *sc, const dr_camer
         e = drk::launch_wave(W, stream, &launches, nullptr, nullptr);
         if (e != cudaSuccess) return nfail(DR_E_CUDA, std::string("dr_render_blocks_noalloc: wave: ") + cudaGetErrorString(e));
     }
-    const float blend = (p->iteration <= 1) ? 1.0f : (1.0f / (float)p->iteration);
-    e = drk::launch_resolve(accum, fb, start_block, n_slots, p->width, p->height, 1.0f / (float)spp, blend, stream, &launches,
-                            nullptr);
+    e = drk::launch_resolve(W, n_slots, stream, &launches, nullptr);
     if (e != cudaSuccess) return nfail(DR_E_CUDA, std::string("dr_render_blocks_noalloc: resolve: ") + cudaGetErrorString(e));
     return DR_OK;
 }

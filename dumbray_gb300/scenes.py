@@ -12,6 +12,11 @@ Workloads (no public dataset is involved; every input is generated from a seed):
                                   value noise (amplitude 0.1, seed 1): the ray-cast microbenchmark mesh.
   * ``full_scene``              - the displaced mesh + a 2-triangle ground plane + 4 emissive quads,
                                   materials chosen by a hash of the triangle index.
+  * ``batch_workload``          - 64 independent scenes (triangle counts log-uniform 1k-2M: a displaced
+                                  icosphere plus random boxes), resolutions from {128..1024}^2, spp from
+                                  {4, 16, 64}, depth 6, seeds 0-63.
+  * ``differentiable_scene``    - icosphere level 7 + box (about 200k triangles), per-triangle albedo
+                                  U[0.1, 0.9], emission on 64 triangles: the gradient workload.
 """
 from __future__ import annotations
 
@@ -20,7 +25,7 @@ import numpy as np
 __all__ = [
     "icosphere", "displace_value_noise", "box", "quad", "outward_ok", "flat_normals",
     "box_and_icosphere", "displaced_icosphere", "full_scene", "camera_basis", "primary_rays",
-    "incoherent_rays", "tri_hash_u32",
+    "incoherent_rays", "tri_hash_u32", "random_boxes", "batch_workload", "differentiable_scene",
 ]
 
 
@@ -251,3 +256,99 @@ def incoherent_rays(n: int, lo, hi, seed: int = 0):
     d = rng.normal(size=(n, 3))
     d /= np.linalg.norm(d, axis=1, keepdims=True)
     return o.astype(np.float32), d.astype(np.float32)
+
+
+def random_boxes(n: int, rng, lo=-1.6, hi=1.6, size=(0.02, 0.25)) -> np.ndarray:
+    """``n`` closed axis-aligned boxes (12 triangles each, outward normals), centres uniform in
+    [lo, hi]^3 and edge lengths uniform in ``size``."""
+    if n <= 0:
+        return np.zeros((0, 3, 3), np.float32)
+    unit = box((1.0, 1.0, 1.0)).astype(np.float64)              # [12, 3, 3]
+    ext = rng.uniform(size[0], size[1], size=(n, 1, 1, 3))
+    ctr = rng.uniform(lo, hi, size=(n, 1, 1, 3))
+    return (unit[None] * ext + ctr).reshape(-1, 3, 3).astype(np.float32)
+
+
+_DISPLACED_CACHE: dict = {}
+
+
+def _displaced_level(level: int) -> np.ndarray:
+    if level not in _DISPLACED_CACHE:
+        _DISPLACED_CACHE[level] = displaced_icosphere(level, 0.1, 1)
+    return _DISPLACED_CACHE[level]
+
+
+def _rotation(rng) -> np.ndarray:
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def batch_workload(n_scenes: int = 64, seed: int = 0, min_tris: int = 1000, max_tris: int = 2_000_000,
+                   resolutions=(128, 256, 512, 1024), spps=(4, 16, 64), depth: int = 6):
+    """The batched-rendering workload: ``n_scenes`` independent scenes.
+
+    Scene i: target triangle count T log-uniform in [min_tris, max_tris]; the largest displaced
+    icosphere (3-octave value noise, amplitude 0.1) with at most T triangles, randomly rotated and
+    scaled to radius U[0.5, 0.9], plus ceil((T - icosphere) / 12) random boxes around it, a 2-triangle
+    ground plane and one emissive quad (radiance 10) above; materials by triangle-index hash as in
+    ``full_scene``.  Resolution square, uniform from ``resolutions``; spp uniform from ``spps``;
+    render seed i.  Returns a list of dicts (tris, mat_id, albedo, roughness, emission, width,
+    height, spp, depth, seed, camera position/target)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_scenes):
+        target = int(round(np.exp(rng.uniform(np.log(min_tris), np.log(max_tris)))))
+        level = 0
+        while 20 * 4 ** (level + 1) <= target and level < 8:
+            level += 1
+        mesh = _displaced_level(level).astype(np.float64)
+        rot = _rotation(rng)
+        radius = rng.uniform(0.5, 0.9)
+        mesh = (mesh @ rot.T * radius).astype(np.float32)
+        n_boxes = max(0, -(-(target - len(mesh)) // 12))
+        boxes = random_boxes(n_boxes, rng)
+        ground = quad((0.0, -1.7, 0.0), (12.0, 12.0), (0.0, 1.0, 0.0))
+        light = quad((0.0, 2.5, 0.0), (1.5, 1.5), (0.0, -1.0, 0.0))
+        tris = np.concatenate([mesh, boxes, ground, light], axis=0)
+        n = len(tris)
+        h = tri_hash_u32(np.arange(n), i) % 100
+        mat = np.where(h < 60, 0, np.where(h < 85, 1, 2)).astype(np.int32)
+        albedo = rng.uniform(0.2, 0.8, size=(n, 3)).astype(np.float32)
+        rough = rng.uniform(0.05, 0.4, size=n).astype(np.float32)
+        mat[-4:] = 0
+        albedo[-4:-2] = 0.5
+        albedo[-2:] = 0.0
+        emission = np.zeros((n, 3), np.float32)
+        emission[-2:] = 10.0
+        res = int(rng.choice(resolutions))
+        spp = int(rng.choice(spps))
+        ang = rng.uniform(0.0, 2.0 * np.pi)
+        cam_pos = (float(3.4 * np.sin(ang)), 0.8, float(-3.4 * np.cos(ang)))
+        out.append(dict(tris=tris, mat_id=mat, albedo=albedo, roughness=rough, emission=emission, width=res,
+                        height=res, spp=spp, depth=depth, seed=i, cam_pos=cam_pos, cam_target=(0.0, 0.0, 0.0),
+                        target_tris=target, level=level, n_boxes=n_boxes))
+    return out
+
+
+def differentiable_scene(level: int = 7, n_emissive: int = 64, seed: int = 7):
+    """Gradient workload: icosphere ``level`` (327,680 triangles at level 7 is the next subdivision
+    above 200k; level 7 it is) of radius 0.6 inside a 12-triangle 2x2x2 room; per-triangle albedo
+    U[0.1, 0.9]^3 (Lambert); emission 10 on ``n_emissive`` sphere triangles picked by a seeded hash.
+    Returns dict(tris, mat_id, albedo, emission, roughness, emissive_ids) and hidden target
+    parameters (albedo_target = an independent U[0.1, 0.9] draw, same emission)."""
+    room = box((2.0, 2.0, 2.0), inward=True)
+    sphere = icosphere(level, radius=0.6)
+    tris = np.concatenate([room, sphere], axis=0)
+    n = len(tris)
+    rng = np.random.default_rng(seed)
+    albedo = rng.uniform(0.1, 0.9, size=(n, 3)).astype(np.float32)
+    albedo_target = rng.uniform(0.1, 0.9, size=(n, 3)).astype(np.float32)
+    ids = len(room) + np.sort(rng.choice(len(sphere), size=n_emissive, replace=False))
+    emission = np.zeros((n, 3), np.float32)
+    emission[ids] = 10.0
+    return dict(tris=tris, mat_id=np.zeros(n, np.int32), albedo=albedo, albedo_target=albedo_target,
+                emission=emission, roughness=np.full(n, 0.2, np.float32), emissive_ids=ids, n_room=len(room))

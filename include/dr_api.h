@@ -235,6 +235,42 @@ void dr_renderer_destroy(dr_renderer *r);
 dr_status dr_render_blocks(dr_renderer *r, const dr_scene *scene, const dr_camera *camera, float *fb_blockmajor,
                            int32_t start_block, int32_t end_block, const dr_render_params *params, void *stream);
 
+/* ---- differentiable rendering (no reference counterpart) -------------------------------------
+ * Path-replay adjoint of the physical-mode render: given dL/dI for the pixels of blocks
+ * [start_block, end_block) (block-major float4, device), ADDS dL/d albedo and dL/d emission
+ * (device float[n][3] each) for the scene's triangles.  The paths are regenerated from the
+ * counter-based random numbers of `params` (same seed / iteration as the forward render), so no
+ * path is stored between the passes: memory is the renderer's wave scratch plus one triangle id
+ * per path vertex of the paths in flight.  Sampling pdfs (light selection, BSDF, MIS) are treated
+ * as constants, which keeps the gradient estimate unbiased. */
+dr_status dr_render_adjoint(dr_renderer *r, const dr_scene *scene, const dr_camera *camera, const float *dl_dfb_blockmajor,
+                            int32_t start_block, int32_t end_block, const dr_render_params *params, float *grad_albedo,
+                            float *grad_emission, void *stream);
+
+/* ---- batches (no reference counterpart) -------------------------------------------------------
+ * Many independent render jobs (scenes, cameras, frame buffers, resolutions, sample counts) whose
+ * paths share the same wavefront waves, so small jobs fill the GPU together.  All jobs of a batch
+ * use the same render mode.  dr_batch_render with use_graph = 1 captures the whole launch
+ * sequence once into a CUDA graph (per renderer scratch set, captured on a private stream, so the
+ * caller's stream may be the legacy default stream) and replays it on the caller's stream;
+ * dr_batch_set_iteration changes the progressive iteration of every job without re-capturing (it
+ * first waits for the batch's previous render, which reads the same job table).  A batch must not
+ * be rendered on two streams at once, and a renderer's scratch serves one render at a time. */
+typedef struct dr_batch dr_batch;
+typedef struct {
+    const dr_scene *scene;
+    dr_camera camera;
+    dr_render_params params;
+    float *fb;
+    int32_t start_block, end_block;
+} dr_batch_item;
+
+dr_status dr_batch_create(const dr_batch_item *items, int32_t n, dr_batch **out);
+dr_status dr_batch_set_iteration(dr_batch *batch, int32_t iteration);
+dr_status dr_batch_render(dr_renderer *r, dr_batch *batch, int32_t use_graph, void *stream);
+int64_t dr_batch_paths(const dr_batch *batch);
+void dr_batch_destroy(dr_batch *batch);
+
 /* Allocation-free variant of dr_render_blocks.  It has no counterpart in the reference: it exists
  * for callers that cannot allocate device memory while they render (a host rendering inside a CUDA
  * stream capture, a plugin host whose device memory belongs to another pool, a latency-critical

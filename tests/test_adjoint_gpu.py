@@ -1,0 +1,159 @@
+"""Path-replay adjoint (dr_render_adjoint): gradients of an L2 image loss with respect to
+per-triangle albedo and emission, checked against central finite differences with common random
+numbers on the GPU (same seeds, parameters written in place so the sampling tables stay fixed:
+the forward estimator is then a smooth function of the parameters) and against finite differences
+of the FP64 CPU oracle.  Tolerance: 1e-2 relative on the checked components."""
+import numpy as np
+import pytest
+import torch
+
+import dumbray_gb300 as dr
+from dumbray_gb300 import scenes
+import _oracle as O
+
+pytestmark = pytest.mark.gpu
+
+W = H = 32
+SPP = (2, 2)
+DEPTH = 3
+
+
+def _setup(cuda):
+    c = scenes.box_and_icosphere(2)
+    tris = c["tris"]
+    n = len(tris)
+    mats = [dr.lambert((0.7, 0.7, 0.7)), dr.glossy((0.8, 0.6, 0.4), 0.3), dr.mirror((0.9, 0.9, 0.9))]
+    h = scenes.tri_hash_u32(np.arange(n), 2) % 100
+    mat = np.where(h < 70, 0, np.where(h < 90, 1, 2)).astype(np.int32)
+    lo = c["n_room"] + c["n_sphere"]
+    mat[lo:] = 0
+    rng = np.random.default_rng(7)
+    albedo = rng.uniform(0.2, 0.8, (n, 3)).astype(np.float32)
+    emission = np.zeros((n, 3), np.float32)
+    emission[lo:] = 10.0
+    rough = np.full(n, 0.3, np.float32)
+    sc = dr.Scene(tris, mat_id=mat, materials=mats)
+    sc.set_triangle_params(albedo, emission, rough)
+    cam = dr.camera(dr.LENS_PINHOLE, position=(0.0, 0.0, -0.99), angle=60.0)
+    p = dr.render_params(W, H, dr.MODE_PHYSICAL, samples=SPP, max_bounces=DEPTH, seed=3)
+    target_alb = np.clip(albedo + rng.normal(0, 0.15, albedo.shape), 0.05, 0.95).astype(np.float32)
+    return sc, cam, p, tris, mat, mats, albedo, emission, rough, target_alb
+
+
+def _render(sc, cam, p, cuda):
+    fb = dr.new_frame_buffer(W, H, cuda)
+    dr.Renderer(1 << 14).render_blocks(sc, cam, fb, 0, dr.block_count(W, H), p)
+    torch.cuda.synchronize()
+    return fb
+
+
+def _loss(fb, target):
+    d = (fb[:, :3].double() - target[:, :3].double())
+    return float((d * d).sum())
+
+
+def test_adjoint_matches_central_differences_with_common_random_numbers(cuda):
+    sc, cam, p, tris, mat, mats, albedo, emission, rough, target_alb = _setup(cuda)
+    n = len(tris)
+    a_ptr, e_ptr = sc.triangle_params_device()
+    alb_dev = dr.device_view(a_ptr, (n, 3), cuda)
+    emi_dev = dr.device_view(e_ptr, (n, 3), cuda)
+    alb_dev.copy_(torch.from_numpy(target_alb).to(cuda))
+    target = _render(sc, cam, p, cuda)
+    alb_dev.copy_(torch.from_numpy(albedo).to(cuda))
+    img = _render(sc, cam, p, cuda)
+    dl = torch.zeros_like(img)
+    dl[:, :3] = 2.0 * (img[:, :3] - target[:, :3])
+    ga = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
+    ge = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
+    dr.Renderer(1 << 14).render_adjoint(sc, cam, dl, 0, dr.block_count(W, H), p, ga, ge)
+    torch.cuda.synchronize()
+    ga_h, ge_h = ga.cpu().numpy(), ge.cpu().numpy()
+    # albedo: the 8 largest-gradient components
+    flat = np.argsort(-np.abs(ga_h).ravel())[:8]
+    for f in flat:
+        k, ch = divmod(int(f), 3)
+        hstep = 1e-3
+        vals = []
+        for sgn in (1, -1):
+            alb_dev[k, ch] = float(albedo[k, ch]) + sgn * hstep
+            vals.append(_loss(_render(sc, cam, p, cuda), target))
+        alb_dev[k, ch] = float(albedo[k, ch])
+        fd = (vals[0] - vals[1]) / (2 * hstep)
+        assert abs(ga_h[k, ch] - fd) <= 1e-2 * abs(fd) + 1e-6, (k, ch, ga_h[k, ch], fd)
+    # emission: both emitter triangles, every channel
+    for k in range(n - 2, n):
+        for ch in range(3):
+            hstep = 1e-2
+            vals = []
+            for sgn in (1, -1):
+                emi_dev[k, ch] = float(emission[k, ch]) + sgn * hstep
+                vals.append(_loss(_render(sc, cam, p, cuda), target))
+            emi_dev[k, ch] = float(emission[k, ch])
+            fd = (vals[0] - vals[1]) / (2 * hstep)
+            assert abs(ge_h[k, ch] - fd) <= 1e-2 * abs(fd) + 1e-6, (k, ch, ge_h[k, ch], fd)
+
+
+def test_adjoint_matches_fp64_oracle_finite_differences(cuda):
+    """Reference gradient: central differences of the FP64 CPU oracle's loss (same estimator, same
+    random numbers, double precision), albedo of the 4 largest-gradient triangles."""
+    sc, cam, p, tris, mat, mats, albedo, emission, rough, target_alb = _setup(cuda)
+    n = len(tris)
+    osc = O.OracleScene(tris, mat_id=mat, materials=mats)
+    osc.set_triangle_params(target_alb, emission, rough)
+    t_or = osc.render_blocks(cam, p).astype(np.float64)
+    osc.set_triangle_params(albedo, emission, rough)
+    img_or = osc.render_blocks(cam, p).astype(np.float64)
+    img = _render(sc, cam, p, cuda)
+    # the adjoint weights come from the GPU image; the oracle's own loss uses its own image
+    dl = torch.zeros_like(img)
+    dl[:, :3] = torch.from_numpy(2.0 * (img_or[:, :3] - t_or[:, :3])).float().to(cuda)
+    ga = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
+    ge = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
+    dr.Renderer(1 << 14).render_adjoint(sc, cam, dl, 0, dr.block_count(W, H), p, ga, ge)
+    torch.cuda.synchronize()
+    ga_h = ga.cpu().numpy()
+    for f in np.argsort(-np.abs(ga_h).ravel())[:4]:
+        k, ch = divmod(int(f), 3)
+        hstep = 1e-3
+        vals = []
+        for sgn in (1, -1):
+            a2 = albedo.copy()
+            a2[k, ch] += sgn * hstep
+            osc.set_triangle_params(a2, emission, rough)
+            im = osc.render_blocks(cam, p).astype(np.float64)
+            vals.append(float(((im[:, :3] - t_or[:, :3]) ** 2).sum()))
+        fd = (vals[0] - vals[1]) / (2 * hstep)
+        assert abs(ga_h[k, ch] - fd) <= 2e-2 * abs(fd) + 1e-6, (k, ch, ga_h[k, ch], fd)
+
+
+def test_autograd_harness(cuda):
+    """torch.autograd.Function over the C ABI: backward equals a direct dr_render_adjoint call."""
+    sc, cam, p, tris, mat, mats, albedo, emission, rough, target_alb = _setup(cuda)
+    n = len(tris)
+    alb = torch.from_numpy(albedo).to(cuda).requires_grad_(True)
+    emi = torch.from_numpy(emission).to(cuda).requires_grad_(True)
+    target = torch.zeros((dr.block_count(W, H) * 128, 4), device=cuda)
+    img = dr.render_differentiable(sc, cam, p, alb, emi)
+    loss = ((img[:, :3] - target[:, :3]) ** 2).sum()
+    loss.backward()
+    dl = torch.zeros_like(img)
+    dl[:, :3] = 2.0 * img.detach()[:, :3]
+    ga = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
+    ge = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
+    dr.Renderer(1 << 14).render_adjoint(sc, cam, dl, 0, dr.block_count(W, H), p, ga, ge)
+    torch.cuda.synchronize()
+    assert torch.allclose(alb.grad, ga, rtol=1e-4, atol=1e-7)
+    assert torch.allclose(emi.grad, ge, rtol=1e-4, atol=1e-7)
+    assert float(alb.grad.abs().sum()) > 0 and float(emi.grad.abs().sum()) > 0
+
+
+def test_adjoint_rejects_reference_mode(cuda):
+    room = scenes.box((2, 2, 2), inward=True)
+    sc = dr.Scene(room, materials=[dr.dumb_based()], lights=[dr.spherical_light((1, 1, 1), (0, 0.5, 0), 0.1)])
+    cam = dr.camera(dr.LENS_SIMPLE_STOCHASTIC, position=(0.0, 0.0, -0.9))
+    p = dr.render_params(16, 16, dr.MODE_REFERENCE)
+    fb = dr.new_frame_buffer(16, 16, cuda)
+    g = torch.zeros((len(room), 3), device=cuda)
+    with pytest.raises(dr.DumbRayError):
+        dr.Renderer(1 << 12).render_adjoint(sc, cam, fb, 0, 2, p, g, g)
