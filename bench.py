@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--wave", type=int, default=1 << 22)
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer e2e pass (profiling cases)")
     ap.add_argument("--no-count", action="store_true", help="skip the traversal-counting pass (profiling cases)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable (adjoint) leg")
+    ap.add_argument("--batch-scenes", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=2, help="timed steps of each batched arm")
     return ap.parse_args()
 
 
@@ -349,10 +353,220 @@ def run_ours(a):
             "mean_rel_diff": float((g.mean() - o.mean()) / max(o.mean(), 1e-9)),
             "mean_diff_in_se": float(diff.mean() / max(diff.std(ddof=1) / np.sqrt(len(diff)), 1e-12)),
             "sample": "centre patch 12,288 px x 64 spp, same seeds"}
+    del rend
+    if rank == 0 and world == 1 and not a.no_batched:
+        out["batched"] = run_batched(dr, torch, dev, a)
+    if rank == 0 and world == 1 and not a.no_adjoint:
+        out["differentiable"] = run_differentiable(dr, torch, dev, a)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def _batch_scene(dr, job, split=0):
+    sc = dr.Scene(job["tris"], mat_id=job["mat_id"], materials=[dr.lambert(), dr.mirror(), dr.glossy()],
+                  split_threshold=split)
+    sc.set_triangle_params(job["albedo"], job["emission"], job["roughness"])
+    return sc
+
+
+def _events_ms(torch, fn, steps):
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(steps):
+        fn(i)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_batched(dr, torch, dev, a):
+    """64 independent scenes rendered scene by scene (plain dr_render_blocks launches, reference
+    octree parameters) and as one batch (shared waves, one CUDA graph, autotuned leaf sizes and wave
+    size).  Both arms render progressive iterations 1..K+1 of every job into the same frame buffers;
+    Mpaths/s = all paths of the K timed iterations / CUDA-event time."""
+    from dumbray_gb300 import autotune, scenes
+
+    t0 = time.time()
+    jobs = scenes.batch_workload(a.batch_scenes)
+    gen_s = time.time() - t0
+    n_tris = [len(j["tris"]) for j in jobs]
+    cams = [dr.camera(dr.LENS_PINHOLE, position=j["cam_pos"], target=j["cam_target"], angle=60.0) for j in jobs]
+    nbs = [dr.block_count(j["width"], j["height"]) for j in jobs]
+    fbs = [dr.new_frame_buffer(j["width"], j["height"], dev) for j in jobs]
+    paths = sum(j["width"] * j["height"] * j["spp"] for j in jobs)
+
+    def params(j, it):
+        return dr.render_params(j["width"], j["height"], dr.MODE_PHYSICAL, samples=samples_xy(j["spp"]),
+                                max_bounces=j["depth"], iteration=it, seed=j["seed"])
+
+    t0 = time.time()
+    plain = [_batch_scene(dr, j) for j in jobs]
+    build_s = time.time() - t0
+    K = a.batch_steps
+
+    # scene-by-scene plain launches
+    rend = dr.Renderer(a.wave)
+
+    def plain_step(i):
+        for j, sc, cam, fb, nb in zip(jobs, plain, cams, fbs, nbs):
+            rend.render_blocks(sc, cam, fb, 0, nb, params(j, 2 + i))
+
+    for j, sc, cam, fb, nb in zip(jobs, plain, cams, fbs, nbs):
+        rend.render_blocks(sc, cam, fb, 0, nb, params(j, 1))
+    plain_ms = _events_ms(torch, plain_step, K)
+    plain_launches = rend.launches()
+    plain_means = np.array([fb[:, :3].double().mean().item() for fb in fbs])
+    rend.close()
+
+    # autotuning: leaf split threshold per size class, then wave size on a quarter of the jobs
+    t0 = time.time()
+    reps = autotune.representatives(jobs, n_tris)
+    best_split, split_table = autotune.tune_leaf_threshold(lambda i, c: _batch_scene(dr, jobs[i], c), reps,
+                                                           lambda i: cams[i], depth=jobs[0]["depth"], device=dev)
+    tuned = []
+    for i, j in enumerate(jobs):
+        c = best_split[autotune.size_class(n_tris[i])]
+        if c == 8:
+            tuned.append(plain[i])
+        else:
+            tuned.append(_batch_scene(dr, j, c))
+            plain[i].close()
+    plain = None
+    items = [(tuned[i], cams[i], params(j, 1), fbs[i], 0, nbs[i]) for i, j in enumerate(jobs)]
+    sub = dr.Batch(items[::4])
+    best_wave, wave_table, brend = autotune.tune_wave(sub)
+    sub.close()
+    tune_s = time.time() - t0
+
+    batch = dr.Batch(items)
+    batch.render(brend, use_graph=True)            # capture + warm-up (iteration 1)
+    l0 = brend.launches()
+
+    def batch_step(i):
+        batch.set_iteration(2 + i)
+        batch.render(brend, use_graph=True)
+
+    batch_ms = _events_ms(torch, batch_step, K)
+    batch_launches = brend.launches() - l0
+    batch_means = np.array([fb[:, :3].double().mean().item() for fb in fbs])
+    rel = np.abs(batch_means - plain_means) / np.maximum(np.abs(plain_means), 1e-9)
+    v_plain = paths * K / (plain_ms / 1e3) / 1e6
+    v_batch = paths * K / (batch_ms / 1e3) / 1e6
+    res = sorted({(j["width"], j["spp"]) for j in jobs})
+    out = {
+        "workload": f"{len(jobs)} scenes, {sum(n_tris):,} triangles (per scene {min(n_tris):,}-{max(n_tris):,}, "
+                    "displaced icosphere + random boxes + ground + emissive quad), square resolutions "
+                    "128-1024, spp 4/16/64, depth 6, seeds 0-63, pinhole",
+        "paths_per_step": int(paths), "steps": K,
+        "scene_by_scene_mpaths_s": round(v_plain, 3), "batched_mpaths_s": round(v_batch, 3),
+        "speedup": round(v_batch / v_plain, 3),
+        "scene_by_scene_ms_per_step": round(plain_ms / K, 1), "batched_ms_per_step": round(batch_ms / K, 1),
+        "batched_gpu_launches_per_step": int(batch_launches // max(1, K)), "graph": True,
+        "autotune": {"leaf_split_by_class": {str(autotune.SIZE_CLASSES[k]) if k < len(autotune.SIZE_CLASSES)
+                                             else "inf": v for k, v in sorted(best_split.items())},
+                     "leaf_probe_ms": {str(k): v for k, v in split_table.items()},
+                     "wave": best_wave, "wave_probe_ms": {str(k): v for k, v in wave_table.items()}},
+        "job_mean_max_rel_diff_batched_vs_plain": float(rel.max()),
+        "host_s": {"generate": round(gen_s, 1), "build": round(build_s, 1), "autotune": round(tune_s, 1)},
+        "resolution_spp_mix": [list(r) for r in res],
+    }
+    batch.close()
+    brend.close()
+    for sc in tuned:
+        sc.close()
+    return out
+
+
+def run_differentiable(dr, torch, dev, a):
+    """Forward render and path-replay adjoint of an L2 image loss w.r.t. per-triangle albedo and
+    emission: icosphere level 7 + box room (327,692 triangles), 512x512, 16 spp, depth 5; target
+    rendered from hidden albedo (seed 7).  Times forward and forward+adjoint steps and checks the
+    largest gradient components against central finite differences with common random numbers."""
+    from dumbray_gb300 import scenes
+
+    S = scenes.differentiable_scene(7)
+    n = len(S["tris"])
+    sc = dr.Scene(S["tris"], mat_id=S["mat_id"], materials=[dr.lambert()])
+    sc.set_triangle_params(S["albedo_target"], S["emission"], S["roughness"])
+    cam = dr.camera(dr.LENS_PINHOLE, position=(0.0, 0.0, -0.99), angle=60.0)
+    W = H = 512
+    p = dr.render_params(W, H, dr.MODE_PHYSICAL, samples=(4, 4), max_bounces=5, seed=7)
+    nb = dr.block_count(W, H)
+    rend = dr.Renderer(1 << 22)
+    target = dr.new_frame_buffer(W, H, dev)
+    rend.render_blocks(sc, cam, target, 0, nb, p)
+    a_ptr, e_ptr = sc.triangle_params_device()
+    alb = dr.device_view(a_ptr, (n, 3), dev)
+    emi = dr.device_view(e_ptr, (n, 3), dev)
+    alb.copy_(torch.from_numpy(S["albedo"]).to(dev))
+    img = dr.new_frame_buffer(W, H, dev)
+    dl = torch.zeros_like(img)
+    ga = torch.zeros((n, 3), dtype=torch.float32, device=dev)
+    ge = torch.zeros((n, 3), dtype=torch.float32, device=dev)
+
+    def fwd(i):
+        rend.render_blocks(sc, cam, img, 0, nb, p)
+
+    def fwd_adj(i):
+        rend.render_blocks(sc, cam, img, 0, nb, p)
+        torch.sub(img[:, :3], target[:, :3], out=dl[:, :3]).mul_(2.0)
+        ga.zero_()
+        ge.zero_()
+        rend.render_adjoint(sc, cam, dl, 0, nb, p, ga, ge)
+
+    K = max(3, a.steps)
+    for i in range(3):
+        fwd_adj(i)
+    fwd_ms = _events_ms(torch, fwd, K) / K
+    fa_ms = _events_ms(torch, fwd_adj, K) / K
+    paths = W * H * 16
+
+    def loss():
+        rend.render_blocks(sc, cam, img, 0, nb, p)
+        d = img[:, :3].double() - target[:, :3].double()
+        return float((d * d).sum())
+
+    ga_h, ge_h = ga.cpu().numpy(), ge.cpu().numpy()
+    errs = []
+    for f in np.argsort(-np.abs(ga_h).ravel())[:8]:
+        k, ch = divmod(int(f), 3)
+        x = float(S["albedo"][k, ch])
+        alb[k, ch] = x + 1e-3
+        lp = loss()
+        alb[k, ch] = x - 1e-3
+        lm = loss()
+        alb[k, ch] = x
+        fd = (lp - lm) / 2e-3
+        errs.append(("albedo", k, ch, float(ga_h[k, ch]), fd, abs(ga_h[k, ch] - fd) / max(abs(fd), 1e-12)))
+    em_ids = S["emissive_ids"]
+    for k in em_ids[np.argsort(-np.abs(ge_h[em_ids]).sum(1))[:4]]:
+        ch = int(np.argmax(np.abs(ge_h[k])))
+        x = float(S["emission"][k, ch])
+        emi[k, ch] = x + 1e-2
+        lp = loss()
+        emi[k, ch] = x - 1e-2
+        lm = loss()
+        emi[k, ch] = x
+        fd = (lp - lm) / 2e-2
+        errs.append(("emission", int(k), ch, float(ge_h[k, ch]), fd, abs(ge_h[k, ch] - fd) / max(abs(fd), 1e-12)))
+    rend.close()
+    sc.close()
+    worst = max(errs, key=lambda e: e[5])
+    return {
+        "workload": f"icosphere L7 + box room ({n:,} tris), per-triangle albedo U[0.1,0.9], emission 10 on 64 tris, "
+                    "512x512, 16 spp, depth 5, L2 loss vs target from hidden albedo (seed 7)",
+        "fwd_ms": round(fwd_ms, 3), "fwd_adj_ms": round(fa_ms, 3), "ratio": round(fa_ms / fwd_ms, 3),
+        "fwd_mpaths_s": round(paths / (fwd_ms / 1e3) / 1e6, 3),
+        "fwd_adj_mpaths_s": round(paths / (fa_ms / 1e3) / 1e6, 3),
+        "fd_check": {"method": "central differences, common random numbers, parameters written in place; "
+                               "h = 1e-3 (albedo), 1e-2 (emission 10)",
+                     "components": len(errs), "max_rel_err": float(max(e[5] for e in errs)),
+                     "worst": {"param": worst[0], "tri": worst[1], "channel": worst[2], "adjoint": worst[3],
+                               "fd": worst[4]}},
+    }
 
 
 def reference_twin(S, dr):

@@ -73,6 +73,7 @@ struct dr_scene {
     float *albedo_dev = nullptr;         // per-triangle albedo / emission read by the kernels
     float *emission_dev = nullptr;
     float *light_pdf_dev = nullptr;
+    int64_t node_f4 = 0, leaf_f4 = 0;    // float4 counts of the device node and leaf-triangle arrays
 
     ~dr_scene() {
         for (void *p : allocs) cudaFree(p);
@@ -322,6 +323,8 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
         delete sc;
         return cuda_fail(e, "dr_scene_create: upload");
     }
+    sc->node_f4 = (int64_t)nodes.size();
+    sc->leaf_f4 = (int64_t)leaf_tris.size();
     drd::Scene &S = sc->dev;
     S.nodes = d_nodes;
     S.leaf_tris = d_leaf;
@@ -724,6 +727,10 @@ struct dr_batch {
     // which cannot be captured.  The instantiated graph is launched on the caller's stream.
     cudaStream_t capture_stream = nullptr;
     cudaEvent_t done = nullptr;   // recorded after each render: the job table is in use until it fires
+    // One device arena holding the octrees of all the batch's scenes (node child / leaf indices
+    // rebased), so the traversal reads nodes and leaf triangles through one pointer for every ray.
+    float4 *arena_nodes = nullptr, *arena_leaf = nullptr;
+    int64_t arena_node_count = 0;
 
     void drop_graph() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -736,11 +743,56 @@ struct dr_batch {
         drop_graph();
         if (capture_stream) cudaStreamDestroy(capture_stream);
         if (done) cudaEventDestroy(done);
+        cudaFree(arena_nodes);
+        cudaFree(arena_leaf);
         cudaFree(items_dev);
     }
 };
 
 extern "C" {
+
+// Concatenates the octrees of the batch's distinct scenes into one device arena and points every
+// job's scene record at it: node groups and leaf records of scene k start after those of scenes
+// 0..k-1; triangle ids in the leaf records stay scene-local (a ray only visits its own scene's nodes).
+static dr_status build_arena(dr_batch *b) {
+    std::vector<const dr_scene *> uniq;
+    std::vector<int64_t> node_off, leaf_off;
+    int64_t nodes = 0, leaf = 0;
+    for (const dr_scene *sc : b->scenes) {
+        if (std::find(uniq.begin(), uniq.end(), sc) != uniq.end()) continue;
+        if ((sc->node_f4 / 2) % 8 != 0) return fail(DR_E_STATE, "dr_batch_create: octree nodes are not in groups of 8");
+        uniq.push_back(sc);
+        node_off.push_back(nodes / 2);
+        leaf_off.push_back(leaf / 3);
+        nodes += sc->node_f4;
+        leaf += sc->leaf_f4;
+    }
+    b->arena_node_count = nodes / 2;
+    if (b->arena_node_count >= (int64_t(1) << 27) || leaf / 3 >= (int64_t(1) << 31))
+        return fail(DR_E_CAPACITY, "dr_batch_create: the scenes' octrees exceed 2^27 nodes or 2^31 leaf references");
+    cudaError_t e = cudaMalloc((void **)&b->arena_nodes, sizeof(float4) * (size_t)std::max<int64_t>(nodes, 2));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->arena_leaf, sizeof(float4) * (size_t)std::max<int64_t>(leaf, 3));
+    for (size_t k = 0; k < uniq.size() && e == cudaSuccess; k++) {
+        const dr_scene *sc = uniq[k];
+        if (sc->leaf_f4)
+            e = cudaMemcpy(b->arena_leaf + 3 * leaf_off[k], sc->dev.leaf_tris, sizeof(float4) * (size_t)sc->leaf_f4,
+                           cudaMemcpyDeviceToDevice);
+        if (e == cudaSuccess && sc->node_f4)
+            e = drk::launch_rebase_nodes(b->arena_nodes + 2 * node_off[k], sc->dev.nodes, sc->node_f4 / 2, (int)(node_off[k] / 8),
+                                         (int)leaf_off[k], nullptr);
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "dr_batch_create: octree arena");
+    for (size_t i = 0; i < b->items.size(); i++) {
+        const size_t k = (size_t)(std::find(uniq.begin(), uniq.end(), b->scenes[i]) - uniq.begin());
+        drd::Scene &S = b->items[i].S;
+        S.nodes = b->arena_nodes;
+        S.leaf_tris = b->arena_leaf;
+        if (S.root_child >= 0) S.root_child += (int)(node_off[k] / 8);
+        S.root_leaf_first += (int)leaf_off[k];
+    }
+    return DR_OK;
+}
 
 dr_status dr_batch_create(const dr_batch_item *items, int32_t n, dr_batch **out) {
     if (!out) return fail(DR_E_ARG, "dr_batch_create: out is NULL");
@@ -779,6 +831,17 @@ dr_status dr_batch_create(const dr_batch_item *items, int32_t n, dr_batch **out)
     b->mode = items[0].params.mode;
     b->total_paths = path;
     b->total_slots = (int)slot;
+    for (int i = 1; i < n; i++) {
+        if (b->mode == DR_MODE_REFERENCE && b->items[i].clip != b->items[0].clip) {
+            delete b;
+            return fail(DR_E_ARG, "dr_batch_create: all jobs of a reference-mode batch must use the same backface culling");
+        }
+    }
+    dr_status ast = build_arena(b);
+    if (ast != DR_OK) {
+        delete b;
+        return ast;
+    }
     cudaError_t e = upload(&b->items_dev, b->items.data(), b->items.size());
     if (e != cudaSuccess) {
         delete b;
@@ -804,6 +867,8 @@ dr_status dr_batch_set_iteration(dr_batch *b, int32_t iteration) {
 
 dr_status dr_batch_render(dr_renderer *r, dr_batch *b, int32_t use_graph, void *stream_ptr) {
     if (!r || !b) return fail(DR_E_ARG, "dr_batch_render: NULL argument");
+    if (r->counting && b->arena_node_count >= (int64_t(1) << 24))
+        return fail(DR_E_CAPACITY, "dr_batch_render: traversal counting supports at most 2^24 octree nodes per batch");
     cudaStream_t stream = (cudaStream_t)stream_ptr;
     dr_status st = ensure_accum(r, (size_t)b->total_slots);
     if (st != DR_OK) return st;

@@ -53,7 +53,8 @@ struct Scene {
     const int *emissive;        // emissive triangle ids
     const float *emissive_cdf;  // inclusive prefix sums of power (at table build time)
     float root_lo[3], root_hi[3];
-    int root_child;             // 0 = root split (children are nodes 0..7), -1 = root is a leaf
+    int root_child;             // node group of the root's 8 children (0 for a standalone scene, the
+                                // scene's offset in a batch arena), -1 = the root is a leaf
     int root_leaf_first, root_leaf_count;
     int n_tris, n_mats, n_lights, n_emissive;
     float emissive_total;
@@ -203,6 +204,12 @@ __device__ __forceinline__ unsigned test_group(const float4 *nodes, int group, i
 // visits exactly the same leaves in the same order.  With COUNT, nbox receives the number of
 // child-box tests the reference's sequential scan performs (it stops scanning a group when a hit
 // is returned below it) plus the root test, and ntri the triangle tests.
+// Traversal stack entry: group << shift | (COUNT: child position taken << 8) | remaining hit mask.
+// The position is only needed to correct the box-test count, so the counting kernels keep 21 bits
+// of group index (2^24 nodes) and the others 24 (2^27 nodes, room for a batch arena).
+template <bool COUNT>
+__host__ __device__ constexpr int group_shift() { return COUNT ? 11 : 8; }
+
 template <bool COUNT>
 __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool clip, int ignore, Hit &h, int &nbox,
                                              int &ntri) {
@@ -215,10 +222,10 @@ __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool cl
     if (COUNT) nbox++;
     if (!slab_hit(S.root_lo[0], S.root_lo[1], S.root_lo[2], S.root_hi[0], S.root_hi[1], S.root_hi[2], o, inv)) return false;
     const int order = (d.z < 0 ? 1 : 0) + (d.y < 0 ? 2 : 0) + (d.x < 0 ? 4 : 0);
-    // stack entry: group << 11 | position taken << 8 | remaining hit mask (visit order)
+    constexpr int GS = group_shift<COUNT>();
     uint32_t stack[kStack];
     int sp = 0;
-    uint32_t cur = test_group(S.nodes, 0, order, o, inv);
+    uint32_t cur = ((uint32_t)S.root_child << GS) | test_group(S.nodes, S.root_child, order, o, inv);
     if (COUNT) nbox += 8;
     for (;;) {
         uint32_t m = cur & 0xFFu;
@@ -229,7 +236,7 @@ __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool cl
         }
         int k = __ffs(m) - 1;
         cur &= ~(1u << k);
-        int group = (int)(cur >> 11);
+        int group = (int)(cur >> GS);
         int node = group * 8 + (order ^ k);
         float4 lo = __ldg(S.nodes + 2 * (size_t)node), hi = __ldg(S.nodes + 2 * (size_t)node + 1);
         int w = __float_as_int(lo.w);
@@ -243,8 +250,8 @@ __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool cl
             }
         } else {
             if (sp >= kStack) return false;  // unreachable for trees of depth <= 24
-            stack[sp++] = (cur & ~(7u << 8)) | ((uint32_t)k << 8);
-            cur = ((uint32_t)(w >> 3) << 11) | test_group(S.nodes, w >> 3, order, o, inv);
+            stack[sp++] = COUNT ? ((cur & ~(7u << 8)) | ((uint32_t)k << 8)) : cur;
+            cur = ((uint32_t)(w >> 3) << GS) | test_group(S.nodes, w >> 3, order, o, inv);
             if (COUNT) nbox += 8;
         }
     }

@@ -770,6 +770,18 @@ __global__ void k_resolve(WaveArgs A, int total_slots) {
     }
 }
 
+// Arena copy of one scene's nodes: child node index += 8 * group_off, first leaf reference += leaf_off.
+__global__ void k_rebase_nodes(float4 *dst, const float4 *src, long long n_nodes, int group_off, int leaf_off) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_nodes; i += (long long)gridDim.x * blockDim.x) {
+        float4 lo = src[2 * i], hi = src[2 * i + 1];
+        int w = __float_as_int(lo.w);
+        w = (w >= 0) ? w + 8 * group_off : ~(~w + leaf_off);
+        lo.w = __int_as_float(w);
+        dst[2 * i] = lo;
+        dst[2 * i + 1] = hi;
+    }
+}
+
 }  // namespace drd
 
 // ---------------------------------------------------------------------------------------------
@@ -923,6 +935,14 @@ cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launc
     if (W.items) launch_wave_t<true>(W, A, stream, P, counters != nullptr, nl);
     else launch_wave_t<false>(W, A, stream, P, counters != nullptr, nl);
     if (launches) *launches += nl;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rebase_nodes(float4 *dst, const float4 *src, long long n_nodes, int group_off, int leaf_off,
+                                cudaStream_t stream) {
+    if (n_nodes <= 0) return cudaSuccess;
+    const int grid = (int)std::min<long long>((n_nodes + 255) / 256, (long long)sm_count() * 8);
+    drd::k_rebase_nodes<<<grid, 256, 0, stream>>>(dst, src, n_nodes, group_off, leaf_off);
     return cudaGetLastError();
 }
 

@@ -82,6 +82,10 @@ cudaError_t launch_cast(const drd::Scene &S, const float *o, const float *d, con
 // counters (nullable): 6 x u64 = {trace rays, trace box tests, trace tri tests, shadow casts, shadow box tests, shadow tri tests}
 cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launches, Profiler *prof,
                         unsigned long long *counters);
+// Copies `n_nodes` octree nodes (float4 pairs) into a batch arena at node group `group_off` (node
+// index 8 * group_off), adding the offsets to child node and first-leaf-reference indices.
+cudaError_t launch_rebase_nodes(float4 *dst, const float4 *src, long long n_nodes, int group_off, int leaf_off,
+                                cudaStream_t stream);
 // Frame-buffer resolve of all jobs: `total_slots` pixel slots of the shared accumulator.
 cudaError_t launch_resolve(const WaveDesc &W, int total_slots, cudaStream_t stream, long long *launches, Profiler *prof);
 

@@ -25,8 +25,6 @@ constexpr int kChunk = 256;
 enum : int { kIdle = 0, kTrav = 1, kLeaf = 2 };
 
 struct LaneRay {
-    const float4 *nodes;       // the ray's scene (per lane when several scenes share a wave)
-    const float4 *leaf;
     f3 o, d, inv;
     int order, ignore;
     uint32_t cur;
@@ -43,8 +41,6 @@ struct LaneRay {
 // Starts a ray: root leaf, root miss, or the root's children tested (Octree.impl.cuh:175-190).
 template <bool COUNT>
 __device__ __forceinline__ int lane_start(const Scene &S, LaneRay &L) {
-    L.nodes = S.nodes;
-    L.leaf = S.leaf_tris;
     L.inv = mkf3(__fdiv_rn(1.0f, L.d.x), __fdiv_rn(1.0f, L.d.y), __fdiv_rn(1.0f, L.d.z));
     L.order = (L.d.z < 0 ? 1 : 0) + (L.d.y < 0 ? 2 : 0) + (L.d.x < 0 ? 4 : 0);
     L.sp = 0;
@@ -64,7 +60,7 @@ __device__ __forceinline__ int lane_start(const Scene &S, LaneRay &L) {
     }
     if (COUNT) L.nb++;
     if (slab_hit(S.root_lo[0], S.root_lo[1], S.root_lo[2], S.root_hi[0], S.root_hi[1], S.root_hi[2], L.o, L.inv)) {
-        L.cur = test_group(S.nodes, 0, L.order, L.o, L.inv);
+        L.cur = ((uint32_t)S.root_child << group_shift<COUNT>()) | test_group(S.nodes, S.root_child, L.order, L.o, L.inv);
         if (COUNT) L.nb += 8;
     }
     return kTrav;
@@ -80,10 +76,12 @@ struct WarpLeafSlots {
 //   bool next(int &begin, int &end)           warp-uniform; false when no work is left
 //   void load(int i, f3 &o, f3 &d, int &ignore, int &job)
 //   const Scene &scene(int job)               the scene of a job (MULTI only)
-//   bool clip(int job)                        backface culling of a job
+//   bool clip(int job)                        backface culling of a job (MULTI = false: job 0 for all)
 //   void store(int i, const Hit &h, int nbox, int ntri)
-// MULTI = false: every ray belongs to scene `S` (uniform).  MULTI = true: rays of different scenes
-// share the warp; each lane keeps its scene's node and triangle pointers.
+// MULTI = false: every ray belongs to scene `S`.  MULTI = true: rays of different scenes share the
+// warp; their trees live in one batch arena (S.nodes / S.leaf_tris are the arena's), so a lane only
+// takes its scene's root (bounds, child group or root leaf) when it starts a ray.  Backface culling
+// is uniform over a wave in both cases.
 template <bool COUNT, bool MULTI, class Source>
 __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, uint32_t *stack, WarpLeafSlots &ws) {
     const unsigned lane = threadIdx.x & 31u;
@@ -92,10 +90,9 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
     bool drained = false;
     int cur_i = -1;
     int mode = kIdle;
-    bool clip = false;
+    constexpr int GS = group_shift<COUNT>();
+    const bool clip = src.clip(0);
     LaneRay L;
-    L.nodes = S.nodes;
-    L.leaf = S.leaf_tris;
     L.r = 0;
     L.r_end = 0;
     L.sp = 0;
@@ -115,7 +112,6 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
                     int ign, job;
                     src.load(cur_i, L.o, L.d, ign, job);
                     L.ignore = ign;
-                    clip = src.clip(job);
                     mode = lane_start<COUNT>(MULTI ? src.scene(job) : S, L);
                 }
                 c_next += min(avail, __popc(want));
@@ -138,9 +134,8 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
             } else {
                 int k = __ffs(m) - 1;
                 L.cur &= ~(1u << k);
-                int node = (int)(L.cur >> 11) * 8 + (L.order ^ k);
-                const float4 *nodes = MULTI ? L.nodes : S.nodes;
-                float4 lo = __ldg(nodes + 2 * (size_t)node), hi = __ldg(nodes + 2 * (size_t)node + 1);
+                int node = (int)(L.cur >> GS) * 8 + (L.order ^ k);
+                float4 lo = __ldg(S.nodes + 2 * (size_t)node), hi = __ldg(S.nodes + 2 * (size_t)node + 1);
                 int w = __float_as_int(lo.w);
                 if (w < 0) {
                     L.r = ~w;
@@ -152,8 +147,8 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
                     L.kleaf = k;
                     mode = kLeaf;
                 } else if (L.sp < kStack) {
-                    stack[L.sp++] = (L.cur & ~(7u << 8)) | ((uint32_t)k << 8);
-                    L.cur = ((uint32_t)(w >> 3) << 11) | test_group(nodes, w >> 3, L.order, L.o, L.inv);
+                    stack[L.sp++] = COUNT ? ((L.cur & ~(7u << 8)) | ((uint32_t)k << 8)) : L.cur;
+                    L.cur = ((uint32_t)(w >> 3) << GS) | test_group(S.nodes, w >> 3, L.order, L.o, L.inv);
                     if (COUNT) L.nb += 8;
                 } else {  // unreachable for depth <= 24: finish as a miss rather than overflow
                     L.cur = 0;
@@ -194,19 +189,13 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
             const int excl1 = ws.incl[own1] - __shfl_sync(0xFFFFFFFFu, pending, own1);
             const int r0 = __shfl_sync(0xFFFFFFFFu, L.r, own0), r1 = __shfl_sync(0xFFFFFFFFu, L.r, own1);
             const int pos0 = r0 + (t0 - excl0), pos1 = r1 + (t1 - excl1);
-            const float4 *leaf0 = S.leaf_tris, *leaf1 = S.leaf_tris;
-            if (MULTI) {
-                leaf0 = (const float4 *)__shfl_sync(0xFFFFFFFFu, (unsigned long long)L.leaf, own0);
-                leaf1 = (const float4 *)__shfl_sync(0xFFFFFFFFu, (unsigned long long)L.leaf, own1);
-            }
-            const bool clip0 = __shfl_sync(0xFFFFFFFFu, clip, own0), clip1 = __shfl_sync(0xFFFFFFFFu, clip, own1);
             float4 A0, B0, C0, A1, B1, C1;
             if (t0 < total) {
-                const float4 *lt = leaf0 + 3 * (size_t)pos0;
+                const float4 *lt = S.leaf_tris + 3 * (size_t)pos0;
                 A0 = __ldg(lt); B0 = __ldg(lt + 1); C0 = __ldg(lt + 2);
             }
             if (t1 < total) {
-                const float4 *lt = leaf1 + 3 * (size_t)pos1;
+                const float4 *lt = S.leaf_tris + 3 * (size_t)pos1;
                 A1 = __ldg(lt); B1 = __ldg(lt + 1); C1 = __ldg(lt + 2);
             }
 #pragma unroll
@@ -223,7 +212,7 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
                     float dist;
                     f3 hp;
                     if (tri_cast_better(f3of(A), f3of(B), f3of(C), __float_as_int(A.w), mkf3(ox, oy, oz), mkf3(dx, dy, dz),
-                                        q ? clip1 : clip0, ign, obest, dist, hp))
+                                        clip, ign, obest, dist, hp))
                         atomicMin(&ws.key[own], ((unsigned long long)__float_as_uint(dist) << 32) | (unsigned)(q ? pos1 : pos0));
                 }
             }
@@ -238,7 +227,7 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
                     const float dist = __uint_as_float((unsigned)(k >> 32));
                     const int pos = (int)(k & 0xFFFFFFFFull);
                     L.best = dist;
-                    L.bi = __float_as_int(__ldg((MULTI ? L.leaf : S.leaf_tris) + 3 * (size_t)pos).w);
+                    L.bi = __float_as_int(__ldg(S.leaf_tris + 3 * (size_t)pos).w);
                     L.bp = xadd(L.o, xmul(L.d, dist));
                 }
             }

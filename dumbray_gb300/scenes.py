@@ -258,13 +258,15 @@ def incoherent_rays(n: int, lo, hi, seed: int = 0):
     return o.astype(np.float32), d.astype(np.float32)
 
 
-def random_boxes(n: int, rng, lo=-1.6, hi=1.6, size=(0.02, 0.25)) -> np.ndarray:
+def random_boxes(n: int, rng, lo=-1.6, hi=1.6, fill=0.25) -> np.ndarray:
     """``n`` closed axis-aligned boxes (12 triangles each, outward normals), centres uniform in
-    [lo, hi]^3 and edge lengths uniform in ``size``."""
+    [lo, hi]^3, edge lengths uniform in [0.5 e, 1.5 e] with e chosen so that the boxes' summed
+    volume is ``fill`` of the region's (the box density stays the same whatever ``n`` is)."""
     if n <= 0:
         return np.zeros((0, 3, 3), np.float32)
     unit = box((1.0, 1.0, 1.0)).astype(np.float64)              # [12, 3, 3]
-    ext = rng.uniform(size[0], size[1], size=(n, 1, 1, 3))
+    e = (fill * (hi - lo) ** 3 / n) ** (1.0 / 3.0)
+    ext = rng.uniform(0.5 * e, 1.5 * e, size=(n, 1, 1, 3))
     ctr = rng.uniform(lo, hi, size=(n, 1, 1, 3))
     return (unit[None] * ext + ctr).reshape(-1, 3, 3).astype(np.float32)
 
@@ -293,7 +295,8 @@ def batch_workload(n_scenes: int = 64, seed: int = 0, min_tris: int = 1000, max_
 
     Scene i: target triangle count T log-uniform in [min_tris, max_tris]; the largest displaced
     icosphere (3-octave value noise, amplitude 0.1) with at most T triangles, randomly rotated and
-    scaled to radius U[0.5, 0.9], plus ceil((T - icosphere) / 12) random boxes around it, a 2-triangle
+    scaled to radius U[0.5, 0.9], plus ceil((T - icosphere) / 12) random boxes around it (summed box
+    volume a quarter of the [-1.6, 1.6]^3 region, whatever their number), a 2-triangle
     ground plane and one emissive quad (radiance 10) above; materials by triangle-index hash as in
     ``full_scene``.  Resolution square, uniform from ``resolutions``; spp uniform from ``spps``;
     render seed i.  Returns a list of dicts (tris, mat_id, albedo, roughness, emission, width,

@@ -113,3 +113,38 @@ def test_batch_rejects_mixed_modes(cuda):
     p = dr.render_params(16, 16, dr.MODE_REFERENCE)
     with pytest.raises(dr.DumbRayError):
         dr.Batch([tuple(jobs[0]), (sc, cam, p, dr.new_frame_buffer(16, 16, cuda), 0, 2)])
+
+
+def test_batch_arena_root_leaf_and_shared_scene(cuda):
+    """A scene whose octree is a single root leaf (no nodes) and one scene used by two jobs (stored
+    once in the batch's octree arena) render as they do alone."""
+    jobs = _phys_jobs(cuda)[:2]
+    small = np.concatenate([scenes.quad((0.0, 0.0, 0.5), (1.5, 1.5), (0.0, 0.0, -1.0)),
+                            scenes.quad((0.0, 0.9, 0.0), (0.4, 0.4), (0.0, -1.0, 0.0))])
+    sc = dr.Scene(small, materials=[dr.lambert()])
+    em = np.zeros((4, 3), np.float32)
+    em[2:] = 5.0
+    sc.set_triangle_params(np.full((4, 3), 0.6, np.float32), em, np.full(4, 0.2, np.float32))
+    assert sc.stats()["nodes"] <= 1
+    cam = dr.camera(dr.LENS_PINHOLE, position=(0.0, 0.0, -1.0), angle=60.0)
+    p = dr.render_params(16, 16, dr.MODE_PHYSICAL, samples=(2, 2), max_bounces=3, seed=4)
+    jobs.append([sc, cam, p, dr.new_frame_buffer(16, 16, cuda), 0, dr.block_count(16, 16)])
+    shared = jobs[1]
+    p2 = dr.render_params(shared[2].width, shared[2].height, dr.MODE_PHYSICAL, samples=(1, 2), max_bounces=2, seed=9)
+    jobs.append([shared[0], shared[1], p2, dr.new_frame_buffer(p2.width, p2.height, cuda), 0,
+                 dr.block_count(p2.width, p2.height)])
+    batch = dr.Batch([tuple(j) for j in jobs])
+    batch.render(dr.Renderer(1 << 12), use_graph=True)
+    torch.cuda.synchronize()
+    for j in jobs:
+        _close(j[3], _render_alone(j, cuda))
+
+
+def test_reference_batch_rejects_mixed_culling(cuda):
+    room = scenes.box((2, 2, 2), inward=True)
+    sc = dr.Scene(room, materials=[dr.dumb_based()], lights=[dr.spherical_light((1, 1, 1), (0, 0.5, 0), 0.1)])
+    cam = dr.camera(dr.LENS_SIMPLE_STOCHASTIC, position=(0.0, 0.0, -0.9))
+    a = dr.render_params(16, 16, dr.MODE_REFERENCE, cull_backfaces=True)
+    b = dr.render_params(16, 16, dr.MODE_REFERENCE, cull_backfaces=False)
+    with pytest.raises(dr.DumbRayError):
+        dr.Batch([(sc, cam, a, dr.new_frame_buffer(16, 16, cuda), 0, 2), (sc, cam, b, dr.new_frame_buffer(16, 16, cuda), 0, 2)])
