@@ -60,6 +60,13 @@ def parse():
     ap.add_argument("--no-count", action="store_true", help="skip the traversal-counting pass (profiling cases)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable (adjoint) leg")
+    ap.add_argument("--no-raycast", action="store_true", help="skip the ray-cast microbenchmark leg")
+    ap.add_argument("--split", type=int, default=12,
+                    help="octree leaf split threshold of the path-trace scene (12: best of 8/12/16/24 on this "
+                         "workload with the physical-mode padding; the reference uses 8)")
+    ap.add_argument("--ref-tree", action="store_true",
+                    help="build the path-trace scene with the reference's octree padding (1.28e-3) instead of the "
+                         "physical-mode padding scaled to the coordinates")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=2, help="timed steps of each batched arm")
     return ap.parse_args()
@@ -79,12 +86,15 @@ def samples_xy(spp):
     return sx, spp // sx
 
 
-def build_scene(dr, level):
+def build_scene(dr, level, split=0, ref_tree=False):
     from dumbray_gb300 import scenes
     S = scenes.full_scene(level=level, seed=1)
     mats = [dr.lambert(), dr.mirror(), dr.glossy()]
     t0 = time.time()
-    scene = dr.Scene(S["tris"], mat_id=S["mat_id"], materials=mats)
+    S["box_epsilon"] = 0.0 if ref_tree else dr.tight_box_epsilon(S["tris"])
+    S["split"] = split if split > 0 else 8
+    scene = dr.Scene(S["tris"], mat_id=S["mat_id"], materials=mats, split_threshold=S["split"],
+                     box_epsilon=0.0 if ref_tree else dr.PHYSICAL_TREE)
     scene.set_triangle_params(S["albedo"], S["emission"], S["roughness"])
     return S, scene, time.time() - t0
 
@@ -202,7 +212,7 @@ def run_ours(a):
     if world > 1:
         import torch.distributed as tdist
         tdist.init_process_group("nccl")
-    S, scene, build_s = build_scene(dr, a.level)
+    S, scene, build_s = build_scene(dr, a.level, a.split, a.ref_tree)
     cam = make_camera(dr, a.lens)
     W, H = a.width, a.height
     sx, sy = samples_xy(a.spp)
@@ -302,7 +312,10 @@ def run_ours(a):
                    "triangles": int(len(S["tris"])), "width": W, "height": H, "spp": a.spp, "depth": a.depth,
                    "lens": a.lens, "mode": "physical", "wave_paths": a.wave, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (scene ~0.3 GB, wavefront queues ~2 GB), no flush",
-                   "scene_build_s": round(build_s, 2)},
+                   "scene_build_s": round(build_s, 2),
+                   "octree": {"split_threshold": S["split"], "box_epsilon": S["box_epsilon"] or 1.28e-3,
+                              "rule": "reference split rule; " + ("reference padding" if a.ref_tree else
+                                      "physical-mode padding 2^-18 x max |coordinate|")}},
         "e2e": {"value": None if e2e is None else round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": fb_bytes, "d2h_bytes_per_step": fb_bytes},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -354,6 +367,8 @@ def run_ours(a):
             "mean_diff_in_se": float(diff.mean() / max(diff.std(ddof=1) / np.sqrt(len(diff)), 1e-12)),
             "sample": "centre patch 12,288 px x 64 spp, same seeds"}
     del rend
+    if rank == 0 and world == 1 and not a.no_raycast:
+        out["raycast"] = run_raycast(dr, torch, dev, a, peak, peak_src)
     if rank == 0 and world == 1 and not a.no_batched:
         out["batched"] = run_batched(dr, torch, dev, a)
     if rank == 0 and world == 1 and not a.no_adjoint:
@@ -366,7 +381,7 @@ def run_ours(a):
 
 def _batch_scene(dr, job, split=0):
     sc = dr.Scene(job["tris"], mat_id=job["mat_id"], materials=[dr.lambert(), dr.mirror(), dr.glossy()],
-                  split_threshold=split)
+                  split_threshold=split, box_epsilon=dr.PHYSICAL_TREE)
     sc.set_triangle_params(job["albedo"], job["emission"], job["roughness"])
     return sc
 
@@ -382,10 +397,60 @@ def _events_ms(torch, fn, steps):
     return e0.elapsed_time(e1)
 
 
+def run_raycast(dr, torch, dev, a, peak, peak_src):
+    """Closest-hit ray casting through dr_cast on the displaced icosphere alone (level 8, 1,310,720
+    triangles, amplitude 0.1, seed 1): 1920x1080 coherent pinhole primary rays (60 degrees, from
+    (0, 0.3, -3) toward the origin) and 8M incoherent rays (origins uniform in [-1.1, 1.1]^3,
+    directions uniform on the sphere, seed 0), each timed over K casts of the whole set with CUDA
+    events, on the reference's octree and on the physical-mode one.  Roofline: algorithmic bytes =
+    rays x (40 + 32 C_box + 36 C_tri) with the mean box and triangle tests per ray counted by
+    dr_cast_counted, divided by the kernel time."""
+    from dumbray_gb300 import scenes
+
+    mesh = scenes.displaced_icosphere(a.level, 0.1, 1)
+    out = {"workload": f"displaced icosphere L{a.level} alone ({len(mesh):,} tris), closest hit, backface culling; "
+                       "reference_tree = the reference's octree (casts bit-exact to Octree::cast), physical_tree = "
+                       "padding 2^-18 x max |coordinate| (same closest hits up to exact ties)"}
+    sets = {"primary_1080p": scenes.primary_rays(1920, 1080, 60.0, (0.0, 0.3, -3.0), (0.0, 0.0, 0.0)),
+            "incoherent_8M": scenes.incoherent_rays(8 * 1024 * 1024, -1.1, 1.1, seed=0)}
+    K = max(3, a.steps)
+    hits = {}
+    for tree, eps in (("reference_tree", 0.0), ("physical_tree", dr.PHYSICAL_TREE)):
+        sc = dr.Scene(mesh, materials=[dr.lambert()], box_epsilon=eps)
+        st = sc.stats()
+        res = {"octree": {"nodes": st["nodes"], "leaf_refs": st["refs"], "refs_per_tri": round(st["refs"] / len(mesh), 2)}}
+        hits[tree] = {}
+        for name, (o, d) in sets.items():
+            ot = torch.from_numpy(o).to(dev)
+            dt = torch.from_numpy(d).to(dev)
+            n = len(o)
+            for _ in range(3):
+                dr.cast(sc, ot, dt)
+            ms = _events_ms(torch, lambda i: dr.cast(sc, ot, dt), K) / K
+            tri, t, nb, nt = dr.cast(sc, ot, dt, counted=True)
+            c_box = float(nb.double().mean())
+            c_tri = float(nt.double().mean())
+            bpr = 40.0 + 32.0 * c_box + 36.0 * c_tri
+            achieved = n * bpr / (ms / 1e3) / 1e9
+            res[name] = {"rays": n, "ms": round(ms, 3), "mrays_s": round(n / (ms / 1e3) / 1e6, 1),
+                         "hit_fraction": round(float((tri >= 0).float().mean()), 4), "c_box": round(c_box, 2),
+                         "c_tri": round(c_tri, 2), "bytes_per_ray": round(bpr, 1),
+                         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                                      "frac": round(achieved / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
+                                      "kernel": "k_cast"}}
+            hits[tree][name] = tri.cpu().numpy()
+            del ot, dt
+        out[tree] = res
+        sc.close()
+    out["physical_vs_reference_tree_hit_mismatch"] = {
+        k: float(np.mean(hits["reference_tree"][k] != hits["physical_tree"][k])) for k in sets}
+    return out
+
+
 def run_batched(dr, torch, dev, a):
-    """64 independent scenes rendered scene by scene (plain dr_render_blocks launches, reference
-    octree parameters) and as one batch (shared waves, one CUDA graph, autotuned leaf sizes and wave
-    size).  Both arms render progressive iterations 1..K+1 of every job into the same frame buffers;
+    """64 independent scenes rendered scene by scene (plain dr_render_blocks launches, library default
+    leaf split 8) and as one batch (shared waves, one CUDA graph, autotuned leaf split and wave
+    size); both with the physical-mode octree padding.  Both arms render progressive iterations 1..K+1 of every job into the same frame buffers;
     Mpaths/s = all paths of the K timed iterations / CUDA-event time."""
     from dumbray_gb300 import autotune, scenes
 
@@ -489,7 +554,7 @@ def run_differentiable(dr, torch, dev, a):
 
     S = scenes.differentiable_scene(7)
     n = len(S["tris"])
-    sc = dr.Scene(S["tris"], mat_id=S["mat_id"], materials=[dr.lambert()])
+    sc = dr.Scene(S["tris"], mat_id=S["mat_id"], materials=[dr.lambert()], box_epsilon=dr.PHYSICAL_TREE)
     sc.set_triangle_params(S["albedo_target"], S["emission"], S["roughness"])
     cam = dr.camera(dr.LENS_PINHOLE, position=(0.0, 0.0, -0.99), angle=60.0)
     W = H = 512

@@ -30,6 +30,7 @@ MAT_DUMB_BASED, MAT_SIMPLE_STOCHASTIC, MAT_LAMBERT, MAT_MIRROR, MAT_GLOSSY = ran
 LIGHT_SPHERICAL, LIGHT_SOFT_DIRECTIONAL, LIGHT_DIRECTIONAL = range(3)
 LENS_DEFAULT_PERSPECTIVE, LENS_SIMPLE_STOCHASTIC, LENS_SPHERICAL_SEGMENT, LENS_PINHOLE, LENS_FISHEYE, LENS_SPHERICAL = range(6)
 MODE_REFERENCE, MODE_PHYSICAL = 0, 1
+PHYSICAL_TREE = -1.0   # Scene(box_epsilon=...): octree padding scaled to the scene (physical-mode scenes)
 BOXING_HEIGHT, BOXING_WIDTH, BOXING_MIN, BOXING_MAX = range(4)
 BLOCK_W, BLOCK_H = 8, 16
 BLOCK_SIZE = BLOCK_W * BLOCK_H
@@ -39,7 +40,7 @@ _F3 = ctypes.c_float * 3
 
 class DrBuildParams(ctypes.Structure):
     _fields_ = [("max_depth", ctypes.c_int32), ("split_threshold", ctypes.c_int32), ("threads", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("box_epsilon", ctypes.c_float)]
 
 
 class DrMaterial(ctypes.Structure):
@@ -290,10 +291,16 @@ def _stream_ptr(stream) -> int:
 
 
 class Scene:
-    """Triangles + materials + lights, octree built on the host and uploaded once (immutable)."""
+    """Triangles + materials + lights, octree built on the host and uploaded once (immutable).
+
+    ``max_depth`` / ``split_threshold`` / ``box_epsilon`` = 0 build the reference's octree
+    (depth 24, 8 triangles per leaf, 1.28e-3 box padding): casts and traversal counts then match the
+    reference's.  ``box_epsilon=PHYSICAL_TREE`` (any negative value) pads boxes by 2^-18 x the largest
+    absolute coordinate instead, for scenes rendered in the physical mode only: the same closest hits
+    up to exact ties, with far fewer duplicated leaf references on finely tessellated meshes."""
 
     def __init__(self, tris, normals=None, mat_id=None, materials=(), lights=(), max_depth=0, split_threshold=0,
-                 threads=0):
+                 threads=0, box_epsilon=0.0):
         L = lib()
         self.tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 3, 3)
         self.n = len(self.tris)
@@ -304,7 +311,7 @@ class Scene:
         self.materials, self.lights = mats, lts
         marr = (DrMaterial * max(1, len(mats)))(*mats)
         larr = (DrLight * max(1, len(lts)))(*lts)
-        bp = DrBuildParams(max_depth, split_threshold, threads, 0)
+        bp = DrBuildParams(max_depth, split_threshold, threads, box_epsilon)
         h = ctypes.c_void_p()
         check(L.dr_scene_create(self.tris.ctypes.data, None if self._nrm is None else self._nrm.ctypes.data,
                                 None if self._mat is None else self._mat.ctypes.data, self.n,
@@ -356,12 +363,21 @@ class Scene:
             pass
 
 
-def build_octree_host(tris, max_depth=0, split_threshold=0, threads=0):
+def tight_box_epsilon(tris) -> float:
+    """Octree box padding scaled to the scene: 2^-18 x the largest absolute coordinate (what
+    ``box_epsilon=PHYSICAL_TREE`` selects).  The leaf-box acceptance test of the traversal must
+    tolerate the float rounding of hit points (a few units of 2^-24 x the larger of |origin| and
+    |hit point|), so this keeps a margin of 2^5 for ray origins up to 2x the scene's extent."""
+    m = float(np.max(np.abs(np.asarray(tris, dtype=np.float32)))) if len(tris) else 1.0
+    return max(m, 1e-30) * 2.0 ** -18
+
+
+def build_octree_host(tris, max_depth=0, split_threshold=0, threads=0, box_epsilon=0.0):
     """Host-only octree build (dr_octree_create_host); returns (stats, box, child, leaf, refs) with
     node 0 = root, as dr_scene_export_tree."""
     L = lib()
     t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 3, 3)
-    bp = DrBuildParams(max_depth, split_threshold, threads, 0)
+    bp = DrBuildParams(max_depth, split_threshold, threads, box_epsilon)
     h = ctypes.c_void_p()
     check(L.dr_octree_create_host(t.ctypes.data, len(t), ctypes.byref(bp), ctypes.byref(h)))
     try:

@@ -236,6 +236,7 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
         if (bp->max_depth > 0) opt.max_depth = std::min(bp->max_depth, drd::kMaxDepth);
         if (bp->split_threshold > 0) opt.split_threshold = bp->split_threshold;
         opt.threads = bp->threads;
+        opt.box_eps = bp->box_epsilon;
     }
     if (!drb::build_octree(sc->xyz.data(), n, opt, sc->tree)) {
         delete sc;
@@ -423,6 +424,7 @@ dr_status dr_octree_create_host(const float *xyz, int32_t n, const dr_build_para
         if (bp->max_depth > 0) opt.max_depth = std::min(bp->max_depth, drd::kMaxDepth);
         if (bp->split_threshold > 0) opt.split_threshold = bp->split_threshold;
         opt.threads = bp->threads;
+        opt.box_eps = bp->box_epsilon;
     }
     if (!drb::build_octree(xyz, n, opt, t->tree)) {
         delete t;

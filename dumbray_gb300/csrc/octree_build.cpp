@@ -176,8 +176,7 @@ Bx clipped_bounds(const Bx &b, const T3 &t) {
 
 // The 8 overlapping octants around `c` (splitAABB, Octree.impl.cuh:423-434); child index
 // bit 2 = upper x, bit 1 = upper y, bit 0 = upper z.
-void octants(const Bx &b, P3 c, Bx *r) {
-    const float E = kBoxEps;
+void octants(const Bx &b, P3 c, Bx *r, float E) {
     for (int i = 0; i < 8; i++) {
         P3 lo, hi;
         lo.x = (i & 4) ? c.x - E : b.lo.x;
@@ -192,9 +191,9 @@ void octants(const Bx &b, P3 c, Bx *r) {
 
 // Shrink a node box to `lo..hi` padded by the octree epsilon, clamped to the old box
 // (reduceNode tail, Octree.impl.cuh:526-532).
-Bx shrink(const Bx &old, P3 lo, P3 hi) {
-    lo = sub(lo, mk(kBoxEps, kBoxEps, kBoxEps));
-    hi = add(hi, mk(kBoxEps, kBoxEps, kBoxEps));
+Bx shrink(const Bx &old, P3 lo, P3 hi, float E) {
+    lo = sub(lo, mk(E, E, E));
+    hi = add(hi, mk(E, E, E));
     lo = mk(std::fmax(lo.x, old.lo.x), std::fmax(lo.y, old.lo.y), std::fmax(lo.z, old.lo.z));
     hi = mk(std::fmin(hi.x, old.hi.x), std::fmin(hi.y, old.hi.y), std::fmin(hi.z, old.hi.z));
     return fixed_box(lo, hi);
@@ -226,6 +225,12 @@ bool build_octree(const float *xyz, int64_t n, const BuildOptions &opt, FlatOctr
     const int threads = opt.threads > 0 ? opt.threads : (int)std::max(1u, std::thread::hardware_concurrency());
     const int max_depth = opt.max_depth > 0 ? opt.max_depth : 24;
     const int split_n = opt.split_threshold > 0 ? opt.split_threshold : 8;
+    float E = opt.box_eps > 0.0f ? opt.box_eps : kBoxEps;
+    if (opt.box_eps < 0.0f) {  // scaled to the scene: 2^-18 x the largest absolute coordinate
+        float m = 0.0f;
+        for (int64_t i = 0; i < 9 * n; i++) m = std::fmax(m, std::fabs(xyz[i]));
+        E = std::fmax(m, 1e-30f) * (1.0f / 262144.0f);
+    }
     auto tri = [&](int32_t i) {
         const float *p = xyz + 9 * (int64_t)i;
         return T3{mk(p[0], p[1], p[2]), mk(p[3], p[4], p[5]), mk(p[6], p[7], p[8])};
@@ -243,7 +248,7 @@ bool build_octree(const float *xyz, int64_t n, const BuildOptions &opt, FlatOctr
         Bx b = fixed_box(lo, hi);
         if (i == 0) root = b;
         else {
-            P3 bl = sub(b.lo, mk(kBoxEps, kBoxEps, kBoxEps)), bh = add(b.hi, mk(kBoxEps, kBoxEps, kBoxEps));
+            P3 bl = sub(b.lo, mk(E, E, E)), bh = add(b.hi, mk(E, E, E));
             root = fixed_box(mk(std::fmin(root.lo.x, bl.x), std::fmin(root.lo.y, bl.y), std::fmin(root.lo.z, bl.z)),
                              mk(std::fmax(root.hi.x, bh.x), std::fmax(root.hi.y, bh.y), std::fmax(root.hi.z, bh.z)));
         }
@@ -306,7 +311,7 @@ bool build_octree(const float *xyz, int64_t n, const BuildOptions &opt, FlatOctr
                 for (int64_t r = level[k].ref_begin; r < level[k].ref_end; r++) c = add(c, centre[r]);
                 c = divs(c, (float)(level[k].ref_end - level[k].ref_begin));
                 split_at[k] = c;
-                octants(level[k].box, c, sub[k].data());
+                octants(level[k].box, c, sub[k].data(), E);
             }
         });
         std::vector<P3>().swap(centre);
@@ -355,7 +360,7 @@ bool build_octree(const float *xyz, int64_t n, const BuildOptions &opt, FlatOctr
                     lo = mk(std::fmin(lo.x, ob.lo.x), std::fmin(lo.y, ob.lo.y), std::fmin(lo.z, ob.lo.z));
                     hi = mk(std::fmax(hi.x, ob.hi.x), std::fmax(hi.y, ob.hi.y), std::fmax(hi.z, ob.hi.z));
                 }
-                leaf_box[k] = shrink(level[k].box, lo, hi);
+                leaf_box[k] = shrink(level[k].box, lo, hi, E);
             }
         });
         // (6) allocate the next level: children of splitting nodes, 8 consecutive, BFS order
@@ -428,7 +433,7 @@ bool build_octree(const float *xyz, int64_t n, const BuildOptions &opt, FlatOctr
             lo = mk(std::fmin(lo.x, cb.lo.x), std::fmin(lo.y, cb.lo.y), std::fmin(lo.z, cb.lo.z));
             hi = mk(std::fmax(hi.x, cb.hi.x), std::fmax(hi.y, cb.hi.y), std::fmax(hi.z, cb.hi.z));
         }
-        boxes[i] = shrink(boxes[i], lo, hi);
+        boxes[i] = shrink(boxes[i], lo, hi, E);
     }
     if (root_child >= 0) {
         P3 lo = root_box.hi, hi = root_box.lo;
@@ -437,7 +442,7 @@ bool build_octree(const float *xyz, int64_t n, const BuildOptions &opt, FlatOctr
             lo = mk(std::fmin(lo.x, cb.lo.x), std::fmin(lo.y, cb.lo.y), std::fmin(lo.z, cb.lo.z));
             hi = mk(std::fmax(hi.x, cb.hi.x), std::fmax(hi.y, cb.hi.y), std::fmax(hi.z, cb.hi.z));
         }
-        root_box = shrink(root_box, lo, hi);
+        root_box = shrink(root_box, lo, hi, E);
     }
 
     out.node_count = nn;

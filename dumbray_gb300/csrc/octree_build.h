@@ -9,6 +9,11 @@ struct BuildOptions {
     int max_depth = 24;        // OCTREE_MAX_DEPTH (Octree.cuh:13)
     int split_threshold = 8;   // OCTREE_POLYCOUNT_TO_SPLIT_NODE (Octree.cuh:11)
     int threads = 0;           // 0 = all host cores
+    // Padding of octant and leaf boxes: 0 = OCTREE_AABB_EPSILON (Octree.impl.cuh:3-5, 1.28e-3),
+    // which casts and traversal counts of the reference require; > 0 = that absolute value;
+    // < 0 = 2^-18 x the largest absolute coordinate.  The closest hit does not depend on it (up to
+    // exact ties), so physical-mode scenes may use a value scaled to the coordinates.
+    float box_eps = 0.0f;
 };
 
 // Flattened octree.  The root is stored separately; the children of an inner node are 8

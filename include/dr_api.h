@@ -38,13 +38,20 @@ typedef struct dr_scene dr_scene;
 typedef struct dr_renderer dr_renderer;
 
 /* ---- octree build parameters -------------------------------------------------------------
- * Octree.cuh:10-13: OCTREE_MAX_DEPTH 24, OCTREE_POLYCOUNT_TO_SPLIT_NODE 8.  Zero fields take
- * those defaults; threads = 0 uses every host core. */
+ * Octree.cuh:10-13: OCTREE_MAX_DEPTH 24, OCTREE_POLYCOUNT_TO_SPLIT_NODE 8; Octree.impl.cuh:3-5:
+ * OCTREE_AABB_EPSILON 1.28e-3 (box_epsilon, the padding of octant and leaf boxes).  Zero fields
+ * take those defaults; threads = 0 uses every host core.  The reference's values reproduce its
+ * tree exactly (casts and per-ray box / triangle test counts).  The closest hit itself does not
+ * depend on the tree up to exact ties, so a scene rendered only in the physical mode may take a
+ * box_epsilon scaled to its coordinates (an absolute 1.28e-3 is a large fraction of the leaf cells
+ * of a finely tessellated unit-size mesh, which duplicates triangles into many leaves):
+ * box_epsilon > 0 is used as given, box_epsilon < 0 selects 2^-18 x the largest absolute vertex
+ * coordinate (margin for the rounding of hit points in the leaf-box acceptance test). */
 typedef struct {
     int32_t max_depth;
     int32_t split_threshold;
     int32_t threads;
-    int32_t reserved;
+    float box_epsilon;
 } dr_build_params;
 
 /* ---- materials --------------------------------------------------------------------------

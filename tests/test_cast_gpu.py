@@ -56,6 +56,26 @@ def test_cast_matches_oracle_incoherent_and_primary(cuda, level, seed):
         _assert_same(idx, t, oi, ot)
 
 
+@pytest.mark.parametrize("level,seed", [(5, 2), (6, 3)])
+def test_physical_tree_casts_match_reference_tree(cuda, level, seed):
+    """The physical-mode octree (box padding scaled to the scene) returns the same closest hits as
+    the reference's tree: index and t bit-exact except exact distance ties (budget 1e-5 of rays)."""
+    tris = np.concatenate([scenes.displaced_icosphere(level, 0.1, seed), scenes.box((3, 3, 3), inward=True)])
+    a = dr.Scene(tris)
+    b = dr.Scene(tris, box_epsilon=dr.PHYSICAL_TREE)
+    assert b.stats()["refs"] < a.stats()["refs"]
+    o1, d1 = scenes.incoherent_rays(60000, -1.3, 1.3, seed=seed)
+    o2, d2 = scenes.primary_rays(128, 96, 50.0, (0.2, 0.5, -2.8), (0.0, 0.0, 0.0))
+    o, d = np.concatenate([o1, o2]), np.concatenate([d1, d2])
+    for cull in (True, False):
+        ia, ta = _gpu_cast(a, o, d, cuda, cull=cull)
+        ib, tb = _gpu_cast(b, o, d, cuda, cull=cull)
+        diff = ia != ib
+        assert diff.sum() <= max(1, int(1e-5 * len(o))), int(diff.sum())
+        same = ~diff & (ia >= 0)
+        assert np.array_equal(ta[same].view(np.int32), tb[same].view(np.int32))
+
+
 def test_cast_counters_equal_reference_traversal(cuda):
     """Box tests follow the reference's sequential child scan (it stops at the returning child);
     triangle tests are identical.  These are the C_box / C_tri of the bytes-per-ray formula."""
