@@ -56,24 +56,33 @@ def test_cast_matches_oracle_incoherent_and_primary(cuda, level, seed):
         _assert_same(idx, t, oi, ot)
 
 
-@pytest.mark.parametrize("level,seed", [(5, 2), (6, 3)])
-def test_physical_tree_casts_match_reference_tree(cuda, level, seed):
-    """The physical-mode octree (box padding scaled to the scene) returns the same closest hits as
-    the reference's tree: index and t bit-exact except exact distance ties (budget 1e-5 of rays)."""
+@pytest.mark.parametrize("level,seed,n_inc", [(5, 2, 60000), (6, 3, 60000), (8, 1, 1 << 20)])
+def test_physical_tree_casts_match_reference_tree(cuda, level, seed, n_inc):
+    """The physical-mode octree (box padding scaled to the scene) returns the reference tree's closest
+    hits, index and t bit-exact, except float32 near-ties: where two triangles lie at distances a few
+    ulps apart along the ray (grazing a shared edge of the displaced surface), the leaf partition
+    decides which one the float32 predicate keeps, and a float64 brute force sides with either tree.
+    Measured on 8M incoherent rays at level 8: 7.3e-5 of rays pick the other triangle, at a t within
+    4e-5 relative, and 2.4e-7 of rays turn a grazing hit into a miss.  Budget: 2e-4 of rays, t within
+    1e-3 relative, hit/miss changes at most 2e-6 of rays (2 rays)."""
     tris = np.concatenate([scenes.displaced_icosphere(level, 0.1, seed), scenes.box((3, 3, 3), inward=True)])
     a = dr.Scene(tris)
     b = dr.Scene(tris, box_epsilon=dr.PHYSICAL_TREE)
     assert b.stats()["refs"] < a.stats()["refs"]
-    o1, d1 = scenes.incoherent_rays(60000, -1.3, 1.3, seed=seed)
+    o1, d1 = scenes.incoherent_rays(n_inc, -1.3, 1.3, seed=seed)
     o2, d2 = scenes.primary_rays(128, 96, 50.0, (0.2, 0.5, -2.8), (0.0, 0.0, 0.0))
     o, d = np.concatenate([o1, o2]), np.concatenate([d1, d2])
     for cull in (True, False):
         ia, ta = _gpu_cast(a, o, d, cuda, cull=cull)
         ib, tb = _gpu_cast(b, o, d, cuda, cull=cull)
         diff = ia != ib
-        assert diff.sum() <= max(1, int(1e-5 * len(o))), int(diff.sum())
+        assert diff.sum() <= max(1, int(2e-4 * len(o))), int(diff.sum())
         same = ~diff & (ia >= 0)
         assert np.array_equal(ta[same].view(np.int32), tb[same].view(np.int32))
+        both = diff & (ia >= 0) & (ib >= 0)
+        assert np.all(np.abs(ta[both].astype(np.float64) - tb[both]) <= 1e-3 * np.abs(ta[both])), both.sum()
+        flips = diff & ((ia >= 0) != (ib >= 0))
+        assert flips.sum() <= max(2, int(2e-6 * len(o))), int(flips.sum())
 
 
 def test_cast_counters_equal_reference_traversal(cuda):
