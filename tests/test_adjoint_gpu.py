@@ -127,6 +127,47 @@ def test_adjoint_matches_fp64_oracle_finite_differences(cuda):
         assert abs(ga_h[k, ch] - fd) <= 2e-2 * abs(fd) + 1e-6, (k, ch, ga_h[k, ch], fd)
 
 
+def test_c5_workload_gradient_vs_fp64_oracle_fd(cuda):
+    """The differentiable workload itself (icosphere L7 + box room, 327,692 triangles, per-triangle albedo
+    U[0.1, 0.9], emission 10 on 64 triangles, 512x512, 16 spp, depth 5) on a 16-block range at the image
+    centre: adjoint gradients of the L2 loss against central differences (h = 1e-3) of the FP64 oracle's
+    loss for the 4 largest albedo components, within 2e-2 relative."""
+    S = scenes.differentiable_scene(7)
+    tris, n = S["tris"], len(S["tris"])
+    mats = [dr.lambert()]
+    sc = dr.Scene(tris, mat_id=S["mat_id"], materials=mats, box_epsilon=dr.PHYSICAL_TREE)
+    sc.set_triangle_params(S["albedo"], S["emission"], S["roughness"])
+    osc = O.OracleScene(tris, mat_id=S["mat_id"], materials=mats)
+    cam = dr.camera(dr.LENS_PINHOLE, position=(0.0, 0.0, -0.99), angle=60.0)
+    p = dr.render_params(512, 512, dr.MODE_PHYSICAL, samples=(4, 4), max_bounces=5, seed=7)
+    s0 = 16 * 64 + 24
+    s1 = s0 + 16
+    rows = slice(s0 * 128, s1 * 128)
+    osc.set_triangle_params(S["albedo_target"], S["emission"], S["roughness"])
+    t_or = osc.render_blocks(cam, p, start=s0, end=s1).astype(np.float64)
+    osc.set_triangle_params(S["albedo"], S["emission"], S["roughness"])
+    i_or = osc.render_blocks(cam, p, start=s0, end=s1).astype(np.float64)
+    dl = torch.zeros((dr.block_count(512, 512) * 128, 4), dtype=torch.float32, device=cuda)
+    dl[rows, :3] = torch.from_numpy(2.0 * (i_or[rows, :3] - t_or[rows, :3])).float().to(cuda)
+    ga = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
+    ge = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
+    dr.Renderer(1 << 16).render_adjoint(sc, cam, dl, s0, s1, p, ga, ge)
+    torch.cuda.synchronize()
+    ga_h = ga.cpu().numpy()
+    assert float(np.abs(ga_h).sum()) > 0 and float(ge.abs().sum()) > 0
+    for f in np.argsort(-np.abs(ga_h).ravel())[:4]:
+        k, ch = divmod(int(f), 3)
+        vals = []
+        for sgn in (1, -1):
+            a2 = S["albedo"].copy()
+            a2[k, ch] += sgn * 1e-3
+            osc.set_triangle_params(a2, S["emission"], S["roughness"])
+            im = osc.render_blocks(cam, p, start=s0, end=s1).astype(np.float64)
+            vals.append(float(((im[rows, :3] - t_or[rows, :3]) ** 2).sum()))
+        fd = (vals[0] - vals[1]) / 2e-3
+        assert abs(ga_h[k, ch] - fd) <= 2e-2 * abs(fd) + 1e-6, (k, ch, ga_h[k, ch], fd)
+
+
 def test_autograd_harness(cuda):
     """torch.autograd.Function over the C ABI: backward equals a direct dr_render_adjoint call."""
     sc, cam, p, tris, mat, mats, albedo, emission, rough, target_alb = _setup(cuda)
