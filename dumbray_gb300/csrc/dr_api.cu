@@ -339,6 +339,7 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
     S.root_leaf_first = (int)T.root_leaf_first;
     S.root_leaf_count = T.root_leaf_count;
     S.n_tris = n;
+    S.front_only = (bp && bp->box_epsilon != 0.0f) ? 1 : 0;
     S.n_mats = std::max(n_mats, 1);
     S.n_lights = n_lights;
     if (n == 0) { S.root_child = -1; S.root_leaf_count = 0; }
@@ -785,7 +786,12 @@ static dr_status build_arena(dr_batch *b) {
     }
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cuda_fail(e, "dr_batch_create: octree arena");
+    // the traversal reads the behind-origin culling flag from the arena (uniform): on only if every
+    // scene of the batch allows it
+    int front = 1;
+    for (const dr_scene *sc : uniq) front &= sc->dev.front_only;
     for (size_t i = 0; i < b->items.size(); i++) {
+        b->items[i].S.front_only = front;
         const size_t k = (size_t)(std::find(uniq.begin(), uniq.end(), b->scenes[i]) - uniq.begin());
         drd::Scene &S = b->items[i].S;
         S.nodes = b->arena_nodes;

@@ -57,6 +57,10 @@ struct Scene {
                                 // scene's offset in a batch arena), -1 = the root is a leaf
     int root_leaf_first, root_leaf_count;
     int n_tris, n_mats, n_lights, n_emissive;
+    // 1 = skip boxes that lie entirely behind the ray origin (set for scenes built with a padding
+    // scaled to the scene).  The reference's slab test keeps them (clipBackface = false), which only
+    // costs work: a hit at t > 0 accepted inside a leaf box means that box reaches t > 0.
+    int front_only;
     float emissive_total;
 };
 
@@ -83,7 +87,8 @@ __device__ __forceinline__ f3 f3of(float4 v) { return f3{v.x, v.y, v.z}; }
 
 // AABB::castPreInversed + Shapes::castPreInversed<AABB>(.., clipBackface = false)
 // (AABB.impl.h:116-130, Shapes.impl.cuh:143-147)
-__device__ __forceinline__ bool slab_hit(float lx, float ly, float lz, float hx, float hy, float hz, f3 o, f3 inv) {
+__device__ __forceinline__ bool slab_hit(float lx, float ly, float lz, float hx, float hy, float hz, f3 o, f3 inv,
+                                         bool front = false) {
     float ds = __fmul_rn(__fsub_rn(lx, o.x), inv.x);
     float de = __fmul_rn(__fsub_rn(hx, o.x), inv.x);
     float mn = fminf(ds, de), mx = fmaxf(ds, de);
@@ -96,6 +101,7 @@ __device__ __forceinline__ bool slab_hit(float lx, float ly, float lz, float hx,
     mn = fmaxf(mn, fminf(ds, de));
     mx = fminf(mx, fmaxf(ds, de));
     if (mn > __fadd_rn(mx, kEps)) return false;
+    if (front && mx < -kEps) return false;  // entirely behind the origin (front_only scenes)
     return mn != FLT_MAX;
 }
 
@@ -187,14 +193,14 @@ __device__ __forceinline__ bool cast_leaf(const Scene &S, int first, int count, 
 }
 
 // Tests the 8 children of a group; bit k of the result = child (order ^ k) is hit.
-__device__ __forceinline__ unsigned test_group(const float4 *nodes, int group, int order, f3 o, f3 inv) {
+__device__ __forceinline__ unsigned test_group(const float4 *nodes, int group, int order, f3 o, f3 inv, bool front) {
     unsigned m = 0;
     const float4 *g = nodes + 16 * (size_t)group;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
         int c = order ^ k;
         float4 lo = __ldg(g + 2 * c), hi = __ldg(g + 2 * c + 1);
-        if (slab_hit(lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, o, inv)) m |= 1u << k;
+        if (slab_hit(lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, o, inv, front)) m |= 1u << k;
     }
     return m;
 }
@@ -220,12 +226,13 @@ __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool cl
         return cast_leaf(S, S.root_leaf_first, S.root_leaf_count, S.root_lo[0], S.root_lo[1], S.root_lo[2], S.root_hi[0],
                          S.root_hi[1], S.root_hi[2], o, d, clip, ignore, h, ntri);
     if (COUNT) nbox++;
-    if (!slab_hit(S.root_lo[0], S.root_lo[1], S.root_lo[2], S.root_hi[0], S.root_hi[1], S.root_hi[2], o, inv)) return false;
+    const bool front = S.front_only != 0;
+    if (!slab_hit(S.root_lo[0], S.root_lo[1], S.root_lo[2], S.root_hi[0], S.root_hi[1], S.root_hi[2], o, inv, front)) return false;
     const int order = (d.z < 0 ? 1 : 0) + (d.y < 0 ? 2 : 0) + (d.x < 0 ? 4 : 0);
     constexpr int GS = group_shift<COUNT>();
     uint32_t stack[kStack];
     int sp = 0;
-    uint32_t cur = ((uint32_t)S.root_child << GS) | test_group(S.nodes, S.root_child, order, o, inv);
+    uint32_t cur = ((uint32_t)S.root_child << GS) | test_group(S.nodes, S.root_child, order, o, inv, front);
     if (COUNT) nbox += 8;
     for (;;) {
         uint32_t m = cur & 0xFFu;
@@ -251,7 +258,7 @@ __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool cl
         } else {
             if (sp >= kStack) return false;  // unreachable for trees of depth <= 24
             stack[sp++] = COUNT ? ((cur & ~(7u << 8)) | ((uint32_t)k << 8)) : cur;
-            cur = ((uint32_t)(w >> 3) << GS) | test_group(S.nodes, w >> 3, order, o, inv);
+            cur = ((uint32_t)(w >> 3) << GS) | test_group(S.nodes, w >> 3, order, o, inv, front);
             if (COUNT) nbox += 8;
         }
     }
