@@ -328,12 +328,19 @@ struct TraceSource {
     }
 };
 
+// Block shape of the traversal kernels (k_trace, k_shadow_phys): 8 warps, 3 blocks per SM caps
+// registers at 80 (24 warps per SM); the traversal state needs about that many without spilling.
+// Measured on the 1080p path trace (Mpaths/s): 256x3 205.7, 128x6 205.4 (80 registers), 128x7 199.8
+// and 64x13 199.8 (72 registers, spills).
+constexpr int kTraceThreads = 256;
+constexpr int kTraceBlocksPerSM = 3;
+
 template <bool COUNT, bool MULTI>
-__global__ void __launch_bounds__(256, 3) k_trace(WaveArgs A, int b) {
+__global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const int n = *((volatile int *)&C->ray_count[b]);
     uint32_t stack[kStack];
-    __shared__ WarpLeafSlots slots[8];
+    __shared__ WarpLeafSlots slots[kTraceThreads / 32];
     TraceSource<MULTI> src{&A, A.q[b & 1], A.hits, &C->fetch_trace[b], n, chunk_for(n), 0, 0, 0};
     trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5]);
     if (COUNT) count_add64(A.counters, src.rays, src.nb, src.nt);
@@ -723,11 +730,11 @@ struct ShadowPhysSource {
 // (direction = light point - shading point, so the light is at t = 1), ignoring the shading
 // triangle; visible if nothing but the light triangle is hit before t = 0.999.
 template <bool COUNT, bool MULTI, bool ADJ>
-__global__ void __launch_bounds__(256, 3) k_shadow_phys(WaveArgs A, int b) {
+__global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_shadow_phys(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const int n = *((volatile int *)&C->shadow_count[b]);
     uint32_t stack[kStack];
-    __shared__ WarpLeafSlots slots[8];
+    __shared__ WarpLeafSlots slots[kTraceThreads / 32];
     ShadowPhysSource<MULTI, ADJ> src{&A, A.sq, A.accum, &C->fetch_shadow[b], n, chunk_for(n), 0, 0, 0};
     trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5]);
     if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
@@ -898,10 +905,11 @@ static void launch_wave_t(const WaveDesc &W, const WaveArgs &A, cudaStream_t str
     k_camera<MULTI><<<grid, 256, 0, stream>>>(A);
     P.end(KC_CAMERA, stream);
     nl++;
+    const int tgrid = grid * (256 / kTraceThreads);   // same threads in flight as the 256-thread kernels
     for (int b = 0; b <= W.max_bounces; b++) {
         P.begin(KC_TRACE, stream);
-        if (count) k_trace<true, MULTI><<<grid, 256, 0, stream>>>(A, b);
-        else k_trace<false, MULTI><<<grid, 256, 0, stream>>>(A, b);
+        if (count) k_trace<true, MULTI><<<tgrid, kTraceThreads, 0, stream>>>(A, b);
+        else k_trace<false, MULTI><<<tgrid, kTraceThreads, 0, stream>>>(A, b);
         P.end(KC_TRACE, stream);
         P.begin(KC_SHADE, stream);
         if (W.mode == DR_MODE_REFERENCE) k_shade_ref<MULTI><<<grid, 256, 0, stream>>>(A, b);
@@ -913,10 +921,10 @@ static void launch_wave_t(const WaveDesc &W, const WaveArgs &A, cudaStream_t str
             if (count) k_shadow_ref<true, MULTI><<<grid, 256, 0, stream>>>(A, b);
             else k_shadow_ref<false, MULTI><<<grid, 256, 0, stream>>>(A, b);
         } else if (W.adjoint) {
-            k_shadow_phys<false, MULTI, true><<<grid, 256, 0, stream>>>(A, b);
+            k_shadow_phys<false, MULTI, true><<<tgrid, kTraceThreads, 0, stream>>>(A, b);
         } else {
-            if (count) k_shadow_phys<true, MULTI, false><<<grid, 256, 0, stream>>>(A, b);
-            else k_shadow_phys<false, MULTI, false><<<grid, 256, 0, stream>>>(A, b);
+            if (count) k_shadow_phys<true, MULTI, false><<<tgrid, kTraceThreads, 0, stream>>>(A, b);
+            else k_shadow_phys<false, MULTI, false><<<tgrid, kTraceThreads, 0, stream>>>(A, b);
         }
         P.end(KC_SHADOW, stream);
         nl += 3;
