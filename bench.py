@@ -410,7 +410,11 @@ def run_raycast(dr, torch, dev, a, peak, peak_src):
     mesh = scenes.displaced_icosphere(a.level, 0.1, 1)
     out = {"workload": f"displaced icosphere L{a.level} alone ({len(mesh):,} tris), closest hit, backface culling; "
                        "reference_tree = the reference's octree (casts bit-exact to Octree::cast), physical_tree = "
-                       "padding 2^-18 x max |coordinate| (same closest hits up to exact ties)"}
+                       "padding 2^-18 x max |coordinate| (same closest hits up to float32 near-ties)",
+           "counts": "c_box / c_tri from dr_cast_counted: on the reference tree the reference's own traversal (it "
+                     "also tests boxes lying behind the ray origin, which dr_cast skips without changing any hit), "
+                     "so the reference-tree roofline is an effective figure; on the physical tree the traversal "
+                     "dr_cast runs"}
     sets = {"primary_1080p": scenes.primary_rays(1920, 1080, 60.0, (0.0, 0.3, -3.0), (0.0, 0.0, 0.0)),
             "incoherent_8M": scenes.incoherent_rays(8 * 1024 * 1024, -1.1, 1.1, seed=0)}
     K = max(3, a.steps)

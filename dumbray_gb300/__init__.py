@@ -297,8 +297,7 @@ class Scene:
     (depth 24, 8 triangles per leaf, 1.28e-3 box padding): casts and traversal counts then match the
     reference's.  ``box_epsilon=PHYSICAL_TREE`` (any negative value) pads boxes by 2^-18 x the largest
     absolute coordinate instead, for scenes rendered in the physical mode only: the same closest hits
-    up to float32 near-ties, with far fewer duplicated leaf references on finely tessellated meshes;
-    its traversals also skip octree boxes lying entirely behind the ray origin."""
+    up to float32 near-ties, with far fewer duplicated leaf references on finely tessellated meshes."""
 
     def __init__(self, tris, normals=None, mat_id=None, materials=(), lights=(), max_depth=0, split_threshold=0,
                  threads=0, box_epsilon=0.0):

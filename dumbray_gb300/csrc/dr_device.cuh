@@ -57,9 +57,11 @@ struct Scene {
                                 // scene's offset in a batch arena), -1 = the root is a leaf
     int root_leaf_first, root_leaf_count;
     int n_tris, n_mats, n_lights, n_emissive;
-    // 1 = skip boxes that lie entirely behind the ray origin (set for scenes built with a padding
-    // scaled to the scene).  The reference's slab test keeps them (clipBackface = false), which only
-    // costs work: a hit at t > 0 accepted inside a leaf box means that box reaches t > 0.
+    // Boxes lying entirely behind the ray origin: the reference's slab test keeps them
+    // (clipBackface = false), which only costs work, since a hit at t > 0 accepted inside a leaf box
+    // means that box reaches t > 0.  Every non-counting traversal skips them; the counting ones
+    // (which reproduce the reference's box-test counts) skip them only when front_only = 1, i.e. for
+    // scenes built with a padding scaled to the scene, whose counts are not the reference's anyway.
     int front_only;
     float emissive_total;
 };
@@ -226,7 +228,7 @@ __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool cl
         return cast_leaf(S, S.root_leaf_first, S.root_leaf_count, S.root_lo[0], S.root_lo[1], S.root_lo[2], S.root_hi[0],
                          S.root_hi[1], S.root_hi[2], o, d, clip, ignore, h, ntri);
     if (COUNT) nbox++;
-    const bool front = S.front_only != 0;
+    const bool front = !COUNT || S.front_only != 0;
     if (!slab_hit(S.root_lo[0], S.root_lo[1], S.root_lo[2], S.root_hi[0], S.root_hi[1], S.root_hi[2], o, inv, front)) return false;
     const int order = (d.z < 0 ? 1 : 0) + (d.y < 0 ? 2 : 0) + (d.x < 0 ? 4 : 0);
     constexpr int GS = group_shift<COUNT>();

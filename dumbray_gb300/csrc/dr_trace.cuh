@@ -59,7 +59,7 @@ __device__ __forceinline__ int lane_start(const Scene &S, LaneRay &L) {
         return kLeaf;
     }
     if (COUNT) L.nb++;
-    const bool front = S.front_only != 0;
+    const bool front = !COUNT || S.front_only != 0;
     if (slab_hit(S.root_lo[0], S.root_lo[1], S.root_lo[2], S.root_hi[0], S.root_hi[1], S.root_hi[2], L.o, L.inv, front)) {
         L.cur = ((uint32_t)S.root_child << group_shift<COUNT>()) |
                 test_group(S.nodes, S.root_child, L.order, L.o, L.inv, front);
@@ -94,7 +94,7 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
     int mode = kIdle;
     constexpr int GS = group_shift<COUNT>();
     const bool clip = src.clip(0);
-    const bool front = S.front_only != 0;   // uniform: one scene, or one arena of a batch
+    const bool front = !COUNT || S.front_only != 0;   // uniform: one scene, or one arena of a batch
     LaneRay L;
     L.r = 0;
     L.r_end = 0;

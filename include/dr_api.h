@@ -46,9 +46,10 @@ typedef struct dr_renderer dr_renderer;
  * box_epsilon scaled to its coordinates (an absolute 1.28e-3 is a large fraction of the leaf cells
  * of a finely tessellated unit-size mesh, which duplicates triangles into many leaves):
  * box_epsilon > 0 is used as given, box_epsilon < 0 selects 2^-18 x the largest absolute vertex
- * coordinate (margin for the rounding of hit points in the leaf-box acceptance test).  Traversals of
- * a scene built with box_epsilon != 0 also skip boxes lying entirely behind the ray origin, which
- * the reference's slab test keeps (clipBackface = false) although no hit at t > 0 can come of them. */
+ * coordinate (margin for the rounding of hit points in the leaf-box acceptance test).  Traversals
+ * skip octree boxes lying entirely behind the ray origin, which the reference's slab test keeps
+ * (clipBackface = false) although no hit at t > 0 can come of them; dr_cast_counted, whose counts
+ * reproduce the reference's, keeps them on scenes built with box_epsilon = 0. */
 typedef struct {
     int32_t max_depth;
     int32_t split_threshold;
