@@ -81,6 +81,9 @@ class DumbRayError(RuntimeError):
 _lib = None
 
 
+PROGRESS_CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p)
+
+
 def lib() -> ctypes.CDLL:
     """The native library (loaded once).  Raises if it has not been built."""
     global _lib
@@ -148,6 +151,35 @@ def lib() -> ctypes.CDLL:
     L.dr_batch_destroy.argtypes = [vp]
     L.dr_render_blocks.restype = i32
     L.dr_render_blocks.argtypes = [vp, vp, vp, vp, i32, i32, vp, vp]
+    for fn in ("dr_image_from_blocks", "dr_image_to_rgba8"):
+        getattr(L, fn).restype = i32
+        getattr(L, fn).argtypes = [vp, i32, i32, vp]
+    for fn in ("dr_image_write_png", "dr_image_write_pfm"):
+        getattr(L, fn).restype = i32
+        getattr(L, fn).argtypes = [vp, i32, i32, ctypes.c_char_p]
+    L.dr_progressive_create.restype = i32
+    L.dr_progressive_create.argtypes = [vp, vp, vp, i32, P(vp)]
+    L.dr_progressive_set_target.restype = i32
+    L.dr_progressive_set_target.argtypes = [vp, i32]
+    L.dr_progressive_set_view.restype = i32
+    L.dr_progressive_set_view.argtypes = [vp, vp, vp]
+    L.dr_progressive_set_callbacks.restype = i32
+    L.dr_progressive_set_callbacks.argtypes = [vp, PROGRESS_CALLBACK, PROGRESS_CALLBACK, PROGRESS_CALLBACK, vp]
+    for fn in ("dr_progressive_start", "dr_progressive_stop"):
+        getattr(L, fn).restype = i32
+        getattr(L, fn).argtypes = [vp]
+    L.dr_progressive_wait.restype = i32
+    L.dr_progressive_wait.argtypes = [vp, i32, i32]
+    L.dr_progressive_completed.restype = i32
+    L.dr_progressive_completed.argtypes = [vp]
+    L.dr_progressive_read.restype = i32
+    L.dr_progressive_read.argtypes = [vp, vp, i32, i32, P(i32)]
+    L.dr_progressive_save_png.restype = i32
+    L.dr_progressive_save_png.argtypes = [vp, ctypes.c_char_p]
+    L.dr_progressive_render_seconds.restype = ctypes.c_double
+    L.dr_progressive_render_seconds.argtypes = [vp]
+    L.dr_progressive_destroy.restype = None
+    L.dr_progressive_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -661,3 +693,103 @@ def device_view(ptr: int, shape, device="cuda"):
 
 def _copy_into(dst_ptr: int, src, n: int):
     device_view(dst_ptr, (n, 3), src.device).copy_(src)
+
+
+# ---- images (host) ---------------------------------------------------------------------------
+
+def _image_arg(rgba):
+    a = np.ascontiguousarray(rgba, dtype=np.float32)
+    if a.ndim != 3 or a.shape[2] != 4:
+        raise ValueError("expected a float32 [height, width, 4] image")
+    return a
+
+
+def to_rgba8(rgba) -> np.ndarray:
+    """dr_image_to_rgba8: the reference's 8-bit conversion (v = 255 c, clamped, truncated)."""
+    a = _image_arg(rgba)
+    out = np.empty(a.shape, np.uint8)
+    check(lib().dr_image_to_rgba8(a.ctypes.data, a.shape[1], a.shape[0], out.ctypes.data))
+    return out
+
+
+def image_from_blocks(fb, width: int, height: int) -> np.ndarray:
+    """dr_image_from_blocks on a host copy of a block-major frame buffer."""
+    f = np.ascontiguousarray(fb.detach().cpu().numpy() if hasattr(fb, "detach") else fb, dtype=np.float32)
+    out = np.empty((height, width, 4), np.float32)
+    check(lib().dr_image_from_blocks(f.ctypes.data, width, height, out.ctypes.data))
+    return out
+
+
+def write_png(rgba, path) -> None:
+    """dr_image_write_png: 8-bit RGBA PNG with the reference's channel conversion."""
+    a = _image_arg(rgba)
+    check(lib().dr_image_write_png(a.ctypes.data, a.shape[1], a.shape[0], str(path).encode()))
+
+
+def write_pfm(rgba, path) -> None:
+    """dr_image_write_pfm: float RGB portable float map (unclamped radiance)."""
+    a = _image_arg(rgba)
+    check(lib().dr_image_write_pfm(a.ctypes.data, a.shape[1], a.shape[0], str(path).encode()))
+
+
+class Progressive:
+    """Progressive render process (dr_progressive, the reference's BufferedRenderProcess without its
+    window): a native worker thread renders iteration after iteration of one view and publishes each
+    finished image.  Callbacks (Python callables without arguments) run on the worker thread."""
+
+    def __init__(self, scene: Scene, cam: DrCamera, params: DrRenderParams, double_buffered: bool = False):
+        h = ctypes.c_void_p()
+        check(lib().dr_progressive_create(scene.handle, ctypes.byref(cam), ctypes.byref(params),
+                                          1 if double_buffered else 0, ctypes.byref(h)))
+        self._h, self._scene, self.width, self.height = h, scene, params.width, params.height
+        self._cbs = None
+
+    def set_target(self, iterations: int):
+        check(lib().dr_progressive_set_target(self._h, int(iterations)))
+
+    def set_view(self, cam: DrCamera = None, params: DrRenderParams = None):
+        check(lib().dr_progressive_set_view(self._h, None if cam is None else ctypes.byref(cam),
+                                            None if params is None else ctypes.byref(params)))
+        if params is not None:
+            self.width, self.height = params.width, params.height
+
+    def set_callbacks(self, on_iteration=None, on_complete=None, on_error=None):
+        wrap = [PROGRESS_CALLBACK(lambda _a, f=f: f()) if f else PROGRESS_CALLBACK() for f in (on_iteration, on_complete, on_error)]
+        self._cbs = wrap   # keep the ctypes thunks alive while the worker may call them
+        check(lib().dr_progressive_set_callbacks(self._h, wrap[0], wrap[1], wrap[2], None))
+
+    def start(self):
+        check(lib().dr_progressive_start(self._h))
+
+    def stop(self):
+        check(lib().dr_progressive_stop(self._h))
+
+    def wait(self, count: int, timeout_ms: int = 60000):
+        check(lib().dr_progressive_wait(self._h, int(count), int(timeout_ms)))
+
+    def completed(self) -> int:
+        return int(lib().dr_progressive_completed(self._h))
+
+    def read(self):
+        """(row-major float32 [H, W, 4] image, its iteration index)."""
+        out = np.empty((self.height, self.width, 4), np.float32)
+        it = ctypes.c_int32()
+        check(lib().dr_progressive_read(self._h, out.ctypes.data, self.width, self.height, ctypes.byref(it)))
+        return out, int(it.value)
+
+    def save_png(self, path):
+        check(lib().dr_progressive_save_png(self._h, str(path).encode()))
+
+    def render_seconds(self) -> float:
+        return float(lib().dr_progressive_render_seconds(self._h))
+
+    def close(self):
+        if self._h is not None:
+            lib().dr_progressive_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -327,6 +327,59 @@ dr_status dr_renderer_set_counting(dr_renderer *r, int32_t enable);
  * {extension rays, their box tests, their triangle tests, shadow casts, their box tests, their triangle tests}. */
 dr_status dr_renderer_counters(dr_renderer *r, int64_t *counts);
 
+/* ---- images (host memory) ----------------------------------------------------------------
+ * Replace Images::saveBufferPNG (__source__/Namespaces/Images/Images.cu:22-40) and the frame
+ * buffer's getColor walk it does.  rgba is a row-major float[height][width][4] image. */
+
+/* Block-major frame buffer (DR_BLOCK_W x DR_BLOCK_H blocks, host copy) -> row-major rgba. */
+dr_status dr_image_from_blocks(const float *fb_blockmajor, int32_t width, int32_t height, float *rgba);
+
+/* The reference's 8-bit conversion of every channel: v = 255*c; v > 255 -> 255, v < 0 -> 0, else
+ * truncated (Images.cu:7-12).  out: uint8[height][width][4]. */
+dr_status dr_image_to_rgba8(const float *rgba, int32_t width, int32_t height, uint8_t *out);
+
+/* 8-bit RGBA PNG of those bytes (stored-deflate zlib stream; any PNG reader decodes the same
+ * pixels as the reference's lodepng file). */
+dr_status dr_image_write_png(const float *rgba, int32_t width, int32_t height, const char *path);
+
+/* Portable float map (RGB, little-endian, rows bottom-up): the unclamped radiance. */
+dr_status dr_image_write_pfm(const float *rgba, int32_t width, int32_t height, const char *path);
+
+/* ---- progressive render process -----------------------------------------------------------
+ * Replaces BufferedRenderProcess (__source__/DataStructures/Renderers/BufferedRenderProcess/
+ * BufferedRenderProcess.cu:42-229) without its window: a host worker thread renders iteration after
+ * iteration of one view (its own dr_renderer and CUDA stream, on the device current at creation)
+ * and publishes each finished image as a host row-major float4 copy.  double_buffered = 0: iterations
+ * accumulate with the progressive blend until `target` iterations; 1: like the reference's double
+ * buffering (swap and reset after each iteration), every frame is one fresh iteration (seed +
+ * frame index) rendered while the previous frame stays readable; `target` then counts frames.
+ * Changing the view restarts the count (the reference restarts on a resolution change).  Callbacks
+ * run on the worker thread. */
+typedef struct dr_progressive dr_progressive;
+typedef void (*dr_progress_callback)(void *arg);
+
+dr_status dr_progressive_create(const dr_scene *scene, const dr_camera *camera, const dr_render_params *params,
+                                int32_t double_buffered, dr_progressive **out);
+/* Iterations (frames when double-buffered) to render before idling; < 0 = until stopped (default). */
+dr_status dr_progressive_set_target(dr_progressive *p, int32_t iterations);
+/* New camera and/or parameters (either may be NULL); restarts the accumulation. */
+dr_status dr_progressive_set_view(dr_progressive *p, const dr_camera *camera, const dr_render_params *params);
+/* setIterationCompletionCallback / setRenderCompletionCallback / setErrorOnIteration. */
+dr_status dr_progressive_set_callbacks(dr_progressive *p, dr_progress_callback on_iteration,
+                                       dr_progress_callback on_complete, dr_progress_callback on_error, void *arg);
+dr_status dr_progressive_start(dr_progressive *p);
+/* Stops the worker after the iteration in flight. */
+dr_status dr_progressive_stop(dr_progressive *p);
+/* Waits until at least `count` iterations (frames) of the current view are complete; DR_E_TIMEOUT otherwise. */
+dr_status dr_progressive_wait(dr_progressive *p, int32_t count, int32_t timeout_ms);
+int32_t dr_progressive_completed(dr_progressive *p);
+/* Copies the last complete image (rgba float[height][width][4]) and its iteration index. */
+dr_status dr_progressive_read(dr_progressive *p, float *rgba, int32_t width, int32_t height, int32_t *iteration);
+dr_status dr_progressive_save_png(dr_progressive *p, const char *path);
+/* Summed wall time of the completed iterations (renderTime, BufferedRenderProcess.cu:109-115). */
+double dr_progressive_render_seconds(dr_progressive *p);
+void dr_progressive_destroy(dr_progressive *p);
+
 #ifdef __cplusplus
 }
 #endif

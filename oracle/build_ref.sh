@@ -1,6 +1,7 @@
 #!/usr/bin/env bash
 # Builds the reference DumbRay CPU path (octree cast + DumbRenderer on host threads) into
-# oracle/_ref/libdumbref.so, for use as a parity checker and as the timed CPU baseline.
+# oracle/_ref/libdumbref.so (plus its PNG writer, Images::saveBufferPNG + lodepng), for use as a
+# parity checker and as the timed CPU baseline.
 #
 # The reference sources are read from $DUMBRAY_REFERENCE (default: the read-only checkout at
 # /root/reference).  They are copied into oracle/_ref/src (git-ignored) because two portability
@@ -49,6 +50,8 @@ TUS=(
   "$S/DataStructures/GeneralPurpose/Semaphore/Semaphore.cu"
   "$S/DataStructures/Screen/FrameBuffer/BlockBasedFrameBuffer/BlockBasedFrameBuffer.impl.cu"
   "$S/Namespaces/Device/Device.cu"
+  "$S/Namespaces/Images/Images.cu"
+  "$S/Namespaces/Images/lodepng.cu"
   "$HERE/ref_driver.cu"
 )
 ARCH="${DUMBRAY_REF_ARCH:-sm_100}"

@@ -21,6 +21,7 @@
 #include "DataStructures/Objects/Scene/Lights/SphericalLightEmitter/SphericalLightEmitter.cuh"
 #include "DataStructures/Objects/Scene/Lights/SimpleSoftDirectionalLight/SimpleSoftDirectionalLight.cuh"
 #include "DataStructures/Objects/Scene/Lights/SimpleDirectionalLight/SimpleDirectionalLight.cuh"
+#include "Namespaces/Images/Images.cuh"
 #include <thread>
 #include <vector>
 #include <chrono>
@@ -159,6 +160,20 @@ double dref_render(void *h, int width, int height, int fsaa_x, int fsaa_y, int m
 			}
 	}
 	return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// Writes a row-major float4 image through the reference's own Images::saveBufferPNG (lodepng), via
+// a host BlockBuffer filled with FrameBuffer::setColor.  Returns the Images::Error code (0 = ok).
+int dref_save_png(const float *rgba, int width, int height, const char *path) {
+	FrameBufferManager fb;
+	fb.cpuHandle()->use<BlockBuffer>();
+	if (!fb.cpuHandle()->setResolution(width, height)) return -1;
+	for (int y = 0; y < height; y++)
+		for (int x = 0; x < width; x++) {
+			const float *p = rgba + 4 * (y * width + x);
+			fb.cpuHandle()->setColor(x, y, Color(p[0], p[1], p[2], p[3]));
+		}
+	return (int)Images::saveBufferPNG(*fb.cpuHandle(), path);
 }
 
 }  // extern "C"

@@ -62,6 +62,9 @@ def reference():
         L.dref_scene_destroy.argtypes = [vp]
         L.dref_render.restype = ctypes.c_double
         L.dref_render.argtypes = [vp, ci, ci, ci, ci, ci, ci, ci, ci, vp]
+        if hasattr(L, "dref_save_png"):
+            L.dref_save_png.restype = ci
+            L.dref_save_png.argtypes = [vp, ci, ci, ctypes.c_char_p]
         _r = L
     return _r
 
