@@ -157,6 +157,18 @@ def lib() -> ctypes.CDLL:
     for fn in ("dr_image_write_png", "dr_image_write_pfm"):
         getattr(L, fn).restype = i32
         getattr(L, fn).argtypes = [vp, i32, i32, ctypes.c_char_p]
+    L.dr_obj_read.restype = i32
+    L.dr_obj_read.argtypes = [ctypes.c_char_p, P(vp)]
+    L.dr_mesh_file_objects.restype = i32
+    L.dr_mesh_file_objects.argtypes = [vp]
+    L.dr_mesh_file_object_name.restype = ctypes.c_char_p
+    L.dr_mesh_file_object_name.argtypes = [vp, i32]
+    L.dr_mesh_file_object_triangles.restype = i32
+    L.dr_mesh_file_object_triangles.argtypes = [vp, i32]
+    L.dr_mesh_file_object_data.restype = i32
+    L.dr_mesh_file_object_data.argtypes = [vp, i32, vp, vp, vp]
+    L.dr_mesh_file_destroy.restype = None
+    L.dr_mesh_file_destroy.argtypes = [vp]
     L.dr_progressive_create.restype = i32
     L.dr_progressive_create.argtypes = [vp, vp, vp, i32, P(vp)]
     L.dr_progressive_set_target.restype = i32
@@ -793,3 +805,23 @@ class Progressive:
             self.close()
         except Exception:
             pass
+
+
+# ---- OBJ meshes (host) -----------------------------------------------------------------------
+
+def read_obj(path):
+    """dr_obj_read: {object name: (xyz [n,3,3], normals [n,3,3], uv [n,3,3])} in file order, read with
+    the reference's rules (groups are `g` ranges, x mirrored, generated normals, triangle fans)."""
+    L = lib()
+    h = ctypes.c_void_p()
+    check(L.dr_obj_read(str(path).encode(), ctypes.byref(h)))
+    try:
+        out = {}
+        for i in range(L.dr_mesh_file_objects(h)):
+            n = L.dr_mesh_file_object_triangles(h, i)
+            xyz, nrm, uv = (np.zeros((n, 3, 3), np.float32) for _ in range(3))
+            check(L.dr_mesh_file_object_data(h, i, xyz.ctypes.data, nrm.ctypes.data, uv.ctypes.data))
+            out[L.dr_mesh_file_object_name(h, i).decode(errors="replace")] = (xyz, nrm, uv)
+        return out
+    finally:
+        L.dr_mesh_file_destroy(h)

@@ -345,6 +345,22 @@ dr_status dr_image_write_png(const float *rgba, int32_t width, int32_t height, c
 /* Portable float map (RGB, little-endian, rows bottom-up): the unclamped radiance. */
 dr_status dr_image_write_pfm(const float *rgba, int32_t width, int32_t height, const char *path);
 
+/* ---- OBJ meshes (host) -----------------------------------------------------------------------
+ * Replace MeshReader::readObj + PolyMesh::bake (__source__/Namespaces/MeshReader/MeshReader.impl.h:
+ * 160-367, __source__/DataStructures/Objects/Meshes/PolyMesh/PolyMesh.impl.h:140-152) with the same
+ * reading rules: objects are the face ranges between `g` lines, x of vertices and normals is mirrored,
+ * missing normals come from generated vertex normals, polygons become triangle fans.  Each object's
+ * triangles are float[n][3][3] (xyz), with per-corner normals and texture coordinates of the same
+ * shape, ready for dr_scene_create. */
+typedef struct dr_mesh_file dr_mesh_file;
+dr_status dr_obj_read(const char *path, dr_mesh_file **out);
+int32_t dr_mesh_file_objects(const dr_mesh_file *m);
+const char *dr_mesh_file_object_name(const dr_mesh_file *m, int32_t object);
+int32_t dr_mesh_file_object_triangles(const dr_mesh_file *m, int32_t object);
+/* Any of xyz / nrm / uv may be NULL. */
+dr_status dr_mesh_file_object_data(const dr_mesh_file *m, int32_t object, float *xyz, float *nrm, float *uv);
+void dr_mesh_file_destroy(dr_mesh_file *m);
+
 /* ---- progressive render process -----------------------------------------------------------
  * Replaces BufferedRenderProcess (__source__/DataStructures/Renderers/BufferedRenderProcess/
  * BufferedRenderProcess.cu:42-229) without its window: a host worker thread renders iteration after

@@ -22,6 +22,7 @@
 #include "DataStructures/Objects/Scene/Lights/SimpleSoftDirectionalLight/SimpleSoftDirectionalLight.cuh"
 #include "DataStructures/Objects/Scene/Lights/SimpleDirectionalLight/SimpleDirectionalLight.cuh"
 #include "Namespaces/Images/Images.cuh"
+#include "Namespaces/MeshReader/MeshReader.h"
 #include <thread>
 #include <vector>
 #include <chrono>
@@ -161,6 +162,37 @@ double dref_render(void *h, int width, int height, int fsaa_x, int fsaa_y, int m
 	}
 	return std::chrono::duration<double>(t1 - t0).count();
 }
+
+// OBJ files through the reference's MeshReader::readObj + PolyMesh::bake: a handle holding the
+// meshes and names, then per mesh the baked triangles (vert / norm / tex corners, 9 floats each).
+struct RefObj {
+	Stacktor<PolyMesh> meshes;
+	Stacktor<String> names;
+};
+void *dref_obj_read(const char *path) {
+	RefObj *o = new RefObj();
+	if (!MeshReader::readObj(o->meshes, o->names, path)) { delete o; return NULL; }
+	return o;
+}
+int dref_obj_meshes(void *h) { return ((RefObj *)h)->meshes.size(); }
+int dref_obj_names(void *h) { return ((RefObj *)h)->names.size(); }
+const char *dref_obj_name(void *h, int i) { return ((RefObj *)h)->names[i] + 0; }
+int dref_obj_triangles(void *h, int i, float *xyz, float *nrm, float *uv) {
+	const BakedTriMesh m = ((RefObj *)h)->meshes[i].bake();
+	for (int k = 0; k < m.size(); k++) {
+		const Triangle *t[3] = {&m[k].vert, &m[k].norm, &m[k].tex};
+		float *dst[3] = {xyz, nrm, uv};
+		for (int q = 0; q < 3; q++) {
+			if (dst[q] == NULL) continue;
+			const Vertex *c[3] = {&t[q]->a, &t[q]->b, &t[q]->c};
+			for (int v = 0; v < 3; v++) {
+				dst[q][9 * k + 3 * v] = c[v]->x; dst[q][9 * k + 3 * v + 1] = c[v]->y; dst[q][9 * k + 3 * v + 2] = c[v]->z;
+			}
+		}
+	}
+	return m.size();
+}
+void dref_obj_free(void *h) { delete (RefObj *)h; }
 
 // Writes a row-major float4 image through the reference's own Images::saveBufferPNG (lodepng), via
 // a host BlockBuffer filled with FrameBuffer::setColor.  Returns the Images::Error code (0 = ok).

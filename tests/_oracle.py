@@ -62,6 +62,18 @@ def reference():
         L.dref_scene_destroy.argtypes = [vp]
         L.dref_render.restype = ctypes.c_double
         L.dref_render.argtypes = [vp, ci, ci, ci, ci, ci, ci, ci, ci, vp]
+        if hasattr(L, "dref_obj_read"):
+            L.dref_obj_read.restype = vp
+            L.dref_obj_read.argtypes = [ctypes.c_char_p]
+            L.dref_obj_meshes.restype = ci
+            L.dref_obj_meshes.argtypes = [vp]
+            L.dref_obj_names.restype = ci
+            L.dref_obj_names.argtypes = [vp]
+            L.dref_obj_name.restype = ctypes.c_char_p
+            L.dref_obj_name.argtypes = [vp, ci]
+            L.dref_obj_triangles.restype = ci
+            L.dref_obj_triangles.argtypes = [vp, ci, vp, vp, vp]
+            L.dref_obj_free.argtypes = [vp]
         if hasattr(L, "dref_save_png"):
             L.dref_save_png.restype = ci
             L.dref_save_png.argtypes = [vp, ci, ci, ctypes.c_char_p]
@@ -204,3 +216,23 @@ def ref_render(tris, mat_id, materials, lights, cam, width, height, fsaa=(1, 1),
         return img, sec
     finally:
         L.dref_scene_destroy(h)
+
+
+def ref_read_obj(path):
+    """The reference's MeshReader::readObj + bake (oracle/_ref): None if it fails, else
+    (names, [(xyz, nrm, uv) per mesh])."""
+    L = reference()
+    h = L.dref_obj_read(str(path).encode())
+    if not h:
+        return None
+    try:
+        names = [L.dref_obj_name(h, i).decode(errors="replace") for i in range(L.dref_obj_names(h))]
+        meshes = []
+        for i in range(L.dref_obj_meshes(h)):
+            n = L.dref_obj_triangles(h, i, None, None, None)
+            arrs = [np.zeros((n, 3, 3), np.float32) for _ in range(3)]
+            L.dref_obj_triangles(h, i, *(a.ctypes.data for a in arrs))
+            meshes.append(tuple(arrs))
+        return names, meshes
+    finally:
+        L.dref_obj_free(h)
