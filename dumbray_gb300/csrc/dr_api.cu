@@ -308,12 +308,22 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
         d.softness = l.softness;
     }
 
-    float4 *d_nodes = nullptr, *d_leaf = nullptr, *d_tris = nullptr, *d_nrms = nullptr;
+    // child boxes of every node group as planes of 8 (see drd::Scene::gbox)
+    std::vector<float> gbox(48 * (nodes.size() / 16));
+    for (size_t g = 0; g < nodes.size() / 16; g++)
+        for (int c = 0; c < 8; c++) {
+            const float4 lo = nodes[16 * g + 2 * c], hi = nodes[16 * g + 2 * c + 1];
+            float *p = &gbox[48 * g];
+            p[c] = lo.x; p[8 + c] = lo.y; p[16 + c] = lo.z;
+            p[24 + c] = hi.x; p[32 + c] = hi.y; p[40 + c] = hi.z;
+        }
+    float4 *d_nodes = nullptr, *d_gbox = nullptr, *d_leaf = nullptr, *d_tris = nullptr, *d_nrms = nullptr;
     int *d_mat = nullptr;
     drd::Material *d_mats = nullptr;
     drd::Light *d_lights = nullptr;
     cudaError_t e = upload(&d_nodes, nodes.data(), nodes.size());
-    if (e == cudaSuccess) { sc->allocs.push_back(d_nodes); e = upload(&d_leaf, leaf_tris.data(), leaf_tris.size()); }
+    if (e == cudaSuccess) { sc->allocs.push_back(d_nodes); e = upload(&d_gbox, (const float4 *)gbox.data(), gbox.size() / 4); }
+    if (e == cudaSuccess) { sc->allocs.push_back(d_gbox); e = upload(&d_leaf, leaf_tris.data(), leaf_tris.size()); }
     if (e == cudaSuccess) { sc->allocs.push_back(d_leaf); e = upload(&d_tris, tris.data(), tris.size()); }
     if (e == cudaSuccess) { sc->allocs.push_back(d_tris); e = upload(&d_nrms, nrms.data(), nrms.size()); }
     if (e == cudaSuccess) { sc->allocs.push_back(d_nrms); e = upload(&d_mat, sc->mat_id.data(), sc->mat_id.size()); }
@@ -328,6 +338,7 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
     sc->leaf_f4 = (int64_t)leaf_tris.size();
     drd::Scene &S = sc->dev;
     S.nodes = d_nodes;
+    S.gbox = d_gbox;
     S.leaf_tris = d_leaf;
     S.tris = d_tris;
     S.nrms = d_nrms;
@@ -732,7 +743,7 @@ struct dr_batch {
     cudaEvent_t done = nullptr;   // recorded after each render: the job table is in use until it fires
     // One device arena holding the octrees of all the batch's scenes (node child / leaf indices
     // rebased), so the traversal reads nodes and leaf triangles through one pointer for every ray.
-    float4 *arena_nodes = nullptr, *arena_leaf = nullptr;
+    float4 *arena_nodes = nullptr, *arena_gbox = nullptr, *arena_leaf = nullptr;
     int64_t arena_node_count = 0;
 
     void drop_graph() {
@@ -747,6 +758,7 @@ struct dr_batch {
         if (capture_stream) cudaStreamDestroy(capture_stream);
         if (done) cudaEventDestroy(done);
         cudaFree(arena_nodes);
+        cudaFree(arena_gbox);
         cudaFree(arena_leaf);
         cudaFree(items_dev);
     }
@@ -775,10 +787,14 @@ static dr_status build_arena(dr_batch *b) {
         return fail(DR_E_CAPACITY, "dr_batch_create: the scenes' octrees exceed 2^27 nodes or 2^31 leaf references");
     cudaError_t e = cudaMalloc((void **)&b->arena_nodes, sizeof(float4) * (size_t)std::max<int64_t>(nodes, 2));
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->arena_leaf, sizeof(float4) * (size_t)std::max<int64_t>(leaf, 3));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->arena_gbox, sizeof(float4) * 12 * (size_t)std::max<int64_t>(nodes / 16, 1));
     for (size_t k = 0; k < uniq.size() && e == cudaSuccess; k++) {
         const dr_scene *sc = uniq[k];
         if (sc->leaf_f4)
             e = cudaMemcpy(b->arena_leaf + 3 * leaf_off[k], sc->dev.leaf_tris, sizeof(float4) * (size_t)sc->leaf_f4,
+                           cudaMemcpyDeviceToDevice);
+        if (e == cudaSuccess && sc->node_f4)
+            e = cudaMemcpy(b->arena_gbox + 12 * (node_off[k] / 8), sc->dev.gbox, sizeof(float4) * 12 * (size_t)(sc->node_f4 / 16),
                            cudaMemcpyDeviceToDevice);
         if (e == cudaSuccess && sc->node_f4)
             e = drk::launch_rebase_nodes(b->arena_nodes + 2 * node_off[k], sc->dev.nodes, sc->node_f4 / 2, (int)(node_off[k] / 8),
@@ -795,6 +811,7 @@ static dr_status build_arena(dr_batch *b) {
         const size_t k = (size_t)(std::find(uniq.begin(), uniq.end(), b->scenes[i]) - uniq.begin());
         drd::Scene &S = b->items[i].S;
         S.nodes = b->arena_nodes;
+        S.gbox = b->arena_gbox;
         S.leaf_tris = b->arena_leaf;
         if (S.root_child >= 0) S.root_child += (int)(node_off[k] / 8);
         S.root_leaf_first += (int)leaf_off[k];

@@ -40,6 +40,9 @@ struct Light {
 
 struct Scene {
     const float4 *nodes;
+    // The same child boxes per node group as planes of 8 floats (lo.x, lo.y, lo.z, hi.x, hi.y, hi.z;
+    // 12 float4 = 192 B per group), read by the group tests: 12 vector loads instead of 16.
+    const float4 *gbox;
     const float4 *leaf_tris;
     const float4 *tris;
     const float4 *nrms;
@@ -194,16 +197,45 @@ __device__ __forceinline__ bool cast_leaf(const Scene &S, int first, int count, 
     return false;
 }
 
-// Tests the 8 children of a group; bit k of the result = child (order ^ k) is hit.
-__device__ __forceinline__ unsigned test_group(const float4 *nodes, int group, int order, f3 o, f3 inv, bool front) {
-    unsigned m = 0;
-    const float4 *g = nodes + 16 * (size_t)group;
+// Tests the 8 children of a group; bit k of the result = child (order ^ k) is hit.  The slab tests
+// of the 8 children run plane by plane on the plane layout (x entry/exit of all children, then y,
+// then z), which keeps 16 running values instead of 48 coordinates live; each child's operations are
+// those of slab_hit in the same order.  Bit c of the octant-order mask then moves to c ^ order, so
+// results and counts equal a test in visit order.
+__device__ __forceinline__ void slab_planes(const float4 *g, int plane, float oc, float ic, float *mn, float *mx, bool first) {
+    const float4 l0 = __ldg(g + 2 * plane), l1 = __ldg(g + 2 * plane + 1);
+    const float4 h0 = __ldg(g + 6 + 2 * plane), h1 = __ldg(g + 6 + 2 * plane + 1);
+    const float lo[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+    const float hi[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
 #pragma unroll
-    for (int k = 0; k < 8; k++) {
-        int c = order ^ k;
-        float4 lo = __ldg(g + 2 * c), hi = __ldg(g + 2 * c + 1);
-        if (slab_hit(lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, o, inv, front)) m |= 1u << k;
+    for (int c = 0; c < 8; c++) {
+        const float ds = __fmul_rn(__fsub_rn(lo[c], oc), ic);
+        const float de = __fmul_rn(__fsub_rn(hi[c], oc), ic);
+        if (first) {
+            mn[c] = fminf(ds, de);
+            mx[c] = fmaxf(ds, de);
+        } else {
+            mn[c] = fmaxf(mn[c], fminf(ds, de));
+            mx[c] = fminf(mx[c], fmaxf(ds, de));
+        }
     }
+}
+
+__device__ __forceinline__ unsigned test_group(const float4 *gbox, int group, int order, f3 o, f3 inv, bool front) {
+    const float4 *g = gbox + 12 * (size_t)group;
+    float mn[8], mx[8];
+    slab_planes(g, 0, o.x, inv.x, mn, mx, true);
+    slab_planes(g, 1, o.y, inv.y, mn, mx, false);
+    slab_planes(g, 2, o.z, inv.z, mn, mx, false);
+    unsigned m = 0;
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        const bool hit = !(mn[c] > __fadd_rn(mx[c], kEps)) && !(front && mx[c] < -kEps) && mn[c] != FLT_MAX;
+        m |= (hit ? 1u : 0u) << c;
+    }
+    if (order & 1) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (order & 2) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (order & 4) m = ((m & 0x0Fu) << 4) | ((m >> 4) & 0x0Fu);
     return m;
 }
 
@@ -234,7 +266,7 @@ __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool cl
     constexpr int GS = group_shift<COUNT>();
     uint32_t stack[kStack];
     int sp = 0;
-    uint32_t cur = ((uint32_t)S.root_child << GS) | test_group(S.nodes, S.root_child, order, o, inv, front);
+    uint32_t cur = ((uint32_t)S.root_child << GS) | test_group(S.gbox, S.root_child, order, o, inv, front);
     if (COUNT) nbox += 8;
     for (;;) {
         uint32_t m = cur & 0xFFu;
@@ -260,7 +292,7 @@ __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool cl
         } else {
             if (sp >= kStack) return false;  // unreachable for trees of depth <= 24
             stack[sp++] = COUNT ? ((cur & ~(7u << 8)) | ((uint32_t)k << 8)) : cur;
-            cur = ((uint32_t)(w >> 3) << GS) | test_group(S.nodes, w >> 3, order, o, inv, front);
+            cur = ((uint32_t)(w >> 3) << GS) | test_group(S.gbox, w >> 3, order, o, inv, front);
             if (COUNT) nbox += 8;
         }
     }
