@@ -199,7 +199,7 @@ def cpu_baseline_ours(S, cam, W, H, depth, seed, spp=(8, 8)):
     paths = px * spp[0] * spp[1]
     return dict(value=paths / dt / 1e6, unit=UNIT, cores=threads, kind="port",
                 sample=f"FP64 oracle, centre patch of 8x12 blocks of {W}x{H} ({px:,} px) x {spp[0] * spp[1]} spp, "
-                       f"depth {depth}, {dt:.1f} s"), (ranges, fb, p)
+                       f"depth {depth}, {dt:.1f} s"), (ranges, fb, p, osc)
 
 
 def run_ours(a):
@@ -347,7 +347,7 @@ def run_ours(a):
             variants[lens] = round(paths_per_frame / (g0.elapsed_time(g1) / 1e3) / 1e6, 3)
         out["lens_variants_mpaths_s"] = variants
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
-        base, (ranges, ofb, p) = cpu_baseline_ours(S, cam, W, H, a.depth, 4321)
+        base, (ranges, ofb, p, osc) = cpu_baseline_ours(S, cam, W, H, a.depth, 4321)
         out["cpu_baseline"] = base
         # accuracy on the same sample: GPU at the same samples vs the FP64 oracle
         gfb = dr.new_frame_buffer(W, H, dev)
@@ -366,6 +366,24 @@ def run_ours(a):
             "mean_rel_diff": float((g.mean() - o.mean()) / max(o.mean(), 1e-9)),
             "mean_diff_in_se": float(diff.mean() / max(diff.std(ddof=1) / np.sqrt(len(diff)), 1e-12)),
             "sample": "centre patch 12,288 px x 64 spp, same seeds"}
+        # converged: 12 blocks (1,536 px) at the centre, 16 progressive iterations of 64 spp (1,024 spp)
+        # on both sides; per-pixel differences from diverging paths average out as 1/sqrt(spp)
+        crng = cpu_sample_ranges(W, H, rows=1, cols=12)
+        ofb2 = np.zeros((nb * 128, 4), np.float32)
+        gfb2 = dr.new_frame_buffer(W, H, dev)
+        threads = os.cpu_count() or 1
+        for it in range(1, 17):
+            pit = dr.render_params(W, H, dr.MODE_PHYSICAL, samples=(8, 8), max_bounces=a.depth, iteration=it, seed=4321)
+            for s0, s1 in crng:
+                osc.render_blocks(cam, pit, fb=ofb2, start=s0, end=s1, threads=threads)
+                rend.render_blocks(scene, cam, gfb2, s0, s1, pit, stream)
+        torch.cuda.synchronize()
+        g2 = np.concatenate([gfb2.cpu().numpy()[s0 * 128:s1 * 128, :3] for s0, s1 in crng]).astype(np.float64)
+        o2 = np.concatenate([ofb2[s0 * 128:s1 * 128, :3] for s0, s1 in crng]).astype(np.float64)
+        out["accuracy_vs_fp64_oracle_converged"] = {
+            "rmse_rel": float(np.sqrt(np.mean((g2 - o2) ** 2)) / max(o2.mean(), 1e-9)),
+            "mean_rel_diff": float((g2.mean() - o2.mean()) / max(o2.mean(), 1e-9)),
+            "sample": "centre row of 12 blocks (1,536 px), 16 iterations x 64 spp = 1,024 spp, same seeds"}
     del rend
     if rank == 0 and world == 1 and not a.no_raycast:
         out["raycast"] = run_raycast(dr, torch, dev, a, peak, peak_src)
