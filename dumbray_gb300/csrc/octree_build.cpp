@@ -11,6 +11,7 @@
 // clipping runs in parallel, every order-sensitive float sum runs serially in list order), so the
 // tree is bit-identical to the reference's on any thread count.  Compile with -ffp-contract=off.
 #include "octree_build.h"
+#include "octree_geom.h"
 
 #include <algorithm>
 #include <array>
@@ -27,176 +28,16 @@ namespace {
 const float kEps = 0.000005f;               // VECTOR_EPSILON (Vector3.h:10)
 const float kBoxEps = 0.000005f * 256.0f;   // OCTREE_AABB_EPSILON (Octree.impl.cuh:3-5)
 
-struct P3 {
-    float x, y, z;
-};
-inline P3 mk(float x, float y, float z) { return P3{x, y, z}; }
-inline P3 add(P3 a, P3 b) { return P3{a.x + b.x, a.y + b.y, a.z + b.z}; }
-inline P3 sub(P3 a, P3 b) { return P3{a.x - b.x, a.y - b.y, a.z - b.z}; }
-inline P3 scale(P3 a, float f) { return P3{a.x * f, a.y * f, a.z * f}; }
-inline P3 divs(P3 a, float f) { float r = 1.0f / f; return P3{a.x * r, a.y * r, a.z * r}; }
-inline P3 crs(P3 a, P3 v) { return P3{a.y * v.z - v.y * a.z, v.x * a.z - a.x * v.z, a.x * v.y - v.x * a.y}; }
-inline float len(P3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
-inline float comp(P3 v, int ax) { return ax == 0 ? v.x : (ax == 1 ? v.y : v.z); }
+using namespace geom;
 
-struct Bx {
-    P3 lo, hi;
-};
-inline Bx fixed_box(P3 s, P3 e) {
-    if (s.x > e.x) std::swap(s.x, e.x);
-    if (s.y > e.y) std::swap(s.y, e.y);
-    if (s.z > e.z) std::swap(s.z, e.z);
-    return Bx{s, e};
-}
-
-struct T3 {
-    P3 a, b, c;
-};
-
-// Vertex order by one axis (Triangle::sortByMases, Triangle.impl.h:183-196).
-inline void order_by(T3 &t, int ax) {
-    float am = comp(t.a, ax), bm = comp(t.b, ax), cm = comp(t.c, ax);
-    if (am > bm) {
-        if (cm > am) std::swap(t.a, t.b);
-        else if (bm > cm) std::swap(t.a, t.c);
-        else { P3 k = t.a; t.a = t.b; t.b = t.c; t.c = k; }
-    } else {
-        if (am > cm) { P3 k = t.a; t.a = t.c; t.c = t.b; t.b = k; }
-        else if (bm > cm) std::swap(t.b, t.c);
-    }
-}
-inline P3 lerp_at(P3 from, P3 to, float fv, float tv, float plane) { return add(from, scale(sub(to, from), (plane - fv) / (tv - fv))); }
-
-// Piecewise slab clipping of one triangle against [s, e] on axis `ax`, emitting pieces through
-// `emit`.  Returns early (true) as soon as `emit` returns true: the same routine serves the
-// exact triangle/box overlap test (AABB::intersectsTri, AABB.impl.h:152-221, which recurses
-// z -> x -> y and stops on the first surviving piece) and the clipping used for intersection
-// centres and bounds (SHAPES_PUSH_INTERSECTIONS, Shapes.impl.cuh:178-262, which keeps all pieces).
-template <class Emit>
-bool slab_clip(T3 t, int ax, float s, float e, Emit &&emit) {
-    order_by(t, ax);
-    float av = comp(t.a, ax), bv = comp(t.b, ax), cv = comp(t.c, ax);
-    if (cv < s || av > e) return false;
-    if (av <= s) {
-        P3 asc = lerp_at(t.a, t.c, av, cv, s);
-        if (bv <= s) {
-            P3 bsc = lerp_at(t.b, t.c, bv, cv, s);
-            if (cv <= e) return emit(T3{asc, bsc, t.c});
-            P3 bec = lerp_at(t.b, t.c, bv, cv, e);
-            if (emit(T3{bsc, bec, asc})) return true;
-            P3 aec = lerp_at(t.a, t.c, av, cv, e);
-            return emit(T3{asc, bec, aec});
-        }
-        if (bv <= e) {
-            if (cv <= e) {
-                if (emit(T3{asc, t.b, t.c})) return true;
-                P3 asb = lerp_at(t.a, t.b, av, bv, s);
-                return emit(T3{asc, asb, t.b});
-            }
-            P3 asb = lerp_at(t.a, t.b, av, bv, s);
-            P3 bec = lerp_at(t.b, t.c, bv, cv, e);
-            if (emit(T3{asb, t.b, bec})) return true;
-            if (emit(T3{asc, asb, bec})) return true;
-            P3 aec = lerp_at(t.a, t.c, av, cv, e);
-            return emit(T3{asc, bec, aec});
-        }
-        P3 asb = lerp_at(t.a, t.b, av, bv, s);
-        P3 aeb = lerp_at(t.a, t.b, av, bv, e);
-        if (emit(T3{asc, asb, aeb})) return true;
-        P3 aec = lerp_at(t.a, t.c, av, cv, e);
-        return emit(T3{asc, aeb, aec});
-    }
-    if (cv <= e) return emit(t);
-    P3 aec = lerp_at(t.a, t.c, av, cv, e);
-    if (bv <= e) {
-        P3 bec = lerp_at(t.b, t.c, bv, cv, e);
-        if (emit(T3{t.a, t.b, bec})) return true;
-        return emit(T3{t.a, aec, bec});
-    }
-    P3 aeb = lerp_at(t.a, t.b, av, bv, e);
-    return emit(T3{t.a, aeb, aec});
-}
-
-// Exact triangle/box overlap: axes z, then x, then y.
-bool overlaps(const Bx &b, const T3 &t) {
-    auto ylevel = [&](const T3 &p) { return slab_clip(p, 1, b.lo.y, b.hi.y, [](const T3 &) { return true; }); };
-    auto xlevel = [&](const T3 &p) { return slab_clip(p, 0, b.lo.x, b.hi.x, ylevel); };
-    return slab_clip(t, 2, b.lo.z, b.hi.z, xlevel);
-}
-
-// All pieces of t inside b (x, then y, then z), in the reference's order.
-struct Pieces {
-    T3 p[32];
-    int n = 0;
-};
-void clip_all(const Bx &b, const T3 &t, Pieces &out) {
-    Pieces x, y;
-    slab_clip(t, 0, b.lo.x, b.hi.x, [&](const T3 &p) { if (x.n < 32) x.p[x.n++] = p; return false; });
-    for (int i = 0; i < x.n; i++)
-        slab_clip(x.p[i], 1, b.lo.y, b.hi.y, [&](const T3 &p) { if (y.n < 32) y.p[y.n++] = p; return false; });
-    out.n = 0;
-    for (int i = 0; i < y.n; i++)
-        slab_clip(y.p[i], 2, b.lo.z, b.hi.z, [&](const T3 &p) { if (out.n < 32) out.p[out.n++] = p; return false; });
-}
-
-// Area-weighted centre of the clipped pieces (Shapes.impl.cuh:289-310).
+// Host wrappers with their own scratch.
 P3 clipped_centre(const Bx &b, const T3 &t) {
-    Pieces l;
-    clip_all(b, t, l);
-    if (l.n == 0) return divs(add(b.lo, b.hi), 2.0f);
-    float total = 0.0f;
-    P3 acc = mk(0, 0, 0);
-    for (int i = 0; i < l.n; i++) {
-        const T3 &p = l.p[i];
-        float w = len(crs(sub(p.b, p.a), sub(p.c, p.a))) * 0.5f + 0.0001f;
-        acc = add(acc, scale(divs(add(add(p.a, p.b), p.c), 3.0f), w));
-        total += w;
-    }
-    return divs(acc, total);
+    Pieces l, x, y;
+    return geom::clipped_centre(b, t, l, x, y);
 }
-
-// Bounds of the clipped pieces (Shapes.impl.cuh:265-287).
 Bx clipped_bounds(const Bx &b, const T3 &t) {
-    Pieces l;
-    clip_all(b, t, l);
-    if (l.n == 0) return b;
-    P3 lo = b.hi, hi = b.lo;
-    for (int i = 0; i < l.n; i++) {
-        const T3 &p = l.p[i];
-        const P3 v[3] = {p.a, p.b, p.c};
-        for (int k = 0; k < 3; k++) {
-            hi = mk(hi.x > v[k].x ? hi.x : v[k].x, hi.y > v[k].y ? hi.y : v[k].y, hi.z > v[k].z ? hi.z : v[k].z);
-        }
-        for (int k = 0; k < 3; k++) {
-            lo = mk(lo.x < v[k].x ? lo.x : v[k].x, lo.y < v[k].y ? lo.y : v[k].y, lo.z < v[k].z ? lo.z : v[k].z);
-        }
-    }
-    return fixed_box(lo, hi);
-}
-
-// The 8 overlapping octants around `c` (splitAABB, Octree.impl.cuh:423-434); child index
-// bit 2 = upper x, bit 1 = upper y, bit 0 = upper z.
-void octants(const Bx &b, P3 c, Bx *r, float E) {
-    for (int i = 0; i < 8; i++) {
-        P3 lo, hi;
-        lo.x = (i & 4) ? c.x - E : b.lo.x;
-        hi.x = (i & 4) ? b.hi.x : c.x + E;
-        lo.y = (i & 2) ? c.y - E : b.lo.y;
-        hi.y = (i & 2) ? b.hi.y : c.y + E;
-        lo.z = (i & 1) ? c.z - E : b.lo.z;
-        hi.z = (i & 1) ? b.hi.z : c.z + E;
-        r[i] = fixed_box(lo, hi);
-    }
-}
-
-// Shrink a node box to `lo..hi` padded by the octree epsilon, clamped to the old box
-// (reduceNode tail, Octree.impl.cuh:526-532).
-Bx shrink(const Bx &old, P3 lo, P3 hi, float E) {
-    lo = sub(lo, mk(E, E, E));
-    hi = add(hi, mk(E, E, E));
-    lo = mk(std::fmax(lo.x, old.lo.x), std::fmax(lo.y, old.lo.y), std::fmax(lo.z, old.lo.z));
-    hi = mk(std::fmin(hi.x, old.hi.x), std::fmin(hi.y, old.hi.y), std::fmin(hi.z, old.hi.z));
-    return fixed_box(lo, hi);
+    Pieces l, x, y;
+    return geom::clipped_bounds(b, t, l, x, y);
 }
 
 void parallel_for(int64_t n, int threads, const std::function<void(int64_t, int64_t)> &fn) {
@@ -240,12 +81,7 @@ bool build_octree(const float *xyz, int64_t n, const BuildOptions &opt, FlatOctr
     // triangle's box is taken unpadded (push, Octree.impl.cuh:97-111).
     Bx root;
     for (int64_t i = 0; i < n; i++) {
-        T3 t = tri((int32_t)i);
-        P3 lo = mk(t.a.x < t.b.x ? t.a.x : t.b.x, t.a.y < t.b.y ? t.a.y : t.b.y, t.a.z < t.b.z ? t.a.z : t.b.z);
-        lo = mk(lo.x < t.c.x ? lo.x : t.c.x, lo.y < t.c.y ? lo.y : t.c.y, lo.z < t.c.z ? lo.z : t.c.z);
-        P3 hi = mk(t.a.x > t.b.x ? t.a.x : t.b.x, t.a.y > t.b.y ? t.a.y : t.b.y, t.a.z > t.b.z ? t.a.z : t.b.z);
-        hi = mk(hi.x > t.c.x ? hi.x : t.c.x, hi.y > t.c.y ? hi.y : t.c.y, hi.z > t.c.z ? hi.z : t.c.z);
-        Bx b = fixed_box(lo, hi);
+        Bx b = tri_box(tri((int32_t)i));
         if (i == 0) root = b;
         else {
             P3 bl = sub(b.lo, mk(E, E, E)), bh = add(b.hi, mk(E, E, E));
