@@ -40,7 +40,7 @@ _F3 = ctypes.c_float * 3
 
 class DrBuildParams(ctypes.Structure):
     _fields_ = [("max_depth", ctypes.c_int32), ("split_threshold", ctypes.c_int32), ("threads", ctypes.c_int32),
-                ("box_epsilon", ctypes.c_float)]
+                ("box_epsilon", ctypes.c_float), ("device_build", ctypes.c_int32)]
 
 
 class DrMaterial(ctypes.Structure):
@@ -344,7 +344,7 @@ class Scene:
     up to float32 near-ties, with far fewer duplicated leaf references on finely tessellated meshes."""
 
     def __init__(self, tris, normals=None, mat_id=None, materials=(), lights=(), max_depth=0, split_threshold=0,
-                 threads=0, box_epsilon=0.0):
+                 threads=0, box_epsilon=0.0, device_build=False):
         L = lib()
         self.tris = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 3, 3)
         self.n = len(self.tris)
@@ -355,7 +355,7 @@ class Scene:
         self.materials, self.lights = mats, lts
         marr = (DrMaterial * max(1, len(mats)))(*mats)
         larr = (DrLight * max(1, len(lts)))(*lts)
-        bp = DrBuildParams(max_depth, split_threshold, threads, box_epsilon)
+        bp = DrBuildParams(max_depth, split_threshold, threads, box_epsilon, 1 if device_build else 0)
         h = ctypes.c_void_p()
         check(L.dr_scene_create(self.tris.ctypes.data, None if self._nrm is None else self._nrm.ctypes.data,
                                 None if self._mat is None else self._mat.ctypes.data, self.n,
@@ -416,12 +416,12 @@ def tight_box_epsilon(tris) -> float:
     return max(m, 1e-30) * 2.0 ** -18
 
 
-def build_octree_host(tris, max_depth=0, split_threshold=0, threads=0, box_epsilon=0.0):
+def build_octree_host(tris, max_depth=0, split_threshold=0, threads=0, box_epsilon=0.0, device_build=False):
     """Host-only octree build (dr_octree_create_host); returns (stats, box, child, leaf, refs) with
     node 0 = root, as dr_scene_export_tree."""
     L = lib()
     t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 3, 3)
-    bp = DrBuildParams(max_depth, split_threshold, threads, box_epsilon)
+    bp = DrBuildParams(max_depth, split_threshold, threads, box_epsilon, 1 if device_build else 0)
     h = ctypes.c_void_p()
     check(L.dr_octree_create_host(t.ctypes.data, len(t), ctypes.byref(bp), ctypes.byref(h)))
     try:

@@ -237,10 +237,13 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
         if (bp->split_threshold > 0) opt.split_threshold = bp->split_threshold;
         opt.threads = bp->threads;
         opt.box_eps = bp->box_epsilon;
+        opt.device = bp->device_build != 0;
     }
-    if (!drb::build_octree(sc->xyz.data(), n, opt, sc->tree)) {
+    std::string berr;
+    if (!(opt.device ? drb::build_octree_gpu(sc->xyz.data(), n, opt, sc->tree, berr)
+                     : drb::build_octree(sc->xyz.data(), n, opt, sc->tree))) {
         delete sc;
-        return fail(DR_E_ARG, "dr_scene_create: octree build failed");
+        return fail(opt.device ? DR_E_CUDA : DR_E_ARG, "dr_scene_create: octree build failed" + (berr.empty() ? std::string() : ": " + berr));
     }
     const drb::FlatOctree &T = sc->tree;
     if (T.node_count >= (int64_t(1) << 24)) {
@@ -437,10 +440,12 @@ dr_status dr_octree_create_host(const float *xyz, int32_t n, const dr_build_para
         if (bp->split_threshold > 0) opt.split_threshold = bp->split_threshold;
         opt.threads = bp->threads;
         opt.box_eps = bp->box_epsilon;
+        opt.device = bp->device_build != 0;
     }
-    if (!drb::build_octree(xyz, n, opt, t->tree)) {
+    std::string berr;
+    if (!(opt.device ? drb::build_octree_gpu(xyz, n, opt, t->tree, berr) : drb::build_octree(xyz, n, opt, t->tree))) {
         delete t;
-        return fail(DR_E_ARG, "dr_octree_create_host: build failed");
+        return fail(opt.device ? DR_E_CUDA : DR_E_ARG, "dr_octree_create_host: build failed" + (berr.empty() ? std::string() : ": " + berr));
     }
     *out = t;
     return DR_OK;

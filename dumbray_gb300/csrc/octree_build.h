@@ -1,6 +1,7 @@
 // octree_build.h - host octree builder (flat, BFS-ordered output) for the GB300 ray caster.
 #pragma once
 #include <cstdint>
+#include <string>
 #include <vector>
 
 namespace drb {
@@ -14,6 +15,7 @@ struct BuildOptions {
     // < 0 = 2^-18 x the largest absolute coordinate.  The closest hit does not depend on it (up to
     // exact ties), so physical-mode scenes may use a value scaled to the coordinates.
     float box_eps = 0.0f;
+    bool device = false;       // build on the GPU (build_octree_gpu), same tree
 };
 
 // Flattened octree.  The root is stored separately; the children of an inner node are 8
@@ -36,5 +38,9 @@ struct FlatOctree {
 
 // xyz: float[n][3][3].  Returns false on invalid input.
 bool build_octree(const float *xyz, int64_t n, const BuildOptions &opt, FlatOctree &out);
+
+// The same build on the current CUDA device (octree_gpu.cu): per-reference clipping and per-node
+// passes on the GPU, level bookkeeping on the host; bit-identical output.  err: reason on failure.
+bool build_octree_gpu(const float *xyz, int64_t n, const BuildOptions &opt, FlatOctree &out, std::string &err);
 
 }  // namespace drb

@@ -55,6 +55,9 @@ typedef struct {
     int32_t split_threshold;
     int32_t threads;
     float box_epsilon;
+    /* 1: build on the current CUDA device (per-reference clipping and per-node passes on the GPU,
+     * level bookkeeping on the host); the tree is bit-identical to the host build.  0: host threads. */
+    int32_t device_build;
 } dr_build_params;
 
 /* ---- materials --------------------------------------------------------------------------
