@@ -94,7 +94,7 @@ def build_scene(dr, level, split=0, ref_tree=False):
     S["box_epsilon"] = 0.0 if ref_tree else dr.tight_box_epsilon(S["tris"])
     S["split"] = split if split > 0 else 8
     scene = dr.Scene(S["tris"], mat_id=S["mat_id"], materials=mats, split_threshold=S["split"],
-                     box_epsilon=0.0 if ref_tree else dr.PHYSICAL_TREE)
+                     box_epsilon=0.0 if ref_tree else dr.PHYSICAL_TREE, device_build=True)
     scene.set_triangle_params(S["albedo"], S["emission"], S["roughness"])
     return S, scene, time.time() - t0
 
@@ -169,6 +169,20 @@ def measured_peak():
         except (KeyError, ValueError):
             pass
     return 6800.0, "fallback"
+
+
+def octree_build_times(dr, S):
+    """Wall time of the octree build alone (dr_octree_create_host + export) on the host threads and on
+    the GPU (device_build, same tree), for the path-trace scene's parameters."""
+    out = {}
+    for name, dev in (("host_threads", False), ("device", True)):
+        dr.build_octree_host(S["tris"][:1000], device_build=dev)   # warm-up (allocator, first launch)
+        t0 = time.time()
+        st = dr.build_octree_host(S["tris"], split_threshold=S["split"], box_epsilon=S["box_epsilon"],
+                                  device_build=dev)[0]
+        out[name] = round(time.time() - t0, 3)
+    out.update(cores=os.cpu_count() or 1, nodes=st["nodes"], leaf_refs=st["refs"])
+    return out
 
 
 def cpu_sample_ranges(W, H, rows=8, cols=12):
@@ -313,6 +327,7 @@ def run_ours(a):
                    "lens": a.lens, "mode": "physical", "wave_paths": a.wave, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (scene ~0.3 GB, wavefront queues ~2 GB), no flush",
                    "scene_build_s": round(build_s, 2),
+                   "octree_build_s": octree_build_times(dr, S),
                    "octree": {"split_threshold": S["split"], "box_epsilon": S["box_epsilon"] or 1.28e-3,
                               "rule": "reference split rule; " + ("reference padding" if a.ref_tree else
                                       "physical-mode padding 2^-18 x max |coordinate|")}},
@@ -399,7 +414,7 @@ def run_ours(a):
 
 def _batch_scene(dr, job, split=0):
     sc = dr.Scene(job["tris"], mat_id=job["mat_id"], materials=[dr.lambert(), dr.mirror(), dr.glossy()],
-                  split_threshold=split, box_epsilon=dr.PHYSICAL_TREE)
+                  split_threshold=split, box_epsilon=dr.PHYSICAL_TREE, device_build=True)
     sc.set_triangle_params(job["albedo"], job["emission"], job["roughness"])
     return sc
 
