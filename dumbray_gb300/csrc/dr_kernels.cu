@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(Wave
     uint32_t stack[kStack];
     __shared__ WarpLeafSlots slots[kTraceThreads / 32];
     TraceSource<MULTI> src{&A, A.q[b & 1], A.hits, &C->fetch_trace[b], n, chunk_for(n), 0, 0, 0};
-    trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5]);
+    trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5], A.inl.S.front_only ? 2 : 1);
     if (COUNT) count_add64(A.counters, src.rays, src.nb, src.nt);
 }
 
@@ -736,7 +736,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_shadow_phy
     uint32_t stack[kStack];
     __shared__ WarpLeafSlots slots[kTraceThreads / 32];
     ShadowPhysSource<MULTI, ADJ> src{&A, A.sq, A.accum, &C->fetch_shadow[b], n, chunk_for(n), 0, 0, 0};
-    trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5]);
+    trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5], A.inl.S.front_only ? 2 : 1);
     if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
 }
 

@@ -85,7 +85,11 @@ struct WarpLeafSlots {
 // takes its scene's root (bounds, child group or root leaf) when it starts a ray.  Backface culling
 // is uniform over a wave in both cases.
 template <bool COUNT, bool MULTI, class Source>
-__device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, uint32_t *stack, WarpLeafSlots &ws) {
+// steps_per_round: traversal steps a lane may take between two cooperative leaf rounds while it
+// stays in inner nodes; more means fewer per-round ballots and prefix sums, but lanes that reached a
+// leaf wait longer (measured: 2 pays on physical-tree scenes, whose leaves are small; 1 elsewhere).
+__device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, uint32_t *stack, WarpLeafSlots &ws,
+                                                 int steps_per_round = 1) {
     const unsigned lane = threadIdx.x & 31u;
     const unsigned lt_mask = (1u << lane) - 1u;
     int c_next = 0, c_end = 0;
@@ -124,7 +128,10 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
             if (drained) break;
             continue;
         }
-        if (mode == kTrav) {
+#pragma unroll 1
+        for (int step = 0; step < steps_per_round; step++) {
+        if (mode != kTrav) break;
+        {
             // ---- one traversal step: pop empty frames, then take one child
             while ((L.cur & 0xFFu) == 0u && L.sp > 0) L.cur = stack[--L.sp];
             uint32_t m = L.cur & 0xFFu;
@@ -158,6 +165,7 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
                     L.sp = 0;
                 }
             }
+        }
         }
         // ---- one cooperative round of leaf triangle tests (castInLeaf)
         int pending = (mode == kLeaf) ? (L.r_end - L.r) : 0;
