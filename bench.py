@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable (adjoint) leg")
     ap.add_argument("--no-raycast", action="store_true", help="skip the ray-cast microbenchmark leg")
+    ap.add_argument("--no-twin", action="store_true", help="skip the reference-mode twin leg")
     ap.add_argument("--split", type=int, default=12,
                     help="octree leaf split threshold of the path-trace scene (12: best of 8/12/16/24 on this "
                          "workload with the physical-mode padding; the reference uses 8)")
@@ -402,6 +403,8 @@ def run_ours(a):
     del rend
     if rank == 0 and world == 1 and not a.no_raycast:
         out["raycast"] = run_raycast(dr, torch, dev, a, peak, peak_src)
+    if rank == 0 and world == 1 and not a.no_twin:
+        out["reference_mode_twin"] = run_reference_twin_gpu(dr, torch, dev, a, S)
     if rank == 0 and world == 1 and not a.no_batched:
         out["batched"] = run_batched(dr, torch, dev, a)
     if rank == 0 and world == 1 and not a.no_adjoint:
@@ -428,6 +431,41 @@ def _events_ms(torch, fn, steps):
     e1.record()
     torch.cuda.synchronize()
     return e0.elapsed_time(e1)
+
+
+def run_reference_twin_gpu(dr, torch, dev, a, S):
+    """The workload of the reference arm (the reference-expressible twin of the path-trace scene:
+    DumbBased / SimpleStochastic materials, 4 spherical lights, SimpleStochasticLense 60 degrees from
+    (0, 0.6, -3.4), depth a.depth) rendered in reference mode (DumbRenderer's estimator) on the
+    reference's octree, as a full 1920x1080 frame at 1 spp per step; same unit as the reference
+    arm, which times a 240x136 sample of that frame on the host cores."""
+    tris, mat, mats, lights = reference_twin(S, dr)
+    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights, device_build=True)
+    cam = dr.camera(dr.LENS_SIMPLE_STOCHASTIC, position=(0.0, 0.6, -3.4), angle=60.0)
+    W, H = 1920, 1080
+    nb = dr.block_count(W, H)
+    fb = dr.new_frame_buffer(W, H, dev)
+    rend = dr.Renderer(a.wave)
+
+    def step(i):
+        rend.render_blocks(sc, cam, fb, 0, nb, dr.render_params(W, H, dr.MODE_REFERENCE, samples=(1, 1),
+                                                                 max_bounces=a.depth, iteration=1 + i, seed=77))
+
+    for i in range(3):
+        step(i)
+    K = max(3, a.steps)
+    ms = _events_ms(torch, lambda i: step(3 + i), K) / K
+    rend.set_profiling(True)
+    step(3 + K)
+    torch.cuda.synchronize()
+    kt = rend.kernel_times()
+    rend.set_profiling(False)
+    rend.close()
+    sc.close()
+    return {"kernel_ms_per_frame": {k: round(v[0], 2) for k, v in kt.items()},
+            "workload": f"reference-expressible twin ({len(tris):,} tris, {len(lights)} spherical lights), reference mode, "
+                        f"{W}x{H} x 1 spp, depth {a.depth}, reference octree",
+            "ms_per_frame": round(ms, 3), "mpaths_s": round(W * H / (ms / 1e3) / 1e6, 2)}
 
 
 def run_raycast(dr, torch, dev, a, peak, peak_src):
