@@ -128,12 +128,20 @@ __global__ void __launch_bounds__(128) k_cast(Scene S, const float *__restrict__
 
 // ---------------------------------------------------------------------------------------------
 // Wave control block (int slots, zeroed at the start of every wave).
+// Engine passes over reference photons per bounce; chains still going after them finish one photon
+// per lane (k_photon_chain).
+constexpr int kPhotonPasses = 4;
+
 struct Ctrl {
     int ray_count[kMaxBounceSlots];
     int shadow_count[kMaxBounceSlots];
     int fetch_trace[kMaxBounceSlots];
     int fetch_shade[kMaxBounceSlots];
     int fetch_shadow[kMaxBounceSlots];
+    // reference photons continuing through blockers: per bounce and engine pass, the list length
+    // (pass p reads list p, written by pass p - 1; list 0 is the shadow queue itself) and its fetch
+    int photon_count[kMaxBounceSlots][kPhotonPasses + 1];
+    int photon_fetch[kMaxBounceSlots][kPhotonPasses + 1];
     int fetch_camera;
     int error;
 };
@@ -435,16 +443,94 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
 // Reference light visibility (DumbRenderer.cu:361-428): cast from the light sample toward the
 // point; it counts if the first hit is the shaded triangle or lies within sqrt(8 eps) of the
 // point; otherwise the blocker's reflected colour decides whether the photon continues.
+//
+// Every cast of a photon runs on the persistent traversal engine (RefPhotonSource), in passes: pass
+// 0 over the shadow queue, pass p over the photons that pass p - 1 sent on through a blocker.  A
+// continuing photon has its own queue record rewritten in place (its lane has already loaded it):
+// origin just past the blocker, colour attenuated, blocker as the ignored object; its index goes to
+// the next pass's list.  Lists alternate between the hits buffer and the p3 plane of the ray queue
+// this bounce has consumed (both idle during this phase).  Photons still going after the last pass
+// finish in k_photon_chain, one per lane, as the reference's loop does.
+__device__ __forceinline__ bool photon_arrives(const Hit &h, int target, f3 hp) {
+    const f3 dd = xsub(h.p, hp);
+    return h.tri == target || xdot(dd, dd) <= (8.0f * kEps);
+}
+
+__device__ __forceinline__ int *photon_list(const WaveArgs &A, int b, int pass) {
+    return (pass & 1) ? reinterpret_cast<int *>(A.hits) : reinterpret_cast<int *>(A.q[b & 1].p3);
+}
+
+template <bool MULTI>
+struct RefPhotonSource {
+    const WaveArgs *A;
+    ShadowQ sq;
+    int *fetch, *out_count, *out_list;
+    const int *in_list;   // nullptr: the shadow queue itself
+    int n, chunk;
+    long long rays, nb, nt;
+    __device__ __forceinline__ int rec(int i) const { return in_list ? in_list[i] : i; }
+    __device__ __forceinline__ bool next(int &b, int &e) { return fetch_chunk(fetch, n, chunk, b, e); }
+    __device__ __forceinline__ void load(int i, f3 &o, f3 &d, int &ign, int &job) {
+        const int r = rec(i);
+        o = f3of(sq.s0[r]);
+        d = f3of(sq.s1[r]);
+        ign = __float_as_int(sq.s2[r].w);
+        job = __float_as_int(sq.s4[r].w);
+    }
+    __device__ __forceinline__ const Scene &scene(int job) { return job_of<MULTI>(*A, job).S; }
+    __device__ __forceinline__ bool clip(int job) { return job_of<MULTI>(*A, job).clip != 0; }
+    __device__ __forceinline__ void store(int i, const Hit &h, int b_, int t_) {
+        rays++;
+        nb += b_;
+        nt += t_;
+        if (h.tri < 0) return;
+        const int r = rec(i);
+        const float4 s0 = sq.s0[r], s1 = sq.s1[r], s2 = sq.s2[r], s3 = sq.s3[r], s4 = sq.s4[r];
+        const c3 lc = mkc(s3.x, s3.y, s3.z);
+        if (photon_arrives(h, __float_as_int(s1.w), f3of(s2))) {
+            accum_add(A->accum, __float_as_int(s0.w), mkc(s4.x * lc.r, s4.y * lc.g, s4.z * lc.b));
+            return;
+        }
+        const Scene &S = job_of<MULTI>(*A, __float_as_int(s4.w)).S;
+        const f3 ld = f3of(s1);
+        const c3 tr = cmul(ref_reflect(S, h.tri, h.p, ld, ld, true, 0), lc);
+        if ((tr.r + tr.g + tr.b) > kEps) {
+            const f3 lo = add3(h.p, mul3(norm3(ld), 64.0f * kEps));
+            sq.s0[r] = make_float4(lo.x, lo.y, lo.z, s0.w);
+            sq.s2[r] = make_float4(s2.x, s2.y, s2.z, __int_as_float(h.tri));
+            sq.s3[r] = make_float4(tr.r, tr.g, tr.b, s3.w);
+            out_list[atomicAdd(out_count, 1)] = r;
+        }
+    }
+};
+
 template <bool COUNT, bool MULTI>
-__global__ void __launch_bounds__(256) k_shadow_ref(WaveArgs A, int b) {
+__global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_shadow_ref(WaveArgs A, int b, int pass) {
     Ctrl *C = A.ctrl;
-    const int n = *((volatile int *)&C->shadow_count[b]);
+    const int n = pass == 0 ? *((volatile int *)&C->shadow_count[b]) : *((volatile int *)&C->photon_count[b][pass]);
+    if (n == 0) return;
+    uint32_t stack[kStack];
+    __shared__ WarpLeafSlots slots[kTraceThreads / 32];
+    RefPhotonSource<MULTI> src{&A, A.sq, pass == 0 ? &C->fetch_shadow[b] : &C->photon_fetch[b][pass],
+                               &C->photon_count[b][pass + 1], photon_list(A, b, pass + 1),
+                               pass == 0 ? nullptr : photon_list(A, b, pass), n, chunk_for(n), 0, 0, 0};
+    trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5]);
+    if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
+}
+
+// Chains still going after the engine passes: one photon per lane, from its rewritten record.
+template <bool COUNT, bool MULTI>
+__global__ void __launch_bounds__(256) k_photon_chain(WaveArgs A, int b) {
+    Ctrl *C = A.ctrl;
+    const int n = *((volatile int *)&C->photon_count[b][kPhotonPasses]);
+    const int *chain = photon_list(A, b, kPhotonPasses);
     for (;;) {
-        int base = warp_fetch(&C->fetch_shadow[b]);
+        int base = warp_fetch(&C->photon_fetch[b][kPhotonPasses]);
         if (base >= n) break;
-        int i = base + (int)lane_id();
+        int j = base + (int)lane_id();
         int casts = 0, nb = 0, nt = 0;
-        if (i < n) {
+        if (j < n) {
+            const int i = chain[j];
             float4 s0 = A.sq.s0[i], s1 = A.sq.s1[i], s2 = A.sq.s2[i], s3 = A.sq.s3[i], s4 = A.sq.s4[i];
             const Item &I = job_of<MULTI>(A, __float_as_int(s4.w));
             const Scene &S = I.S;
@@ -453,14 +539,13 @@ __global__ void __launch_bounds__(256) k_shadow_ref(WaveArgs A, int b) {
             int target = __float_as_int(s1.w);
             int slot = __float_as_int(s0.w);
             c3 lc = mkc(s3.x, s3.y, s3.z);
-            int restrict_obj = -1;
-            for (int guard = 0; guard < 64; guard++) {
+            int restrict_obj = __float_as_int(s2.w);
+            for (int guard = kPhotonPasses; guard < 64; guard++) {   // casts 0 .. kPhotonPasses-1 were the passes'
                 Hit h;
                 casts++;
                 cast_closest<COUNT>(S, lo, ld, clip, restrict_obj, h, nb, nt);
                 if (h.tri < 0) break;
-                f3 dd = xsub(h.p, hp);
-                if (h.tri == target || xdot(dd, dd) <= (8.0f * kEps)) {
+                if (photon_arrives(h, target, hp)) {
                     accum_add(A.accum, slot, mkc(s4.x * lc.r, s4.y * lc.g, s4.z * lc.b));
                     break;
                 }
@@ -918,8 +1003,13 @@ static void launch_wave_t(const WaveDesc &W, const WaveArgs &A, cudaStream_t str
         P.end(KC_SHADE, stream);
         P.begin(KC_SHADOW, stream);
         if (W.mode == DR_MODE_REFERENCE) {
-            if (count) k_shadow_ref<true, MULTI><<<grid, 256, 0, stream>>>(A, b);
-            else k_shadow_ref<false, MULTI><<<grid, 256, 0, stream>>>(A, b);
+            for (int pass = 0; pass < kPhotonPasses; pass++) {
+                if (count) k_shadow_ref<true, MULTI><<<tgrid, kTraceThreads, 0, stream>>>(A, b, pass);
+                else k_shadow_ref<false, MULTI><<<tgrid, kTraceThreads, 0, stream>>>(A, b, pass);
+            }
+            if (count) k_photon_chain<true, MULTI><<<grid, 256, 0, stream>>>(A, b);
+            else k_photon_chain<false, MULTI><<<grid, 256, 0, stream>>>(A, b);
+            nl += kPhotonPasses;
         } else if (W.adjoint) {
             k_shadow_phys<false, MULTI, true><<<tgrid, kTraceThreads, 0, stream>>>(A, b);
         } else {
