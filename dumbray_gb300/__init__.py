@@ -57,7 +57,7 @@ class DrLight(ctypes.Structure):
 class DrCamera(ctypes.Structure):
     _fields_ = [("lens", ctypes.c_int32), ("angle", ctypes.c_float * 2), ("focal_distance", ctypes.c_float),
                 ("softness", ctypes.c_float), ("filter", _F3), ("position", _F3), ("right", _F3), ("up", _F3),
-                ("forward", _F3)]
+                ("forward", _F3), ("origin_rows", ctypes.c_int32), ("row_x", _F3), ("row_y", _F3), ("row_z", _F3)]
 
 
 class DrRenderParams(ctypes.Structure):
@@ -169,6 +169,24 @@ def lib() -> ctypes.CDLL:
     L.dr_mesh_file_object_data.argtypes = [vp, i32, vp, vp, vp]
     L.dr_mesh_file_destroy.restype = None
     L.dr_mesh_file_destroy.argtypes = [vp]
+    L.dr_scene_file_load.restype = i32
+    L.dr_scene_file_load.argtypes = [ctypes.c_char_p, P(vp)]
+    L.dr_scene_file_counts.restype = i32
+    L.dr_scene_file_counts.argtypes = [vp, vp]
+    L.dr_scene_file_geometry.restype = i32
+    L.dr_scene_file_geometry.argtypes = [vp, vp, vp, vp]
+    L.dr_scene_file_materials.restype = i32
+    L.dr_scene_file_materials.argtypes = [vp, vp]
+    L.dr_scene_file_lights.restype = i32
+    L.dr_scene_file_lights.argtypes = [vp, vp]
+    L.dr_scene_file_camera.restype = i32
+    L.dr_scene_file_camera.argtypes = [vp, vp]
+    L.dr_scene_file_render_params.restype = i32
+    L.dr_scene_file_render_params.argtypes = [vp, vp]
+    L.dr_scene_file_create_scene.restype = i32
+    L.dr_scene_file_create_scene.argtypes = [vp, vp, P(vp)]
+    L.dr_scene_file_destroy.restype = None
+    L.dr_scene_file_destroy.argtypes = [vp]
     L.dr_progressive_create.restype = i32
     L.dr_progressive_create.argtypes = [vp, vp, vp, i32, P(vp)]
     L.dr_progressive_set_target.restype = i32
@@ -808,6 +826,54 @@ class Progressive:
 
 
 # ---- OBJ meshes (host) -----------------------------------------------------------------------
+
+class SceneFile:
+    """A DumbRay scene file (.dumb) read by dr_scene_file_load, like DumbRenderContext::fromFile:
+    triangles in push order (``tris``, per-corner ``normals``, ``mat_id``), ``materials``, ``lights``,
+    the file's ``camera`` and reference-mode ``params`` (width / height left 0)."""
+
+    def __init__(self, path):
+        L = lib()
+        h = ctypes.c_void_p()
+        check(L.dr_scene_file_load(str(path).encode(), ctypes.byref(h)))
+        try:
+            counts = np.zeros(3, np.int32)
+            check(L.dr_scene_file_counts(h, counts.ctypes.data))
+            n, nm, nl = (int(c) for c in counts)
+            self.tris = np.zeros((n, 3, 3), np.float32)
+            self.normals = np.zeros((n, 3, 3), np.float32)
+            self.mat_id = np.zeros(n, np.int32)
+            check(L.dr_scene_file_geometry(h, self.tris.ctypes.data, self.normals.ctypes.data, self.mat_id.ctypes.data))
+            marr = (DrMaterial * max(1, nm))()
+            larr = (DrLight * max(1, nl))()
+            if nm:
+                check(L.dr_scene_file_materials(h, ctypes.addressof(marr)))
+            if nl:
+                check(L.dr_scene_file_lights(h, ctypes.addressof(larr)))
+            self.materials = [marr[i] for i in range(nm)]
+            self.lights = [larr[i] for i in range(nl)]
+            self.camera = DrCamera()
+            check(L.dr_scene_file_camera(h, ctypes.byref(self.camera)))
+            self.params = DrRenderParams()
+            check(L.dr_scene_file_render_params(h, ctypes.byref(self.params)))
+        finally:
+            L.dr_scene_file_destroy(h)
+
+    def render_params(self, width, height, iteration=1, seed=0) -> DrRenderParams:
+        p = DrRenderParams.from_buffer_copy(self.params)
+        p.width, p.height, p.iteration, p.seed = width, height, iteration, seed
+        return p
+
+    def scene(self, **build) -> "Scene":
+        """The octree scene over the file's geometry (DumbRenderContext::buildFromFile); ``build``
+        takes Scene's build keywords."""
+        return Scene(self.tris, normals=self.normals, mat_id=self.mat_id, materials=self.materials,
+                     lights=self.lights, **build)
+
+
+def load_scene_file(path) -> SceneFile:
+    return SceneFile(path)
+
 
 def read_obj(path):
     """dr_obj_read: {object name: (xyz [n,3,3], normals [n,3,3], uv [n,3,3])} in file order, read with

@@ -200,7 +200,7 @@ extern "C" {
 
 const char *dr_last_error(void) { return g_err.c_str(); }
 
-int32_t dr_version(void) { return 100; }
+int32_t dr_version(void) { return 200; }
 
 int32_t dr_block_count(int32_t width, int32_t height) {
     if (width <= 0 || height <= 0) return 0;

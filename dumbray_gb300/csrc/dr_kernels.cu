@@ -244,7 +244,12 @@ __device__ inline bool lens_ray(const Item &I, int x, int y, int s, uint32_t key
         o = f3{c.position[0], c.position[1], c.position[2]};
         return true;
     }
-    o = add3(cam_to_world(c, o), f3{c.position[0], c.position[1], c.position[2]});
+    if (c.origin_rows)
+        o = f3{o.x * c.row_x[0] + o.y * c.row_x[1] + o.z * c.row_x[2] + c.position[0],
+               o.x * c.row_y[0] + o.y * c.row_y[1] + o.z * c.row_y[2] + c.position[1],
+               o.x * c.row_z[0] + o.y * c.row_z[1] + o.z * c.row_z[2] + c.position[2]};
+    else
+        o = add3(cam_to_world(c, o), f3{c.position[0], c.position[1], c.position[2]});
     d = cam_to_world(c, d);
     return true;
 }

@@ -114,7 +114,13 @@ typedef struct {
  *   DR_LENS_FISHEYE   equidistant fisheye, angle[0] = full field of view across the image height
  *   DR_LENS_SPHERICAL latitude/longitude, angle[0] x angle[1] degrees per unit screen space
  * Camera space is +x right, +y up, +z forward; world direction = x*right + y*up + z*forward,
- * origin = position + (lens origin expressed in the same basis). */
+ * origin = position + (lens origin expressed in the same basis).
+ * origin_rows = 1 maps lens origins the way the reference's Camera does (Camera.impl.cuh:7-10,
+ * `ray >>= transform`; Transform.impl.h:84-90): o -> (o.row_x, o.row_y, o.row_z) + position, while
+ * directions keep the right / up / forward combination (Transform::direction, Transform.impl.h:166).
+ * The two differ for a rotated camera (the rows are the transpose of the direction basis, times the
+ * scale); only the spherical-segment lens has origins off the camera position.  Zero-initialised
+ * cameras keep the basis mapping. */
 #define DR_LENS_DEFAULT_PERSPECTIVE 0
 #define DR_LENS_SIMPLE_STOCHASTIC 1
 #define DR_LENS_SPHERICAL_SEGMENT 2
@@ -132,6 +138,10 @@ typedef struct {
     float right[3];
     float up[3];
     float forward[3];
+    int32_t origin_rows;
+    float row_x[3];
+    float row_y[3];
+    float row_z[3];
 } dr_camera;
 
 /* ---- render parameters ---------------------------------------------------------------------
@@ -363,6 +373,37 @@ int32_t dr_mesh_file_object_triangles(const dr_mesh_file *m, int32_t object);
 /* Any of xyz / nrm / uv may be NULL. */
 dr_status dr_mesh_file_object_data(const dr_mesh_file *m, int32_t object, float *xyz, float *nrm, float *uv);
 void dr_mesh_file_destroy(dr_mesh_file *m);
+
+/* ---- scene files (.dumb) ---------------------------------------------------------------------
+ * Replace DumbRenderContext::fromFile (__source__/DataStructures/DumbRenderContext/DumbRenderContext.cu:
+ * 300-372) and what it calls: the Dson text format (Namespaces/Dson/Dson.cu:225-447), "include",
+ * "materials" (dumb_based with its presets, simple_stochastic), "lights" (simple_soft_directional,
+ * simple_spherical), "groups" and "objects" (OBJ meshes placed by Transforms, groups with fallback /
+ * override materials), "camera" (simple_stochastic / spherical_segment lenses, Transform with
+ * position / rotation / scale / relative_position) and "renderer" (boxing, bounces, samples per
+ * pixel, backface culling; the thread / block settings are validated and not used).  Relative paths
+ * resolve against the directory of the file that names them, then the working directory.
+ * What the reference registers but this renderer has no counterpart for (fresnel_color materials,
+ * spotlights, textures, mesh primitives, which the reference leaves unimplemented) fails the load
+ * with a message naming it.  The triangles come out in the reference's push order (an object that
+ * names no OBJ object takes every object of the file, in file order; the reference's order there
+ * is that of a hash map). */
+typedef struct dr_scene_file dr_scene_file;
+dr_status dr_scene_file_load(const char *path, dr_scene_file **out);
+/* counts: [0] triangles, [1] materials, [2] lights. */
+dr_status dr_scene_file_counts(const dr_scene_file *f, int32_t *counts);
+/* Triangles (float[n][3][3]), per-corner normals (same shape) and material ids (int32[n]); any may
+ * be NULL. */
+dr_status dr_scene_file_geometry(const dr_scene_file *f, float *xyz, float *nrm, int32_t *mat_id);
+dr_status dr_scene_file_materials(const dr_scene_file *f, dr_material *mats);
+dr_status dr_scene_file_lights(const dr_scene_file *f, dr_light *lights);
+/* The file's camera (origin_rows = 1) and reference-mode render parameters (width / height are 0;
+ * iteration 1, seed 0). */
+dr_status dr_scene_file_camera(const dr_scene_file *f, dr_camera *camera);
+dr_status dr_scene_file_render_params(const dr_scene_file *f, dr_render_params *params);
+/* dr_scene_create over the file's geometry, materials and lights (DumbRenderContext::buildFromFile). */
+dr_status dr_scene_file_create_scene(const dr_scene_file *f, const dr_build_params *bp, dr_scene **out);
+void dr_scene_file_destroy(dr_scene_file *f);
 
 /* ---- progressive render process -----------------------------------------------------------
  * Replaces BufferedRenderProcess (__source__/DataStructures/Renderers/BufferedRenderProcess/

@@ -857,7 +857,12 @@ void ref_lens(const Cam &cam, float sx, float sy, float pdx, float pdy, uint32_t
         d = normalized(target - origin);
         filter = col(c.filter);
     }
-    o = cam_dir(c, o) + col3(c.position);
+    if (c.origin_rows)
+        o = v3(o.x * c.row_x[0] + o.y * c.row_x[1] + o.z * c.row_x[2] + c.position[0],
+               o.x * c.row_y[0] + o.y * c.row_y[1] + o.z * c.row_y[2] + c.position[1],
+               o.x * c.row_z[0] + o.y * c.row_z[1] + o.z * c.row_z[2] + c.position[2]);
+    else
+        o = cam_dir(c, o) + col3(c.position);
     d = cam_dir(c, d);
 }
 

@@ -77,6 +77,21 @@ def reference():
         if hasattr(L, "dref_save_png"):
             L.dref_save_png.restype = ci
             L.dref_save_png.argtypes = [vp, ci, ci, ctypes.c_char_p]
+        if hasattr(L, "dref_dumb_load"):
+            L.dref_dumb_load.restype = vp
+            L.dref_dumb_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ci]
+            L.dref_dumb_free.argtypes = [vp]
+            L.dref_dumb_counts.argtypes = [vp, vp]
+            L.dref_dumb_geometry.argtypes = [vp, vp, vp, vp]
+            L.dref_dumb_material.argtypes = [vp, ci, vp]
+            L.dref_dumb_light.argtypes = [vp, ci, vp]
+            L.dref_dumb_camera.argtypes = [vp, vp]
+            L.dref_dumb_settings.argtypes = [vp, vp]
+            L.dref_record_material.argtypes = [vp, vp]
+            L.dref_record_light.argtypes = [vp, vp]
+            L.dref_record_lens.argtypes = [vp, vp]
+            L.dref_dumb_render.restype = ctypes.c_double
+            L.dref_dumb_render.argtypes = [vp, ci, ci, ci, ci, vp]
         _r = L
     return _r
 
@@ -236,3 +251,89 @@ def ref_read_obj(path):
         return names, meshes
     finally:
         L.dref_obj_free(h)
+
+
+# ---- scene files through the reference's own loader (DumbRenderContext::fromFile) ----------------
+
+class RefSceneFileError(RuntimeError):
+    pass
+
+
+def _ref_dumb_open(path):
+    L = reference()
+    err = ctypes.create_string_buffer(8192)
+    h = L.dref_dumb_load(str(path).encode(), err, len(err))
+    if not h:
+        raise RefSceneFileError(err.value.decode(errors="replace"))
+    return L, h
+
+
+def ref_scene_file_dump(path):
+    """What the reference's loader built, as canonical float dumps: geometry (xyz, normals, material
+    ids in push order), per-material / per-light dumps, camera (lens + transform) and settings."""
+    L, h = _ref_dumb_open(path)
+    try:
+        c = np.zeros(3, np.int32)
+        L.dref_dumb_counts(h, c.ctypes.data)
+        n = int(c[0])
+        xyz = np.zeros((n, 9), np.float32)
+        nrm = np.zeros((n, 9), np.float32)
+        mat = np.zeros(n, np.int32)
+        L.dref_dumb_geometry(h, xyz.ctypes.data, nrm.ctypes.data, mat.ctypes.data)
+        mats = np.zeros((int(c[1]), 16), np.float32)
+        for i in range(int(c[1])):
+            L.dref_dumb_material(h, i, mats[i].ctypes.data)
+        lights = np.zeros((int(c[2]), 16), np.float32)
+        for i in range(int(c[2])):
+            L.dref_dumb_light(h, i, lights[i].ctypes.data)
+        cam = np.zeros(32, np.float32)
+        L.dref_dumb_camera(h, cam.ctypes.data)
+        settings = np.zeros(8, np.int32)
+        L.dref_dumb_settings(h, settings.ctypes.data)
+        return dict(xyz=xyz, nrm=nrm, mat=mat, materials=mats, lights=lights, camera=cam[:29], settings=settings[:6])
+    finally:
+        L.dref_dumb_free(h)
+
+
+def scene_file_dump(f):
+    """The same dumps for a dumbray_gb300.SceneFile: materials, lights and the lens go through the
+    reference's constructors (dref_record_*), the transform fields are the camera's own."""
+    L = reference()
+    n = len(f.tris)
+    mats = np.zeros((len(f.materials), 16), np.float32)
+    for i, m in enumerate(f.materials):
+        rec = ref_material_record(m)
+        L.dref_record_material(rec.ctypes.data, mats[i].ctypes.data)
+    lights = np.zeros((len(f.lights), 16), np.float32)
+    for i, l in enumerate(f.lights):
+        rec = ref_light_record(l)
+        L.dref_record_light(rec.ctypes.data, lights[i].ctypes.data)
+    c = f.camera
+    crec = np.zeros(16, np.float32)
+    crec[0] = c.lens
+    crec[1:3] = list(c.angle)
+    crec[3], crec[4] = c.focal_distance, c.softness
+    crec[5:8] = list(c.filter)
+    cam = np.zeros(32, np.float32)
+    L.dref_record_lens(crec.ctypes.data, cam.ctypes.data)
+    cam[8:11], cam[11:14], cam[14:17] = list(c.right), list(c.up), list(c.forward)
+    cam[17:20], cam[20:23], cam[23:26] = list(c.row_x), list(c.row_y), list(c.row_z)
+    cam[26:29] = list(c.position)
+    p = f.params
+    settings = np.array([p.boxing, p.max_bounces, p.samples_x, p.samples_y, 1, p.cull_backfaces], np.int32)
+    return dict(xyz=f.tris.reshape(n, 9), nrm=f.normals.reshape(n, 9), mat=f.mat_id, materials=mats, lights=lights,
+                camera=cam[:29], settings=settings)
+
+
+def ref_dumb_render(path, width, height, iterations, threads=8):
+    """Reference DumbRenderer render of a scene file loaded by the reference (its camera and renderer
+    settings); returns (row-major RGBA image, seconds)."""
+    L, h = _ref_dumb_open(path)
+    try:
+        img = np.zeros((height, width, 4), np.float32)
+        sec = L.dref_dumb_render(h, width, height, iterations, threads, img.ctypes.data)
+        if sec < 0:
+            raise RefSceneFileError("reference render failed")
+        return img, sec
+    finally:
+        L.dref_dumb_free(h)

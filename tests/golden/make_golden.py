@@ -8,6 +8,11 @@
                    culling on.
   render_*.npz     reference DumbRenderer CPU renders (four independent runs of 512 progressive
                    iterations each) of small reference-expressible scenes, 32x32.
+  scene_file/      a scene file (scene.dumb including materials.dumb, meshes in props.obj) that uses
+                   presets, groups with fallback / override materials, rotated and scaled items and a
+                   rotated spherical-segment camera; render_scene_file.npz holds the reference's renders
+                   of it, loaded by the reference's own DumbRenderContext::fromFile (four runs of 512
+                   iterations, 32x24).
 
 Run from the repository root after `bash oracle/build_ref.sh`:  python tests/golden/make_golden.py
 """
@@ -85,9 +90,108 @@ def render_fixtures(iterations=512, runs=4, size=32, bounces=2):
         print(kind, "reference seconds", secs, "mean", runs_arr[..., :3].mean())
 
 
+SCENE_FILE_DIR = OUT / "scene_file"
+
+SCENE_FILE_MATERIALS = """{
+	"materials": [
+		{ "name": "walls", "type": "dumb_based", "preset": "matte", "diffuse": [ 0.7, 0.7, 0.7 ] },
+		{ "name": "red", "type": "dumb_based", "preset": "matte", "diffuse": [ 0.7, 0.1, 0.1 ], "fresnel": [ 0.3, 0.2, 0.2 ] },
+		{ "name": "gold", "type": "dumb_based", "preset": "gold", "specular": 24 },
+		{ "name": "chalk", "type": "simple_stochastic", "color": [ 0.9, 0.85, 0.8 ], "diffuse": 0.3, "smoothness": 0.6, "shininess": 8 }
+	]
+}
+"""
+
+SCENE_FILE_MAIN = """{
+	"include": [ "materials.dumb" ],
+	"lights": [
+		{ "type": "simple_spherical", "color": [ 1.5, 1.5, 1.4 ], "position": [ 0, 0.8, 0 ], "radius": 0.1 },
+		{ "type": "simple_soft_directional", "color": [ 0.1, 0.1, 0.12 ] }
+	],
+	"groups": [
+		{
+			"name": "props",
+			"elements": [
+				{ "mesh": { "obj": "props.obj", "object": "sphere" },
+				  "transform": { "position": [ 0.3, -0.5, 0.25 ], "scale": [ 0.6, 0.6, 0.6 ] },
+				  "material": "gold" },
+				{ "mesh": { "obj": "props.obj", "object": "cube" },
+				  "transform": { "position": [ -0.4, -0.75, 0.3 ], "rotation": [ 20, 30, 0 ], "scale": [ 0.3, 0.3, 0.3 ] } }
+			],
+			"fallback_material": "chalk",
+			"transform": { "position": [ 0, 0.05, 0 ] }
+		}
+	],
+	"objects": [
+		{ "mesh": { "obj": "props.obj", "object": "room" }, "material": "walls" },
+		{ "group": "props", "transform": { "rotation": [ 0, 15, 0 ] } },
+		{
+			"elements": [
+				{ "mesh": { "obj": "props.obj", "object": "cube" },
+				  "transform": { "position": [ 0.55, -0.8, -0.2 ], "rotation": [ 0, 45, 10 ], "scale": [ 0.25, 0.35, 0.25 ] } }
+			],
+			"override_material": "red",
+			"transform": { "position": [ 0, 0.02, 0 ] }
+		}
+	],
+	"camera": {
+		"lense": { "type": "spherical_segment", "angle": 70, "distance": 1.6, "sensor": 0.01, "filter": [ 1, 0.95, 0.9 ] },
+		"transform": { "position": [ 0, 0.05, -0.55 ], "rotation": [ 6, -9, 3 ], "relative_position": [ 0, 0, -0.3 ] }
+	},
+	"renderer": {
+		"pixel": { "boxing": "width", "bounces": 2, "samples_per_pixel": [ 1, 1 ] }
+	}
+}
+"""
+
+
+def _obj_text(objects):
+    """OBJ text with one `g` group per (name, triangles); x is written negated because the reader
+    mirrors it back."""
+    lines, base = [], 1
+    for name, tris in objects:
+        lines.append(f"g {name}")
+        for t in tris:
+            for v in t:
+                lines.append(f"v {-float(v[0]):.9g} {float(v[1]):.9g} {float(v[2]):.9g}")
+        for i in range(len(tris)):
+            lines.append(f"f {base + 3 * i} {base + 3 * i + 1} {base + 3 * i + 2}")
+        base += 3 * len(tris)
+    return "\n".join(lines) + "\n"
+
+
+def write_scene_file(directory=SCENE_FILE_DIR):
+    directory = Path(directory)
+    directory.mkdir(parents=True, exist_ok=True)
+    objects = [("room", scenes.box((2.0, 2.0, 2.0), inward=True)), ("sphere", scenes.icosphere(2, 0.5)),
+               ("cube", scenes.box((1.0, 1.0, 1.0)))]
+    (directory / "props.obj").write_text(_obj_text(objects))
+    (directory / "materials.dumb").write_text(SCENE_FILE_MATERIALS)
+    (directory / "scene.dumb").write_text(SCENE_FILE_MAIN)
+    return directory / "scene.dumb"
+
+
+def scene_file_fixtures(iterations=512, runs=4, width=32, height=24):
+    path = write_scene_file()
+    out, secs = [], 0.0
+    for _ in range(runs):
+        img, t = O.ref_dumb_render(path, width, height, iterations)
+        out.append(img)
+        secs += t
+    runs_arr = np.stack(out)
+    np.savez_compressed(OUT / "render_scene_file.npz", runs=runs_arr, iterations=np.int64(iterations),
+                        width=np.int64(width), height=np.int64(height), seconds=np.float64(secs))
+    print("scene file: reference seconds", secs, "mean", runs_arr[..., :3].mean())
+
+
 if __name__ == "__main__":
     if not O.reference_available():
         raise SystemExit("build the reference first: bash oracle/build_ref.sh")
-    cast_fixtures()
-    render_fixtures()
+    only = sys.argv[1:]
+    if not only or "cast" in only:
+        cast_fixtures()
+    if not only or "render" in only:
+        render_fixtures()
+    if not only or "scene_file" in only:
+        scene_file_fixtures()
     print("golden fixtures written to", OUT)
