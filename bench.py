@@ -35,9 +35,9 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Mpaths/s 1080p 64spp on 1 GB300: plain vs batched, fwd vs fwd+adjoint, at RMSE"
 # DRAM bytes (read + write) per extension ray of k_trace, from one ncu capture of every k_trace launch
-# of a 960x544, 4 spp frame of the same scene, camera and octree (0.966 GB over 3,946,242 rays); the
+# of a 960x544, 4 spp frame of the same scene, camera and octree (0.933 GB over 3,946,242 rays); the
 # `traffic` of an average full-size launch is this times its ray count (profiles/k_trace_full_path_trace_1080p.md).
-TRACE_DRAM_BYTES_PER_RAY = 244.7
+TRACE_DRAM_BYTES_PER_RAY = 236.4
 UNIT = "Mpaths/s"
 
 

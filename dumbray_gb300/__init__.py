@@ -26,8 +26,8 @@ _HERE = Path(__file__).resolve().parent
 LIB_PATH = _HERE / "_build" / "libdumbray_gb300.so"
 
 DR_OK, DR_E_ARG, DR_E_CUDA, DR_E_CAPACITY, DR_E_TIMEOUT, DR_E_NOMEM, DR_E_STATE = range(7)
-MAT_DUMB_BASED, MAT_SIMPLE_STOCHASTIC, MAT_LAMBERT, MAT_MIRROR, MAT_GLOSSY = range(5)
-LIGHT_SPHERICAL, LIGHT_SOFT_DIRECTIONAL, LIGHT_DIRECTIONAL = range(3)
+MAT_DUMB_BASED, MAT_SIMPLE_STOCHASTIC, MAT_LAMBERT, MAT_MIRROR, MAT_GLOSSY, MAT_FRESNEL, MAT_DEFAULT = range(7)
+LIGHT_SPHERICAL, LIGHT_SOFT_DIRECTIONAL, LIGHT_DIRECTIONAL, LIGHT_SPOTLIGHT = range(4)
 LENS_DEFAULT_PERSPECTIVE, LENS_SIMPLE_STOCHASTIC, LENS_SPHERICAL_SEGMENT, LENS_PINHOLE, LENS_FISHEYE, LENS_SPHERICAL = range(6)
 MODE_REFERENCE, MODE_PHYSICAL = 0, 1
 PHYSICAL_TREE = -1.0   # Scene(box_epsilon=...): octree padding scaled to the scene (physical-mode scenes)
@@ -51,7 +51,10 @@ class DrMaterial(ctypes.Structure):
 
 class DrLight(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int32), ("color", _F3), ("position", _F3), ("direction", _F3),
-                ("radius", ctypes.c_float), ("distance", ctypes.c_float), ("softness", ctypes.c_float)]
+                ("radius", ctypes.c_float), ("distance", ctypes.c_float), ("softness", ctypes.c_float),
+                ("luminosity", ctypes.c_float), ("hotspot_angle", ctypes.c_float), ("falloff_angle", ctypes.c_float),
+                ("falloff_power", ctypes.c_float), ("emitter_size", ctypes.c_float),
+                ("emit_from_sphere", ctypes.c_int32), ("cast_shadows", ctypes.c_int32), ("samples", ctypes.c_int32)]
 
 
 class DrCamera(ctypes.Structure):
@@ -288,6 +291,43 @@ def soft_directional_light(color, direction, distance, softness) -> DrLight:
     l.direction[:] = direction
     l.distance = distance
     l.softness = softness
+    return l
+
+
+def fresnel_shader(color=(1.0, 1.0, 1.0)) -> DrMaterial:
+    """Shaders::FresnelShader(color) (FresnelShader.impl.cuh:5-19): no indirect samples."""
+    m = DrMaterial()
+    m.type = MAT_FRESNEL
+    m.color[:] = color
+    return m
+
+
+def default_shader(color=(1.0, 1.0, 1.0), diffuse=0.7, smoothness=0.2, shininess=8.0) -> DrMaterial:
+    """DefaultShaderGeneric(color, diffuse, smoothness, shine) (DefaultShader.impl.cuh:3-10)."""
+    m = DrMaterial()
+    m.type = MAT_DEFAULT
+    m.color[:] = color
+    m.diffuse = diffuse
+    m.smoothness = smoothness
+    m.shininess = shininess
+    return m
+
+
+def spotlight(color=(1.0, 1.0, 1.0), luminosity=1500.0, position=(0.0, 0.0, 0.0), direction=(0.0, 0.0, 1.0),
+              hotspot_angle=16.0, falloff_angle=64.0, falloff_power=1.0, emitter_size=0.25, emit_from_sphere=False,
+              cast_shadows=True, samples=1) -> DrLight:
+    """Lights::Spotlight(...) with the reference's defaults (Spotlight.cuh:7-11)."""
+    l = DrLight()
+    l.type = LIGHT_SPOTLIGHT
+    l.color[:] = color
+    l.luminosity = luminosity
+    l.position[:] = position
+    l.direction[:] = direction
+    l.hotspot_angle, l.falloff_angle, l.falloff_power = hotspot_angle, falloff_angle, falloff_power
+    l.emitter_size = emitter_size
+    l.emit_from_sphere = 1 if emit_from_sphere else 0
+    l.cast_shadows = 1 if cast_shadows else 0
+    l.samples = samples
     return l
 
 

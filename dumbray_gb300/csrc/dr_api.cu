@@ -207,6 +207,31 @@ int32_t dr_block_count(int32_t width, int32_t height) {
     return ((width + DR_BLOCK_W - 1) / DR_BLOCK_W) * ((height + DR_BLOCK_H - 1) / DR_BLOCK_H);
 }
 
+// Lights::Spotlight constructor state (Spotlight.impl.cuh:5-33): colour x luminosity, normalised
+// direction, emitter size at least 32 VECTOR_EPSILON, angles folded into [0, 180] with the falloff
+// angle at least the hotspot angle (a negative falloff angle takes minus the hotspot angle, as the
+// reference does), their cosines, 0..16 samples.
+static void spotlight_state(const dr_light &l, drd::Light &d) {
+    for (int k = 0; k < 3; k++) d.color[k] = l.color[k] * l.luminosity;
+    float im = 1 / std::sqrt(l.direction[0] * l.direction[0] + l.direction[1] * l.direction[1] + l.direction[2] * l.direction[2]);
+    for (int k = 0; k < 3; k++) d.direction[k] = l.direction[k] * im;
+    const float eps = 0.000005f;
+    d.emitter = (l.emitter_size < (32 * eps)) ? (32 * eps) : l.emitter_size;
+    float inner = l.hotspot_angle, outer = l.falloff_angle;
+    if (inner < 0.0f) inner = (-inner);
+    if (inner > 180.0f) inner = 180.0f;
+    if (outer < 0.0f) outer = (-inner);
+    if (outer > 180.0f) outer = 180.0f;
+    if (outer < inner) outer = inner;
+    const float pi = 3.14159265359f;
+    d.inner_cos = std::cos(inner * pi / 180.0f);
+    d.outer_cos = std::cos(outer * pi / 180.0f);
+    d.falloff = l.falloff_power;
+    d.samples = (l.samples > 0) ? ((l.samples > 16) ? 16 : l.samples) : 0;
+    d.shadows = l.cast_shadows ? 1 : 0;
+    d.sphere = l.emit_from_sphere ? 1 : 0;
+}
+
 dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat_id, int32_t n, const dr_material *mats,
                           int32_t n_mats, const dr_light *lights, int32_t n_lights, const dr_build_params *bp, dr_scene **out) {
     if (out == nullptr) return fail(DR_E_ARG, "dr_scene_create: out is NULL");
@@ -219,9 +244,9 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
         if (mat_id[i] < 0 || (n_mats > 0 && mat_id[i] >= n_mats) || (n_mats == 0 && mat_id[i] != 0))
             return fail(DR_E_ARG, "dr_scene_create: material id out of range at triangle " + std::to_string(i));
     for (int32_t i = 0; i < n_mats; i++)
-        if (mats[i].type < 0 || mats[i].type > DR_MAT_GLOSSY) return fail(DR_E_ARG, "dr_scene_create: bad material type");
+        if (mats[i].type < 0 || mats[i].type > DR_MAT_DEFAULT) return fail(DR_E_ARG, "dr_scene_create: bad material type");
     for (int32_t i = 0; i < n_lights; i++)
-        if (lights[i].type < 0 || lights[i].type > DR_LIGHT_DIRECTIONAL) return fail(DR_E_ARG, "dr_scene_create: bad light type");
+        if (lights[i].type < 0 || lights[i].type > DR_LIGHT_SPOTLIGHT) return fail(DR_E_ARG, "dr_scene_create: bad light type");
 
     dr_scene *sc = new (std::nothrow) dr_scene();
     if (!sc) return fail(DR_E_NOMEM, "dr_scene_create: out of host memory");
@@ -309,6 +334,7 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
         d.radius = l.radius;
         d.distance = l.distance;
         d.softness = l.softness;
+        if (l.type == DR_LIGHT_SPOTLIGHT) spotlight_state(l, d);
     }
 
     // child boxes of every node group as planes of 8 (see drd::Scene::gbox)
@@ -356,6 +382,9 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
     S.front_only = (bp && bp->box_epsilon != 0.0f) ? 1 : 0;
     S.n_mats = std::max(n_mats, 1);
     S.n_lights = n_lights;
+    S.shadow_photons = 0;
+    for (int32_t i = 0; i < n_lights; i++)
+        S.shadow_photons += (lights[i].type == DR_LIGHT_SPOTLIGHT) ? (dl[i].shadows ? dl[i].samples : 0) : 1;
     if (n == 0) { S.root_child = -1; S.root_leaf_count = 0; }
 
     sc->albedo.resize(3 * (size_t)n);
@@ -683,7 +712,7 @@ dr_status dr_render_blocks(dr_renderer *r, const dr_scene *sc, const dr_camera *
     W.max_bounces = I.max_bounces;
     W.adjoint = false;
     wave_buffers(r, W);
-    const int lights = (I.mode == DR_MODE_REFERENCE) ? I.S.n_lights : 1;
+    const int lights = (I.mode == DR_MODE_REFERENCE) ? I.S.shadow_photons : 1;
     return run_waves(r, W, (long long)I.n_slots * I.spp, wave_size(r, lights, 1LL << 40), I.n_slots, stream, &r->prof, r->counting,
                      true);
 }
@@ -850,7 +879,7 @@ dr_status dr_batch_create(const dr_batch_item *items, int32_t n, dr_batch **out)
         slot += I.n_slots;
         path += (long long)I.n_slots * I.spp;
         b->max_bounces = std::max(b->max_bounces, I.max_bounces);
-        if (I.mode == DR_MODE_REFERENCE) b->max_lights = std::max(b->max_lights, I.S.n_lights);
+        if (I.mode == DR_MODE_REFERENCE) b->max_lights = std::max(b->max_lights, I.S.shadow_photons);
         b->scenes.push_back(it.scene);
         b->params.push_back(it.params);
     }

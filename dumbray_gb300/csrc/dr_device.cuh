@@ -32,10 +32,14 @@ struct Material {
 
 struct Light {
     int type;
-    float color[3];
+    float color[3];      // spotlight: colour x luminosity
     float position[3];
-    float direction[3];
+    float direction[3];  // spotlight: normalised
     float radius, distance, softness;
+    // spotlight (Lights::Spotlight constructor state): emitter size, cosines of the hotspot and
+    // falloff half-angles, falloff power, photons per shading point, occlusion test, sphere emitter
+    float emitter, inner_cos, outer_cos, falloff;
+    int samples, shadows, sphere;
 };
 
 struct Scene {
@@ -60,6 +64,7 @@ struct Scene {
                                 // scene's offset in a batch arena), -1 = the root is a leaf
     int root_leaf_first, root_leaf_count;
     int n_tris, n_mats, n_lights, n_emissive;
+    int shadow_photons;  // shadow records one reference-mode hit can emit (1 per light, a spotlight's samples)
     // Boxes lying entirely behind the ray origin: the reference's slab test keeps them
     // (clipBackface = false), which only costs work, since a hit at t > 0 accepted inside a leaf box
     // means that box reaches t > 0.  Every non-counting traversal skips them; the counting ones

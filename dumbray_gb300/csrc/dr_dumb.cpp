@@ -9,10 +9,12 @@
 //    300-372): "include", "materials", "lights", "groups", "objects", "camera", "renderer", in that
 //    order, includes parsed into the same context with paths relative to the including file;
 //  * materials (parseMaterial, :654-684): DumbBasedShader::fromDson (Shaders/DumbBasedShader/
-//    DumbBasedShader.impl.cuh:125-179, presets :9-12 of the header, constructor :5-15) and
-//    SimpleStochasticShader::fromDson (SimpleStochasticShader.impl.cuh:4-12, 39-66);
+//    DumbBasedShader.impl.cuh:125-179, presets :9-12 of the header, constructor :5-15),
+//    SimpleStochasticShader::fromDson (SimpleStochasticShader.impl.cuh:4-12, 39-66) and
+//    Shaders::FresnelShader::fromDson (FresnelShader.impl.cuh:20-24);
 //  * lights: SimpleSoftDirectionalLight::fromDson (SimpleSoftDirectionalLight.impl.cuh:5-10, 25-49),
-//    SphericalLightEmitter::fromDson (SphericalLightEmitter.impl.cuh:5-9, 20-41);
+//    SphericalLightEmitter::fromDson (SphericalLightEmitter.impl.cuh:5-9, 20-41),
+//    Lights::Spotlight::fromDson (Spotlight.impl.cuh:79-151);
 //  * groups and objects (DumbRenderContext.cu:103-259, 738-790): items place OBJ objects through
 //    their Transform, groups apply fallback / override materials and their own Transform after
 //    their members', top-level objects must end up with a material;
@@ -21,8 +23,8 @@
 //    BakedTriFace >> Transform (Meshes/BakedTriMesh/BakedTriMesh.impl.h:16-18);
 //  * the camera (parseCamera, :491-530; SimpleStochasticLense / SphericalSegmentLense ::fromDson)
 //    and renderer settings (parseRenderer, :531-633).
-// Components the reference registers without a counterpart in this renderer (fresnel_color,
-// spotlight, textures) and mesh primitives (unimplemented in the reference) fail with a message.
+// Textures (no counterpart in this renderer) and mesh primitives (unimplemented in the reference)
+// fail with a message.
 #include <cerrno>
 #include <climits>
 #include <cmath>
@@ -469,7 +471,7 @@ class Loader {
         std::memset(&m, 0, sizeof(m));
         if (t == "dumb_based") dumb_based(v, m);
         else if (t == "simple_stochastic") simple_stochastic(v, m);
-        else if (t == "fresnel_color") raise("material type \"fresnel_color\" is not supported by this renderer");
+        else if (t == "fresnel_color") fresnel_color(v, m);
         else raise("unknown material type: \"" + t + "\"");
         int id = (int)materials.size();
         materials.push_back(m);
@@ -550,6 +552,25 @@ class Loader {
         m.shininess = shininess;
     }
 
+    // Shaders::FresnelShader::fromDson (FresnelShader.impl.cuh:20-24): white, then an "engine_color"
+    // preset (DumbStructs.cuh:143-169; the reference ignores a bad one), then the colour entries.
+    static void fresnel_color(const JValue &v, dr_material &m) {
+        V color{1.0f, 1.0f, 1.0f};
+        if (const JValue *e = v.get("engine_color")) {
+            if (e->kind == JValue::STR) {
+                const std::string &n = e->str;
+                if (n == "iron") color = V{0.56f, 0.57f, 0.58f};
+                else if (n == "copper") color = V{0.95f, 0.64f, 0.54f};
+                else if (n == "gold") color = V{1.0f, 0.71f, 0.29f};
+                else if (n == "aluminum") color = V{0.91f, 0.92f, 0.92f};
+                else if (n == "silver") color = V{0.95f, 0.93f, 0.88f};
+            }
+        }
+        colored(v, "color", "texture", "tiling", "offset", color);
+        m.type = DR_MAT_FRESNEL;
+        m.color[0] = color.x, m.color[1] = color.y, m.color[2] = color.z;
+    }
+
     int material_ref(const JValue &v) {
         if (v.kind == JValue::STR) {
             auto it = material_names_.find(v.str);
@@ -595,11 +616,49 @@ class Loader {
             l.position[0] = position.x, l.position[1] = position.y, l.position[2] = position.z;
             l.radius = radius;
         } else if (t == "spotlight") {
-            raise("light type \"spotlight\" is not supported by this renderer");
+            spotlight(v, l);
         } else {
             raise("unknown light type: \"" + t + "\"");
         }
         lights.push_back(l);
+    }
+
+    // Lights::Spotlight::fromDson (Spotlight.impl.cuh:79-151): constructor arguments with their
+    // defaults; "target" (minus the position read so far) wins over "direction"; an unknown
+    // "emitter_shape" keeps the disc (the reference only reports it).
+    static void spotlight(const JValue &v, dr_light &l) {
+        V color{1.0f, 1.0f, 1.0f}, pos{0.0f, 0.0f, 0.0f}, dir{0.0f, 0.0f, 1.0f};
+        float lum = 1500.0f, inner = 16.0f, outer = 64.0f, power = 1.0f, size = 0.25f;
+        bool sphere = false, shadows = true;
+        int samples = 1;
+        if (const JValue *p = v.get("color")) color = vector_from(*p, "spotlight color");
+        if (const JValue *p = v.get("luminosity")) lum = as_float(*p, "spotlight luminosity");
+        if (const JValue *p = v.get("position")) pos = vector_from(*p, "spotlight position");
+        if (const JValue *p = v.get("target")) dir = vsub(vector_from(*p, "spotlight target"), pos);
+        else if (const JValue *p = v.get("direction")) dir = vector_from(*p, "spotlight direction");
+        if (const JValue *p = v.get("hotspot_angle")) inner = as_float(*p, "spotlight hotspot angle");
+        if (const JValue *p = v.get("falloff_angle")) outer = as_float(*p, "spotlight falloff angle");
+        if (const JValue *p = v.get("falloff_power")) power = as_float(*p, "spotlight falloff power");
+        if (const JValue *p = v.get("emitter_size")) size = as_float(*p, "spotlight emitter size");
+        if (const JValue *p = v.get("emitter_shape")) {
+            const std::string &shape = as_string(*p, "spotlight emitter shape");
+            if (shape == "sphere") sphere = true;
+            else if (shape == "disc") sphere = false;
+        }
+        if (const JValue *p = v.get("cast_shadows")) shadows = as_bool(*p, "spotlight shadow cast flag");
+        if (const JValue *p = v.get("sample_count")) samples = as_int(*p, "spotlight sample count");
+        l.type = DR_LIGHT_SPOTLIGHT;
+        l.color[0] = color.x, l.color[1] = color.y, l.color[2] = color.z;
+        l.position[0] = pos.x, l.position[1] = pos.y, l.position[2] = pos.z;
+        l.direction[0] = dir.x, l.direction[1] = dir.y, l.direction[2] = dir.z;
+        l.luminosity = lum;
+        l.hotspot_angle = inner;
+        l.falloff_angle = outer;
+        l.falloff_power = power;
+        l.emitter_size = size;
+        l.emit_from_sphere = sphere ? 1 : 0;
+        l.cast_shadows = shadows ? 1 : 0;
+        l.samples = samples;
     }
 
     // ---- meshes, items, groups, objects ----

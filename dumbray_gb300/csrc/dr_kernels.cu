@@ -402,7 +402,11 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
                 TriV v = load_tri(S.tris, tri), nt = load_tri(S.nrms, tri);
                 int ctype = 0;
                 if (m.type == 0) child = dumb_based_request(m, v, nt, hp, d, key, (uint32_t)b, cd, ctype);
-                else {
+                else if (m.type == DR_MAT_FRESNEL) child = false;
+                else if (m.type == DR_MAT_DEFAULT) {
+                    cd = default_request(v, nt, hp, d);
+                    child = true;
+                } else {
                     cd = ss_request(m, v, nt, hp, d, key, (uint32_t)b);
                     child = true;
                 }
@@ -412,27 +416,42 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
                 }
             }
         }
-        // light photons: one shadow record per light of the path's scene
+        // light photons: one shadow record per photon of each light of the path's scene (a
+        // spotlight sends `samples` photons); photons of a light that casts no shadows are added
+        // at once (DumbRenderer.cu:300-316: no cast, every photon illuminates)
         const int n_lights = MULTI ? 16 : A.inl.S.n_lights;
         for (int li = 0; li < n_lights; li++) {
             const bool has = active && li < S.n_lights;
             if (MULTI && !__any_sync(0xFFFFFFFFu, has)) break;
-            bool emit = false;
-            f3 lo, ld;
-            c3 lc, contrib;
-            if (has) {
-                light_photon(S.lights[li], hp, key, (uint32_t)b, li, lo, ld, lc);
-                c3 r = ref_reflect(S, tri, hp, ld, neg3(f3of(p1)), true, 0);
-                contrib = cmul(thr, r);
-                emit = (contrib.r + contrib.g + contrib.b) != 0.0f && (lc.r + lc.g + lc.b) != 0.0f;
-            }
-            int w = warp_alloc(&C->shadow_count[b], emit);
-            if (emit) {
-                A.sq.s0[w] = make_float4(lo.x, lo.y, lo.z, p0.w);
-                A.sq.s1[w] = make_float4(ld.x, ld.y, ld.z, __int_as_float(tri));
-                A.sq.s2[w] = make_float4(hp.x, hp.y, hp.z, __int_as_float(-1));
-                A.sq.s3[w] = make_float4(lc.r, lc.g, lc.b, 0.0f);
-                A.sq.s4[w] = make_float4(contrib.r, contrib.g, contrib.b, __int_as_float(p3.w));
+            const int cnt = has ? light_photons(S.lights[li]) : 0;
+            const int kmax = __reduce_max_sync(0xFFFFFFFFu, cnt);
+            for (int k = 0; k < kmax; k++) {
+                bool emit = false;
+                f3 lo, ld;
+                c3 lc, contrib;
+                if (k < cnt) {
+                    const Light &L = S.lights[li];
+                    bool ok = true;
+                    if (L.type == DR_LIGHT_SPOTLIGHT) ok = spot_photon(L, hp, key, (uint32_t)b, li, k, lo, ld, lc);
+                    else light_photon(L, hp, key, (uint32_t)b, li, lo, ld, lc);
+                    if (ok) {
+                        c3 r = ref_reflect(S, tri, hp, ld, neg3(f3of(p1)), true, 0);
+                        contrib = cmul(thr, r);
+                        emit = (contrib.r + contrib.g + contrib.b) != 0.0f && (lc.r + lc.g + lc.b) != 0.0f;
+                        if (emit && L.type == DR_LIGHT_SPOTLIGHT && !L.shadows) {
+                            accum_add(A.accum, __float_as_int(p0.w), cmul(contrib, lc));
+                            emit = false;
+                        }
+                    }
+                }
+                int w = warp_alloc(&C->shadow_count[b], emit);
+                if (emit) {
+                    A.sq.s0[w] = make_float4(lo.x, lo.y, lo.z, p0.w);
+                    A.sq.s1[w] = make_float4(ld.x, ld.y, ld.z, __int_as_float(tri));
+                    A.sq.s2[w] = make_float4(hp.x, hp.y, hp.z, __int_as_float(-1));
+                    A.sq.s3[w] = make_float4(lc.r, lc.g, lc.b, 0.0f);
+                    A.sq.s4[w] = make_float4(contrib.r, contrib.g, contrib.b, __int_as_float(p3.w));
+                }
             }
         }
         int w = warp_alloc(&C->ray_count[b + 1], child);

@@ -112,7 +112,7 @@ extern "C" dr_status dr_render_blocks_noalloc(const dr_scene *sc, const dr_camer
     const int fx = std::max(1, p->samples_x), fy = std::max(1, p->samples_y);
     const int spp = fx * fy;
     const int n_slots = (end_block - start_block) * DR_BLOCK_W * DR_BLOCK_H;
-    const int per_path_shadow = (p->mode == DR_MODE_REFERENCE) ? std::max(1, S->n_lights) : 1;
+    const int per_path_shadow = (p->mode == DR_MODE_REFERENCE) ? std::max(1, S->shadow_photons) : 1;
     long long wave = std::min<long long>(kWavePaths, (long long)kShadowRecords / per_path_shadow);
     wave = std::max<long long>(32, (wave / 32) * 32);
 

@@ -1,13 +1,15 @@
 // dr_shading.cuh - device shading models.
 //
-// Reference semantics (DR_MODE_REFERENCE): DumbBasedShader and SimpleStochasticShader
-// (__source__/DataStructures/Objects/Components/Shaders/DumbBasedShader/DumbBasedShader.impl.cuh:18-122,
-//  .../SimpleStochasticShader/SimpleStochasticShader.impl.cuh:13-37), the three analytic lights
-// (.../Scene/Lights/*: SphericalLightEmitter.impl.cuh:10-18, SimpleSoftDirectionalLight.impl.cuh:12-19,
-//  SimpleDirectionalLight.impl.cuh:13-16) and lenses (.../Components/Lenses/*).  getReflectedColor is
+// Reference semantics (DR_MODE_REFERENCE): DumbBasedShader, SimpleStochasticShader, FresnelShader and
+// DefaultShader (__source__/DataStructures/Objects/Components/Shaders/DumbBasedShader/DumbBasedShader.impl.cuh:18-122,
+//  .../SimpleStochasticShader/SimpleStochasticShader.impl.cuh:13-37, .../FresnelShader/FresnelShader.impl.cuh:11-19,
+//  .../DefaultShader/DefaultShader.impl.cuh:3-52), the four lights (.../Scene/Lights/*:
+//  SphericalLightEmitter.impl.cuh:10-18, SimpleSoftDirectionalLight.impl.cuh:12-19,
+//  SimpleDirectionalLight.impl.cuh:13-16, Spotlight.impl.cuh:35-77) and lenses (.../Components/Lenses/*).  getReflectedColor is
 // linear in the photon colour, so every function here returns the colour FACTOR and callers multiply.
 // Physical semantics (DR_MODE_PHYSICAL): Lambert / mirror / GGX glossy with emissive triangles.
 #pragma once
+#include "../../include/dr_api.h"
 #include "dr_device.cuh"
 
 namespace drd {
@@ -180,11 +182,46 @@ __device__ inline c3 ss_reflect(const Material &m, const TriV &v, const TriV &nt
     return cscale(mkc(m.color[0], m.color[1], m.color[2]), (diff * rc) + (gloss * powf(oc, m.shininess)));
 }
 
-// Material::getReflectedColor dispatch (colour factor).
+// ---- FresnelShader: no indirect samples; DumbTools::fresnel(colour, interpolated normal, -photon
+// direction) (FresnelShader.impl.cuh:11-19, DumbStructs.cuh:136-140); the normal is not normalised.
+__device__ inline c3 fresnel_reflect(const Material &m, const TriV &v, const TriV &nt, f3 hit, f3 photon_dir) {
+    f3 masses = get_masses(v, hit);
+    f3 light = neg3(norm3(photon_dir));
+    f3 normal = mass_center(nt, masses);
+    float val = (1.0f - dot3(normal, light));
+    float sq = (val * val);
+    float f = sq * sq * val;
+    return mkc(m.color[0] + ((1.0f - m.color[0]) * f), m.color[1] + ((1.0f - m.color[1]) * f),
+               m.color[2] + ((1.0f - m.color[2]) * f));
+}
+
+// ---- DefaultShaderGeneric (DefaultShader.impl.cuh:3-52): one sample along the reflection of the
+// ray about the interpolated normal (not normalised, weight 1, type 0); reflected colour
+// albedo x (diff cosL + gloss max(cos(refl, observer), 0)^shininess) with the constructor's
+// diffuse / smoothness normalisation; the observer is (hit + direction) - hit, as the reference
+// forms it.
+__device__ inline f3 default_request(const TriV &v, const TriV &nt, f3 hit, f3 raydir) {
+    return reflect3(raydir, mass_center(nt, get_masses(v, hit)));
+}
+__device__ inline c3 default_reflect(const Material &m, const TriV &v, const TriV &nt, f3 hit, f3 photon_dir, f3 observer) {
+    float diff, gloss;
+    ss_params(m, diff, gloss);
+    f3 normal = mass_center(nt, get_masses(v, hit));
+    f3 cam = sub3(add3(hit, observer), hit);
+    f3 refl = reflect3(photon_dir, normal);
+    float cosL = fmaxf(dot3(refl, normal) / sqrtf(sqr3(refl) * sqr3(normal)), 0.0f);
+    float oc = fmaxf(dot3(refl, cam) / sqrtf(sqr3(refl) * sqr3(cam)), 0.0f);
+    return cscale(mkc(m.color[0], m.color[1], m.color[2]), (diff * cosL) + (gloss * powf(oc, m.shininess)));
+}
+
+// Material::getReflectedColor dispatch (colour factor).  The physical-mode types take the
+// SimpleStochastic branch, as they always have in the reference mode.
 __device__ inline c3 ref_reflect(const Scene &S, int tri, f3 hit, f3 photon_dir, f3 observer, bool direct, int sample_type) {
     const Material &m = S.mats[__ldg(S.mat_id + tri)];
     TriV v = load_tri(S.tris, tri), nt = load_tri(S.nrms, tri);
     if (m.type == 0) return dumb_based_reflect(m, v, nt, hit, photon_dir, observer, direct, sample_type);
+    if (m.type == DR_MAT_FRESNEL) return fresnel_reflect(m, v, nt, hit, photon_dir);
+    if (m.type == DR_MAT_DEFAULT) return default_reflect(m, v, nt, hit, photon_dir, observer);
     return ss_reflect(m, v, nt, hit, photon_dir, observer);
 }
 
@@ -215,6 +252,54 @@ __device__ inline void light_photon(const Light &l, f3 point, uint32_t key, uint
         d = dir;
         c = mkc(l.color[0], l.color[1], l.color[2]);
     }
+}
+
+// Photons light `l` sends toward one shading point: a spotlight's sample count, else 1.
+__device__ __forceinline__ int light_photons(const Light &l) { return (l.type == DR_LIGHT_SPOTLIGHT) ? l.samples : 1; }
+
+// Spotlight::getVertexPhotons, photon k of `count` (Spotlight.impl.cuh:35-77): a point on the
+// emitter disc (ver / hor frame about the direction) or in the emitter sphere, colour scaled by
+// emitter area over emitter + spread area (the disc area is left out for a sphere) and the cubic
+// falloff between the hotspot and falloff cones.  Returns false where the reference skips the
+// photon (point on the emitter, outside the falloff cone).  Random dimensions 4096 + 64 li + 3 k.
+__device__ inline bool spot_photon(const Light &l, f3 point, uint32_t key, uint32_t bounce, int li, int k, f3 &o, f3 &d,
+                                   c3 &c) {
+    const uint32_t d0 = 4096u + 64u * (uint32_t)li + 3u * (uint32_t)k;
+    const f3 dir = f3{l.direction[0], l.direction[1], l.direction[2]};
+    const f3 pos0 = f3{l.position[0], l.position[1], l.position[2]};
+    f3 non_dir = (dir.z > 0.9f) ? f3{1.0f, 0.0f, 0.0f} : f3{0.0f, 0.0f, 1.0f};
+    f3 ver = norm3(cross3(dir, non_dir));
+    f3 hor = cross3(dir, ver);
+    f3 pos;
+    if (l.sphere) {
+        pos = point_on_sphere(rnd(key, bounce, d0), rnd(key, bounce, d0 + 1), l.emitter);
+        pos = mul3(pos, rnd(key, bounce, d0 + 2));
+        pos = add3(pos, pos0);
+    } else {
+        float angle = (rnd(key, bounce, d0) * ((2.0f * 3.14159265359f) - 0.0f)) + 0.0f;
+        f3 ring = add3(mul3(ver, cosf(angle)), mul3(hor, sinf(angle)));
+        pos = add3(pos0, mul3(mul3(ring, l.emitter), sqrtf(rnd(key, bounce, d0 + 1))));
+    }
+    f3 delta = sub3(point, pos);
+    float sqr_distance = sqr3(delta);
+    if (sqr_distance < kEps) return false;
+    float distance = sqrtf(sqr_distance);
+    float base = (l.emitter * l.emitter);
+    float spread = fmaxf(1.0f - l.outer_cos, kEps);
+    float surface = ((l.sphere ? 0.0f : base) + (sqr_distance * spread));
+    float s = (base / (((float)l.samples) * surface));
+    c = mkc(l.color[0] * s, l.color[1] * s, l.color[2] * s);
+    f3 dd = divf3(delta, distance);
+    float cosine = dot3(dd, dir);
+    if (cosine < l.inner_cos) {
+        if (cosine < l.outer_cos) return false;
+        float a = ((l.inner_cos - cosine) / (l.inner_cos - l.outer_cos));
+        float b = (1.0f - a);
+        c = cscale(c, powf((a * b * b) + (b * (1.0f - (a * a))), l.falloff));
+    }
+    o = pos;
+    d = dd;
+    return true;
 }
 
 // ---- physical mode ---------------------------------------------------------------------------

@@ -66,13 +66,21 @@ typedef struct {
  *                            (__source__/.../Shaders/DumbBasedShader/DumbBasedShader.impl.cuh:5-122)
  *   DR_MAT_SIMPLE_STOCHASTIC SimpleStochasticShader(albedo=color, diffuse, smoothness, shininess)
  *                            (__source__/.../Shaders/SimpleStochasticShader/SimpleStochasticShader.impl.cuh:4-37)
+ *   DR_MAT_FRESNEL           Shaders::FresnelShader(fresnel=color): no indirect samples, Schlick term
+ *                            of the interpolated normal (.../Shaders/FresnelShader/FresnelShader.impl.cuh:5-19)
+ *   DR_MAT_DEFAULT           DefaultShaderGeneric(albedo=color, diffuse, smoothness, shininess): one
+ *                            mirror-direction sample, diffuse + Phong lobe (.../Shaders/DefaultShader/
+ *                            DefaultShader.impl.cuh:3-52)
  * Physical-mode materials (no reference counterpart; albedo = color, overridable per triangle):
- *   DR_MAT_LAMBERT, DR_MAT_MIRROR, DR_MAT_GLOSSY (GGX, alpha = roughness). */
+ *   DR_MAT_LAMBERT, DR_MAT_MIRROR, DR_MAT_GLOSSY (GGX, alpha = roughness).  In the physical mode the
+ *   reference-semantics types shade as Lambert with their colour. */
 #define DR_MAT_DUMB_BASED 0
 #define DR_MAT_SIMPLE_STOCHASTIC 1
 #define DR_MAT_LAMBERT 2
 #define DR_MAT_MIRROR 3
 #define DR_MAT_GLOSSY 4
+#define DR_MAT_FRESNEL 5
+#define DR_MAT_DEFAULT 6
 
 typedef struct {
     int32_t type;
@@ -90,10 +98,17 @@ typedef struct {
 /* ---- lights (reference semantics; Light function pack, Light.cuh:14-59) -----------------
  *   DR_LIGHT_SPHERICAL         SphericalLightEmitter(color, position, radius)
  *   DR_LIGHT_SOFT_DIRECTIONAL  SimpleSoftDirectionalLight(color, direction, distance, softness)
- *   DR_LIGHT_DIRECTIONAL       SimpleDirectionalLight(color, direction, distance) */
+ *   DR_LIGHT_DIRECTIONAL       SimpleDirectionalLight(color, direction, distance)
+ *   DR_LIGHT_SPOTLIGHT         Lights::Spotlight(color, luminosity, position, direction, hotspot_angle,
+ *                              falloff_angle, falloff_power, emitter_size, emit_from_sphere, cast_shadows,
+ *                              samples) (.../Scene/Lights/Spotlight/Spotlight.impl.cuh:5-79): `samples`
+ *                              photons per shading point (0..16) from a disc or sphere emitter with a
+ *                              cone falloff; cast_shadows = 0 lights without an occlusion test.
+ * At most 16 lights per scene. */
 #define DR_LIGHT_SPHERICAL 0
 #define DR_LIGHT_SOFT_DIRECTIONAL 1
 #define DR_LIGHT_DIRECTIONAL 2
+#define DR_LIGHT_SPOTLIGHT 3
 
 typedef struct {
     int32_t type;
@@ -103,6 +118,15 @@ typedef struct {
     float radius;
     float distance;
     float softness;
+    /* DR_LIGHT_SPOTLIGHT only (angles in degrees) */
+    float luminosity;
+    float hotspot_angle;
+    float falloff_angle;
+    float falloff_power;
+    float emitter_size;
+    int32_t emit_from_sphere;
+    int32_t cast_shadows;
+    int32_t samples;
 } dr_light;
 
 /* ---- camera / lenses (Lense function pack, Lense.cuh:46-82; Camera.impl.cuh:7-14) --------
@@ -377,15 +401,16 @@ void dr_mesh_file_destroy(dr_mesh_file *m);
 /* ---- scene files (.dumb) ---------------------------------------------------------------------
  * Replace DumbRenderContext::fromFile (__source__/DataStructures/DumbRenderContext/DumbRenderContext.cu:
  * 300-372) and what it calls: the Dson text format (Namespaces/Dson/Dson.cu:225-447), "include",
- * "materials" (dumb_based with its presets, simple_stochastic), "lights" (simple_soft_directional,
- * simple_spherical), "groups" and "objects" (OBJ meshes placed by Transforms, groups with fallback /
+ * "materials" (dumb_based with its presets, simple_stochastic, fresnel_color), "lights"
+ * (simple_soft_directional, simple_spherical, spotlight), "groups" and "objects" (OBJ meshes placed by Transforms, groups with fallback /
  * override materials), "camera" (simple_stochastic / spherical_segment lenses, Transform with
  * position / rotation / scale / relative_position) and "renderer" (boxing, bounces, samples per
  * pixel, backface culling; the thread / block settings are validated and not used).  Relative paths
  * resolve against the directory of the file that names them, then the working directory.
- * What the reference registers but this renderer has no counterpart for (fresnel_color materials,
- * spotlights, textures, mesh primitives, which the reference leaves unimplemented) fails the load
- * with a message naming it.  The triangles come out in the reference's push order (an object that
+ * Materials: dumb_based, simple_stochastic, fresnel_color; lights: simple_soft_directional,
+ * simple_spherical, spotlight (everything the reference's registry holds).  Textures (no
+ * counterpart in this renderer) and mesh primitives (left unimplemented by the reference) fail the
+ * load with a message naming them.  The triangles come out in the reference's push order (an object that
  * names no OBJ object takes every object of the file, in file order; the reference's order there
  * is that of a hash map). */
 typedef struct dr_scene_file dr_scene_file;

@@ -644,12 +644,41 @@ inline Col operator*(Col a, float f) { return Col{a.r * f, a.g * f, a.b * f}; }
 inline Col col(const float *p) { return Col{p[0], p[1], p[2]}; }
 inline float clamp01(float v) { return std::fmax(0.0f, std::fmin(v, 1.0f)); }
 
+// Lights::Spotlight constructor state (Spotlight.impl.cuh:5-33).
+struct Spot {
+    Col color;  // colour x luminosity
+    V3 direction;
+    float emitter, inner_cos, outer_cos, falloff;
+    int samples;
+    bool shadows, sphere;
+};
+Spot spot_state(const dr_light &l) {
+    Spot s;
+    s.color = Col{l.color[0] * l.luminosity, l.color[1] * l.luminosity, l.color[2] * l.luminosity};
+    s.direction = normalized(col3(l.direction));
+    s.emitter = (l.emitter_size < (32 * EPS)) ? (32 * EPS) : l.emitter_size;
+    float inner = l.hotspot_angle, outer = l.falloff_angle;
+    if (inner < 0.0f) inner = (-inner);
+    if (inner > 180.0f) inner = 180.0f;
+    if (outer < 0.0f) outer = (-inner);
+    if (outer > 180.0f) outer = 180.0f;
+    if (outer < inner) outer = inner;
+    s.inner_cos = std::cos(inner * PI_F / 180.0f);
+    s.outer_cos = std::cos(outer * PI_F / 180.0f);
+    s.falloff = l.falloff_power;
+    s.samples = (l.samples > 0) ? ((l.samples > 16) ? 16 : l.samples) : 0;
+    s.shadows = l.cast_shadows != 0;
+    s.sphere = l.emit_from_sphere != 0;
+    return s;
+}
+
 struct Scene {
     Octree tree;
     std::vector<Tri> nrm;
     std::vector<int> mat;
     std::vector<dr_material> mats;
     std::vector<dr_light> lights;
+    std::vector<struct Spot> spots;                // per light; spotlight constructor state
     std::vector<float> albedo, emission, rough;  // physical-mode per-triangle params
     std::vector<int> emissive;                   // emissive triangle ids
     std::vector<double> emissive_cdf;            // by power (luminance-free: r+g+b) x area
@@ -763,13 +792,84 @@ Col ss_reflect(const dr_material &m, const Tri &v, const Tri &nt, V3 hit, V3 pho
     return col(m.color) * ((diff * rc) + (gloss * std::pow(oc, m.shininess)));
 }
 
+// Shaders::FresnelShader::getReflectedColor (FresnelShader.impl.cuh:14-19, DumbStructs.cuh:136-140):
+// Schlick term of the interpolated (not normalised) normal and the reversed photon direction.
+Col fresnel_reflect(const dr_material &m, const Tri &v, const Tri &nt, V3 hit, V3 photon_dir) {
+    V3 masses = get_masses(v, hit);
+    V3 light = -normalized(photon_dir);
+    V3 normal = mass_center(nt, masses);
+    float val = (1.0f - dot(normal, light));
+    float sq = (val * val);
+    float f = sq * sq * val;
+    Col c = col(m.color);
+    return Col{c.r + ((1.0f - c.r) * f), c.g + ((1.0f - c.g) * f), c.b + ((1.0f - c.b) * f)};
+}
+
+// DefaultShaderGeneric (DefaultShader.impl.cuh:3-52): the sample is the reflection of the ray about
+// the interpolated normal; the reflected colour uses the observer (hit + direction) - hit.
+V3 default_request(const Tri &v, const Tri &nt, V3 hit, V3 raydir) { return reflection(raydir, mass_center(nt, get_masses(v, hit))); }
+Col default_reflect(const dr_material &m, const Tri &v, const Tri &nt, V3 hit, V3 photon_dir, V3 observer) {
+    float diff, gloss;
+    ss_params(m, diff, gloss);
+    V3 normal = mass_center(nt, get_masses(v, hit));
+    V3 cam = (hit + observer) - hit;
+    V3 refl = reflection(photon_dir, normal);
+    float cosL = std::fmax(dot(refl, normal) / std::sqrt(sqrmag(refl) * sqrmag(normal)), 0.0f);
+    float oc = std::fmax(dot(refl, cam) / std::sqrt(sqrmag(refl) * sqrmag(cam)), 0.0f);
+    return col(m.color) * ((diff * cosL) + (gloss * std::pow(oc, m.shininess)));
+}
+
 // Material::getReflectedColor dispatch; photon colour factored out.
 Col reflect(const Scene &S, int tri, V3 hit, V3 photon_dir, V3 observer, bool direct, int sample_type, bool &pass) {
     const dr_material &m = S.mats[S.mat[tri]];
     pass = false;
     if (m.type == DR_MAT_DUMB_BASED)
         return dumb_based_reflect(m, S.tree.tri[tri], S.nrm[tri], hit, photon_dir, observer, direct, sample_type, pass);
+    if (m.type == DR_MAT_FRESNEL) return fresnel_reflect(m, S.tree.tri[tri], S.nrm[tri], hit, photon_dir);
+    if (m.type == DR_MAT_DEFAULT) return default_reflect(m, S.tree.tri[tri], S.nrm[tri], hit, photon_dir, observer);
     return ss_reflect(m, S.tree.tri[tri], S.nrm[tri], hit, photon_dir, observer);
+}
+
+// Spotlight::getVertexPhotons, photon k (Spotlight.impl.cuh:35-77); false where the reference skips
+// the photon.  Random dimensions 4096 + 64 li + 3 k.
+bool spot_photon(const dr_light &l, const Spot &sp, V3 point, uint32_t key, uint32_t bounce, int li, int k, V3 &o, V3 &d,
+                 Col &c) {
+    const uint32_t d0 = 4096u + 64u * (uint32_t)li + 3u * (uint32_t)k;
+    const V3 dir = sp.direction;
+    V3 non_dir = (dir.z > 0.9f) ? v3(1.0f, 0.0f, 0.0f) : v3(0.0f, 0.0f, 1.0f);
+    V3 ver = normalized(cross(dir, non_dir));
+    V3 hor = cross(dir, ver);
+    V3 pos;
+    if (sp.sphere) {
+        pos = point_on_sphere(rnd(key, bounce, d0), rnd(key, bounce, d0 + 1), sp.emitter);
+        pos = pos * rnd(key, bounce, d0 + 2);
+        pos = pos + col3(l.position);
+    } else {
+        float angle = (rnd(key, bounce, d0) * ((2.0f * PI_F) - 0.0f)) + 0.0f;
+        V3 ring = (ver * std::cos(angle)) + (hor * std::sin(angle));
+        pos = col3(l.position) + ((ring * sp.emitter) * std::sqrt(rnd(key, bounce, d0 + 1)));
+    }
+    V3 delta = point - pos;
+    float sqr_distance = sqrmag(delta);
+    if (sqr_distance < EPS) return false;
+    float distance = std::sqrt(sqr_distance);
+    float base = (sp.emitter * sp.emitter);
+    float spread = std::fmax(1.0f - sp.outer_cos, EPS);
+    float surface = ((sp.sphere ? 0.0f : base) + (sqr_distance * spread));
+    float s = (base / (((float)sp.samples) * surface));
+    c = sp.color * s;
+    float inv = 1.0f / distance;
+    V3 dd = delta * inv;
+    float cosine = dot(dd, dir);
+    if (cosine < sp.inner_cos) {
+        if (cosine < sp.outer_cos) return false;
+        float a = ((sp.inner_cos - cosine) / (sp.inner_cos - sp.outer_cos));
+        float b = (1.0f - a);
+        c = c * std::pow((a * b * b) + (b * (1.0f - (a * a))), sp.falloff);
+    }
+    o = pos;
+    d = dd;
+    return true;
 }
 
 // Light::getVertexPhotons: photon ray (origin, direction) and colour for a shading point.
@@ -888,7 +988,13 @@ Col ref_path(const Scene &S, const Cam &cam, const dr_render_params &p, float sx
         if (layer < p.max_bounces) {
             if (m.type == DR_MAT_DUMB_BASED)
                 have_child = dumb_based_request(m, S.tree.tri[hit], S.nrm[hit], hp, d, key, (uint32_t)layer, cd, ctype);
-            else {
+            else if (m.type == DR_MAT_FRESNEL)
+                have_child = false;
+            else if (m.type == DR_MAT_DEFAULT) {
+                cd = default_request(S.tree.tri[hit], S.nrm[hit], hp, d);
+                ctype = 0;
+                have_child = true;
+            } else {
                 cd = ss_request(m, S.tree.tri[hit], S.nrm[hit], hp, d, key, (uint32_t)layer);
                 ctype = 0;
                 have_child = true;
@@ -897,9 +1003,22 @@ Col ref_path(const Scene &S, const Cam &cam, const dr_render_params &p, float sx
         // direct light: photons cast from the light toward the point, DumbRenderer.cu:300-316, 361-428
         Col direct{0, 0, 0};
         for (int li = 0; li < (int)S.lights.size(); li++) {
+          const dr_light &L = S.lights[li];
+          const bool spot = L.type == DR_LIGHT_SPOTLIGHT;
+          const int count = spot ? S.spots[li].samples : 1;
+          for (int k = 0; k < count; k++) {
             V3 lo, ld;
             Col lc;
-            light_photon(S.lights[li], hp, key, (uint32_t)layer, li, lo, ld, lc);
+            if (spot) {
+                if (!spot_photon(L, S.spots[li], hp, key, (uint32_t)layer, li, k, lo, ld, lc)) continue;
+                if (!S.spots[li].shadows) {
+                    bool pass;
+                    direct = direct + reflect(S, hit, hp, ld, -d, true, 0, pass) * lc;
+                    continue;
+                }
+            } else {
+                light_photon(L, hp, key, (uint32_t)layer, li, lo, ld, lc);
+            }
             int restrict_obj = -1;
             for (int guard = 0; guard < 64; guard++) {
                 float lt;
@@ -921,6 +1040,7 @@ Col ref_path(const Scene &S, const Cam &cam, const dr_render_params &p, float sx
                     restrict_obj = lh;
                 } else break;
             }
+          }
         }
         total = total + thr * direct;
         if (!have_child) break;
@@ -1177,6 +1297,7 @@ void *dro_scene_create(const float *xyz, const float *nrm, const int *mat, int n
     }
     S->mats.assign(mats, mats + n_mats);
     S->lights.assign(lights, lights + n_lights);
+    for (int i = 0; i < n_lights; i++) S->spots.push_back(spot_state(lights[i]));
     S->albedo.resize(3 * (size_t)n);
     S->emission.assign(3 * (size_t)n, 0.0f);
     S->rough.resize(n);

@@ -8,8 +8,8 @@
 //   Octree<Renderable<BakedTriFace>>::push/build   __source__/DataStructures/Objects/Scene/Raycasters/Octree/Octree.impl.cuh:97-129
 //   Octree<...>::cast                              Octree.impl.cuh:174-212
 //   DumbRenderer (CPU threads) via Renderer::iterate  __source__/DataStructures/Renderers/Renderer/Renderer.cu:143-156
-//   DumbBasedShader / SimpleStochasticShader        __source__/DataStructures/Objects/Components/Shaders/*
-//   SphericalLightEmitter / SimpleSoftDirectionalLight / SimpleDirectionalLight   __source__/DataStructures/Objects/Scene/Lights/*
+//   DumbBasedShader / SimpleStochasticShader / FresnelShader / DefaultShader   __source__/DataStructures/Objects/Components/Shaders/*
+//   SphericalLightEmitter / SimpleSoftDirectionalLight / SimpleDirectionalLight / Spotlight   __source__/DataStructures/Objects/Scene/Lights/*
 //   DefaultPerspectiveLense / SimpleStochasticLense / Lenses::SphericalSegmentLense  __source__/DataStructures/Objects/Components/Lenses/*
 #include "DataStructures/Renderers/DumbRenderer/DumbRenderer.cuh"
 #include "DataStructures/Screen/FrameBuffer/BlockBasedFrameBuffer/BlockBasedFrameBuffer.cuh"
@@ -21,6 +21,9 @@
 #include "DataStructures/Objects/Scene/Lights/SphericalLightEmitter/SphericalLightEmitter.cuh"
 #include "DataStructures/Objects/Scene/Lights/SimpleSoftDirectionalLight/SimpleSoftDirectionalLight.cuh"
 #include "DataStructures/Objects/Scene/Lights/SimpleDirectionalLight/SimpleDirectionalLight.cuh"
+#include "DataStructures/Objects/Scene/Lights/Spotlight/Spotlight.cuh"
+#include "DataStructures/Objects/Components/Shaders/FresnelShader/FresnelShader.cuh"
+#include "DataStructures/Objects/Components/Shaders/DefaultShader/DefaultShader.cuh"
 #include "Namespaces/Images/Images.cuh"
 #include "Namespaces/MeshReader/MeshReader.h"
 #include <thread>
@@ -41,6 +44,41 @@ static BakedTriFace make_face(const float *v, const float *n) {
 	}
 	Triangle tex(Vector3(0, 0, 0), Vector3(1, 0, 0), Vector3(0, 1, 0));
 	return BakedTriFace(vert, norm, tex);
+}
+
+// Records (16 floats) of the reference objects the scene holds, built through their constructors.
+//   material: [0] 0 DumbBasedShader (fresnel [1..3], specular [4], diffuse [5..7], metal [8]),
+//             1 SimpleStochasticShader (colour [1..3], diffuse [4], smoothness [5], shininess [6]),
+//             2 Shaders::FresnelShader (colour [1..3]), 3 DefaultShader (as 1)
+//   light:    [0] 0 SphericalLightEmitter (colour [1..3], position [4..6], radius [7]),
+//             1 SimpleSoftDirectionalLight (colour, direction [4..6], distance [7], softness [8]),
+//             2 SimpleDirectionalLight (colour, direction, distance [7]),
+//             3 Lights::Spotlight (colour, position [4..6], direction [7..9], luminosity [10], hotspot
+//               [11] and falloff [12] angles, falloff power [13], emitter size [14], flags [15]:
+//               1 emit from sphere, 2 cast shadows, samples << 2)
+void ref_material(Material<BakedTriFace> &dst, const float *m) {
+	const int type = (int)m[0];
+	if (type == 0)
+		dst.use<DumbBasedShader>((ColoredTexture)ColorRGB(m[1], m[2], m[3]), m[4], (ColoredTexture)ColorRGB(m[5], m[6], m[7]), m[8]);
+	else if (type == 1)
+		dst.use<SimpleStochasticShader>(ColorRGB(m[1], m[2], m[3]), m[4], m[5], m[6]);
+	else if (type == 2)
+		dst.use<Shaders::FresnelShader>(ColoredTexture(Color(m[1], m[2], m[3], 1.0f)));
+	else
+		dst.use<DefaultShader>(ColorRGB(m[1], m[2], m[3]), m[4], m[5], m[6]);
+}
+void ref_light(Light &dst, const float *l) {
+	const int type = (int)l[0];
+	Color c(l[1], l[2], l[3], 1.0f);
+	Vector3 v(l[4], l[5], l[6]);
+	if (type == 0) dst.use<SphericalLightEmitter>(c, v, l[7]);
+	else if (type == 1) dst.use<SimpleSoftDirectionalLight>(c, v, l[7], l[8]);
+	else if (type == 2) dst.use<SimpleDirectionalLight>(c, v, l[7]);
+	else {
+		const int flags = (int)l[15];
+		dst.use<Lights::Spotlight>(c, l[10], v, Vector3(l[7], l[8], l[9]), l[11], l[12], l[13], l[14],
+			(flags & 1) != 0, (flags & 2) != 0, flags >> 2);
+	}
 }
 
 extern "C" {
@@ -108,20 +146,12 @@ void *dref_scene_create(const float *xyz, const float *nrm, const int *mat, int 
 	for (int i = 0; i < n_mats; i++) {
 		const float *m = mats + 16 * i;
 		Material<BakedTriFace> &dst = s->scene.materials.cpuHandle()->operator[](i);
-		if ((int)m[0] == 0)
-			dst.use<DumbBasedShader>((ColoredTexture)ColorRGB(m[1], m[2], m[3]), m[4], (ColoredTexture)ColorRGB(m[5], m[6], m[7]), m[8]);
-		else
-			dst.use<SimpleStochasticShader>(ColorRGB(m[1], m[2], m[3]), m[4], m[5], m[6]);
+		ref_material(dst, m);
 	}
 	s->scene.lights.cpuHandle()->flush(n_lights);
 	for (int i = 0; i < n_lights; i++) {
 		const float *l = lights + 16 * i;
-		Light &dst = s->scene.lights.cpuHandle()->operator[](i);
-		Color c(l[1], l[2], l[3], 1.0f);
-		Vector3 v(l[4], l[5], l[6]);
-		if ((int)l[0] == 0) dst.use<SphericalLightEmitter>(c, v, l[7]);
-		else if ((int)l[0] == 1) dst.use<SimpleSoftDirectionalLight>(c, v, l[7], l[8]);
-		else dst.use<SimpleDirectionalLight>(c, v, l[7]);
+		ref_light(s->scene.lights.cpuHandle()->operator[](i), l);
 	}
 	int lens = (int)cam[0];
 	if (lens == 0) s->camera.cpuHandle()->lense.use<DefaultPerspectiveLense>(cam[1]);

@@ -37,8 +37,15 @@
 #include "DataStructures/Objects/Scene/Lights/SphericalLightEmitter/SphericalLightEmitter.cuh"
 #include "DataStructures/Objects/Scene/Lights/SimpleSoftDirectionalLight/SimpleSoftDirectionalLight.cuh"
 #include "DataStructures/Objects/Components/Lenses/DefaultPerspectiveLense/DefaultPerspectiveLense.cuh"
+#include "DataStructures/Objects/Components/Shaders/FresnelShader/FresnelShader.cuh"
+#include "DataStructures/Objects/Components/Shaders/DefaultShader/DefaultShader.cuh"
+#include "DataStructures/Objects/Scene/Lights/Spotlight/Spotlight.cuh"
 #include "DataStructures/Objects/Scene/Lights/SimpleDirectionalLight/SimpleDirectionalLight.cuh"
 #include "DataStructures/Screen/FrameBuffer/BlockBasedFrameBuffer/BlockBasedFrameBuffer.cuh"
+
+// Reference objects from records (oracle/ref_driver.cu).
+void ref_material(Material<BakedTriFace> &dst, const float *m);
+void ref_light(Light &dst, const float *l);
 
 namespace {
 
@@ -69,6 +76,19 @@ DREF_ROB(RobSegAlpha, Lenses::SphericalSegmentLense, Vector2, alpha)
 DREF_ROB(RobSegDist, Lenses::SphericalSegmentLense, float, dist)
 DREF_ROB(RobSegSoft, Lenses::SphericalSegmentLense, float, soft)
 DREF_ROB(RobSegFilter, Lenses::SphericalSegmentLense, Color, filter)
+DREF_ROB(RobFresnelColor, Shaders::FresnelShader, ColoredTexture, color)
+DREF_ROB(RobDefAlbedo, DefaultShader, ColorRGB, albedo)
+DREF_ROB(RobDefDiff, DefaultShader, float, diff)
+DREF_ROB(RobDefGloss, DefaultShader, float, gloss)
+DREF_ROB(RobDefShine, DefaultShader, float, shininess)
+DREF_ROB(RobSpotColor, Lights::Spotlight, Color, color)
+DREF_ROB(RobSpotPos, Lights::Spotlight, Vector3, position)
+DREF_ROB(RobSpotDir, Lights::Spotlight, Vector3, direction)
+DREF_ROB(RobSpotEmit, Lights::Spotlight, float, emitterSize)
+DREF_ROB(RobSpotInner, Lights::Spotlight, float, innerCosine)
+DREF_ROB(RobSpotOuter, Lights::Spotlight, float, outerCosine)
+DREF_ROB(RobSpotFalloff, Lights::Spotlight, float, outerFalloff)
+DREF_ROB(RobSpotFlags, Lights::Spotlight, uint8_t, flags)
 
 DumbRenderContextData *ctx_data(DumbRenderContext *c) { return (DumbRenderContextData *)(c->*get(RobData())); }
 
@@ -85,6 +105,8 @@ bool is_type(const Generic_ &g) {
 //     DumbBased: [1..3] fresnelColor, [4..6] diffuseColor (constructor-scaled), [7] spec,
 //       [8] specMass, [9] alphaCutoutThreshold, [10..13] texture ids fresnel/diffuse/normal/alpha
 //     SimpleStochastic: [1..3] albedo, [4] diff, [5] gloss, [6] shine
+//     (2) FresnelShader: [1..3] colour, [4] texture id;  (3) DefaultShader: [1..3] albedo, [4] diff,
+//       [5] gloss, [6] shininess
 void dump_material(const Material<BakedTriFace> &m, float *o) {
 	std::memset(o, 0, 16 * sizeof(float));
 	typedef Shader<BakedTriFace> Pack;
@@ -103,10 +125,22 @@ void dump_material(const Material<BakedTriFace> &m, float *o) {
 		o[0] = 1;
 		o[1] = a.r; o[2] = a.g; o[3] = a.b;
 		o[4] = s->*get(RobDiff()); o[5] = s->*get(RobGloss()); o[6] = s->*get(RobShine());
+	} else if (is_type<Pack, Material<BakedTriFace>, Shaders::FresnelShader>(m)) {
+		const ColoredTexture &c = m.getObject<Shaders::FresnelShader>()->*get(RobFresnelColor());
+		o[0] = 2;
+		o[1] = c.color.r; o[2] = c.color.g; o[3] = c.color.b; o[4] = (float)c.textureId;
+	} else if (is_type<Pack, Material<BakedTriFace>, DefaultShader>(m)) {
+		const DefaultShader *s = m.getObject<DefaultShader>();
+		const ColorRGB &a = s->*get(RobDefAlbedo());
+		o[0] = 3;
+		o[1] = a.r; o[2] = a.g; o[3] = a.b;
+		o[4] = s->*get(RobDefDiff()); o[5] = s->*get(RobDefGloss()); o[6] = s->*get(RobDefShine());
 	} else o[0] = -1;
 }
-//   light: [0]=type (0 SphericalLightEmitter, 1 SimpleSoftDirectionalLight, 2 SimpleDirectionalLight, -1 other)
+//   light: [0]=type (0 SphericalLightEmitter, 1 SimpleSoftDirectionalLight, 3 Lights::Spotlight, -1 other)
 //     spherical: [1..3] col, [4..6] pos, [7] rad;  soft directional: [1..3] color, [4..6] dir, [7] dist, [8] soft
+//     spotlight: [1..3] color (x luminosity), [4..6] position, [7..9] direction, [10] emitterSize,
+//       [11] innerCosine, [12] outerCosine, [13] outerFalloff, [14] flags
 void dump_light(const Light &l, float *o) {
 	std::memset(o, 0, 16 * sizeof(float));
 	if (is_type<LightInterface, Light, SphericalLightEmitter>(l)) {
@@ -119,6 +153,15 @@ void dump_light(const Light &l, float *o) {
 		o[0] = 1;
 		o[1] = s->color.r; o[2] = s->color.g; o[3] = s->color.b;
 		o[4] = s->dir.x; o[5] = s->dir.y; o[6] = s->dir.z; o[7] = s->dist; o[8] = s->soft;
+	} else if (is_type<LightInterface, Light, Lights::Spotlight>(l)) {
+		const Lights::Spotlight *s = l.getObject<Lights::Spotlight>();
+		const Color &c = s->*get(RobSpotColor());
+		const Vector3 &p = s->*get(RobSpotPos()), &d = s->*get(RobSpotDir());
+		o[0] = 3;
+		o[1] = c.r; o[2] = c.g; o[3] = c.b;
+		o[4] = p.x; o[5] = p.y; o[6] = p.z; o[7] = d.x; o[8] = d.y; o[9] = d.z;
+		o[10] = s->*get(RobSpotEmit()); o[11] = s->*get(RobSpotInner()); o[12] = s->*get(RobSpotOuter());
+		o[13] = s->*get(RobSpotFalloff()); o[14] = (float)(s->*get(RobSpotFlags()));
 	} else o[0] = -1;
 }
 //   lens: [0]=type (0 DefaultPerspectiveLense, 1 SimpleStochasticLense, 2 SphericalSegmentLense, -1 other/none)
@@ -235,19 +278,12 @@ void dref_dumb_settings(void *h, int *out) {
 // so a loader's output can be compared with the reference's field by field.
 void dref_record_material(const float *m, float *out) {
 	Material<BakedTriFace> mat;
-	if ((int)m[0] == 0)
-		mat.use<DumbBasedShader>((ColoredTexture)ColorRGB(m[1], m[2], m[3]), m[4], (ColoredTexture)ColorRGB(m[5], m[6], m[7]), m[8]);
-	else
-		mat.use<SimpleStochasticShader>(ColorRGB(m[1], m[2], m[3]), m[4], m[5], m[6]);
+	ref_material(mat, m);
 	dump_material(mat, out);
 }
 void dref_record_light(const float *l, float *out) {
 	Light light;
-	Color c(l[1], l[2], l[3], 1.0f);
-	Vector3 v(l[4], l[5], l[6]);
-	if ((int)l[0] == 0) light.use<SphericalLightEmitter>(c, v, l[7]);
-	else if ((int)l[0] == 1) light.use<SimpleSoftDirectionalLight>(c, v, l[7], l[8]);
-	else light.use<SimpleDirectionalLight>(c, v, l[7]);
+	ref_light(light, l);
 	dump_light(light, out);
 }
 void dref_record_lens(const float *cam, float *out) {

@@ -179,24 +179,34 @@ def ref_cast(tris, o, d, cull=True, threads=8):
 
 
 def ref_material_record(m: dr.DrMaterial) -> np.ndarray:
+    """Constructor record for oracle/ref_driver.cu's ref_material."""
     r = np.zeros(16, np.float32)
     if m.type == dr.MAT_DUMB_BASED:
         r[:9] = [0, *m.fresnel, m.specular, *m.color, m.metal]
     elif m.type == dr.MAT_SIMPLE_STOCHASTIC:
         r[:7] = [1, *m.color, m.diffuse, m.smoothness, m.shininess]
+    elif m.type == dr.MAT_FRESNEL:
+        r[:4] = [2, *m.color]
+    elif m.type == dr.MAT_DEFAULT:
+        r[:7] = [3, *m.color, m.diffuse, m.smoothness, m.shininess]
     else:
         raise ValueError("material has no reference counterpart")
     return r
 
 
 def ref_light_record(l: dr.DrLight) -> np.ndarray:
+    """Constructor record for oracle/ref_driver.cu's ref_light."""
     r = np.zeros(16, np.float32)
     if l.type == dr.LIGHT_SPHERICAL:
         r[:8] = [0, *l.color, *l.position, l.radius]
     elif l.type == dr.LIGHT_SOFT_DIRECTIONAL:
         r[:9] = [1, *l.color, *l.direction, l.distance, l.softness]
-    else:
+    elif l.type == dr.LIGHT_DIRECTIONAL:
         r[:8] = [2, *l.color, *l.direction, l.distance]
+    else:
+        flags = (1 if l.emit_from_sphere else 0) | (2 if l.cast_shadows else 0) | (int(l.samples) << 2)
+        r[:16] = [3, *l.color, *l.position, *l.direction, l.luminosity, l.hotspot_angle, l.falloff_angle,
+                  l.falloff_power, l.emitter_size, flags]
     return r
 
 

@@ -7,7 +7,10 @@
   cast_c1.npz      the 20,492-triangle box + icosphere level 5 geometry; 16,384 incoherent rays,
                    culling on.
   render_*.npz     reference DumbRenderer CPU renders (four independent runs of 512 progressive
-                   iterations each) of small reference-expressible scenes, 32x32.
+                   iterations each) of small reference-expressible scenes, 32x32: a room and a sphere
+                   of each reference shader (DumbBased diffuse / metal, SimpleStochastic, Fresnel,
+                   Default) under a spherical light, and under spotlights (disc emitter with shadows;
+                   sphere emitter without shadows beside a soft directional light).
   scene_file/      a scene file (scene.dumb including materials.dumb, meshes in props.obj) that uses
                    presets, groups with fallback / override materials, rotated and scaled items and a
                    rotated spherical-segment camera; render_scene_file.npz holds the reference's renders
@@ -64,20 +67,36 @@ def render_scene(kind: str):
     mat[len(room):] = 2
     white = dr.dumb_based(diffuse=(0.7, 0.7, 0.7), metal=0.0)
     red = dr.dumb_based(diffuse=(0.7, 0.1, 0.1), metal=0.0)
-    if kind == "diffuse":
+    if kind in ("diffuse", "spot", "spot_open"):
         obj = dr.dumb_based(diffuse=(0.5, 0.6, 0.7), metal=0.0)
     elif kind == "metal":
         obj = dr.dumb_based(fresnel=(1.022, 0.782, 0.344), specular=16.0, diffuse=(1.0, 1.0, 1.0), metal=0.5)
+    elif kind == "fresnel":
+        obj = dr.fresnel_shader((0.9, 0.6, 0.3))
+    elif kind == "default":
+        obj = dr.default_shader((0.8, 0.8, 0.9), 0.5, 0.4, 16.0)
     else:
         obj = dr.simple_stochastic((0.9, 0.9, 0.9), 0.3, 0.7, 8.0)
     mats = [white, red, obj]
-    lights = [dr.spherical_light((1.5, 1.5, 1.5), (0.0, 0.8, 0.0), 0.1)]
+    if kind == "spot":
+        lights = [dr.spotlight((1.0, 0.95, 0.9), 150.0, (0.0, 0.9, 0.0), (0.1, -1.0, 0.15), 20.0, 50.0, 1.5, 0.1,
+                               emit_from_sphere=False, cast_shadows=True, samples=4)]
+    elif kind == "spot_open":
+        # emitter and shadowed light kept away from every surface (no near-singular 1/d^2 samples)
+        lights = [dr.spotlight((0.9, 0.95, 1.0), 60.0, (0.3, 0.75, -0.2), (-0.2, -1.0, 0.1), 25.0, 60.0, 1.0, 0.08,
+                               emit_from_sphere=True, cast_shadows=False, samples=3),
+                  dr.soft_directional_light((0.3, 0.3, 0.3), (0.3, -1.0, 0.2), 3.0, 0.05)]
+    else:
+        lights = [dr.spherical_light((1.5, 1.5, 1.5), (0.0, 0.8, 0.0), 0.1)]
     cam = dr.camera(dr.LENS_SIMPLE_STOCHASTIC, position=(0.0, 0.0, -0.95), angle=60.0)
     return tris, mat, mats, lights, cam
 
 
-def render_fixtures(iterations=512, runs=4, size=32, bounces=2):
-    for kind in ("diffuse", "metal", "ss"):
+RENDER_KINDS = ("diffuse", "metal", "ss", "fresnel", "default", "spot", "spot_open")
+
+
+def render_fixtures(iterations=512, runs=4, size=32, bounces=2, kinds=RENDER_KINDS):
+    for kind in kinds:
         tris, mat, mats, lights, cam = render_scene(kind)
         out, secs = [], 0.0
         for _ in range(runs):
@@ -192,6 +211,9 @@ if __name__ == "__main__":
         cast_fixtures()
     if not only or "render" in only:
         render_fixtures()
+    for k in only:
+        if k.startswith("render_"):
+            render_fixtures(kinds=(k[len("render_"):],))
     if not only or "scene_file" in only:
         scene_file_fixtures()
     print("golden fixtures written to", OUT)

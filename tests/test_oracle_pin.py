@@ -41,7 +41,7 @@ def test_oracle_cast_matches_live_reference():
 
 
 
-@pytest.mark.parametrize("kind", ["diffuse", "metal", "ss"])
+@pytest.mark.parametrize("kind", ["diffuse", "metal", "ss", "fresnel", "default", "spot", "spot_open"])
 def test_oracle_render_matches_reference_statistically(kind):
     """4 oracle runs (256 spp each) vs 4 reference DumbRenderer runs (512 iterations each): MSE of
     the run means within 1.5x of what the runs' own per-pixel variances predict; image means within

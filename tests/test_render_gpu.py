@@ -53,11 +53,15 @@ def _ref_scene(kind, light="spherical"):
         lights = [dr.directional_light((1.0, 0.9, 0.8), (0.2, -1.0, 0.1), 3.0)]
     elif light == "two":
         lights = lights + [dr.soft_directional_light((0.5, 0.5, 0.8), (-0.3, -1.0, 0.2), 3.0, 0.02)]
+    elif light == "spot":
+        lights = render_scene("spot")[3]
+    elif light == "spot_open":
+        lights = render_scene("spot_open")[3]
     return tris, mat, mats, lights, cam
 
 
-@pytest.mark.parametrize("kind", ["diffuse", "metal", "ss"])
-@pytest.mark.parametrize("light", ["spherical", "soft", "directional", "two"])
+@pytest.mark.parametrize("kind", ["diffuse", "metal", "ss", "fresnel", "default"])
+@pytest.mark.parametrize("light", ["spherical", "soft", "directional", "two", "spot", "spot_open"])
 def test_reference_mode_matches_oracle(cuda, kind, light):
     tris, mat, mats, lights, cam = _ref_scene(kind, light)
     sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights)
@@ -115,7 +119,7 @@ def test_block_range_and_progressive_blend(cuda):
     _compare(dr.blockmajor_to_image(g, W, H), dr.blockmajor_to_image(ofb, W, H))
 
 
-@pytest.mark.parametrize("kind", ["diffuse", "metal", "ss"])
+@pytest.mark.parametrize("kind", ["diffuse", "metal", "ss", "fresnel", "default", "spot", "spot_open"])
 def test_gpu_matches_reference_renderer_statistically(cuda, kind):
     """8 GPU runs (1024 spp each) vs 4 reference DumbRenderer runs (golden fixture, 512 iterations
     each): MSE of the run means within 1.5x of the predicted variance, image means within 4 SE."""

@@ -149,6 +149,26 @@ VARIANTS = {
       "objects": [ { %s, "material": "m" } ],
       "camera": { "lense": { "type": "simple_stochastic" } },
       "renderer": { "pixel": { "boxing": "min" } } }""" % (OBJ % "cube"),
+    # fresnel_color (engine colours, colour override, an unknown engine colour the reference ignores)
+    # and spotlights (defaults, target, folded angles, sphere emitter, no shadows, sample clamping,
+    # an unknown emitter shape the reference ignores)
+    "fresnel_and_spotlight": """{ "materials": [
+        { "name": "f0", "type": "fresnel_color" },
+        { "name": "f1", "type": "fresnel_color", "engine_color": "copper" },
+        { "name": "f2", "type": "fresnel_color", "engine_color": "silver", "color": [ 0.5, 0.6, 0.7 ] },
+        { "name": "f3", "type": "fresnel_color", "engine_color": "unobtainium", "texture": null },
+        { "name": "f4", "type": "fresnel_color", "engine_color": "iron" },
+        { "name": "f5", "type": "fresnel_color", "engine_color": "gold" },
+        { "name": "f6", "type": "fresnel_color", "engine_color": "aluminum" } ],
+      "lights": [
+        { "type": "spotlight" },
+        { "type": "spotlight", "color": [ 1, 0.5, 0.2 ], "luminosity": 300, "position": [ 1, 2, 3 ], "target": [ 0, 0, 0 ],
+          "hotspot_angle": 20, "falloff_angle": 10, "falloff_power": 2, "emitter_size": 0.5, "emitter_shape": "sphere",
+          "cast_shadows": false, "sample_count": 40 },
+        { "type": "spotlight", "direction": [ 0, -1, 0.2 ], "hotspot_angle": -30, "falloff_angle": 200, "emitter_size": 0,
+          "emitter_shape": "cone", "sample_count": -2 },
+        { "type": "spotlight", "hotspot_angle": 250, "falloff_angle": -5, "direction": [ 3, 0, 0 ], "sample_count": 7 } ],
+      "objects": [ { %s, "material": "f1" } ] }""" % (OBJ % "cube"),
     "no_camera": """{ "materials": [ { "name": "m", "type": "dumb_based" } ],
       "objects": [ { %s, "material": "m" } ], "camera": { "transform": { "rotation": [ 0, 90, 0 ] } } }"""
     % (OBJ % "cube"),
@@ -212,9 +232,8 @@ def test_errors(tmp_path, text, needle):
 
 @pytest.mark.parametrize("text,needle", [
     # what this renderer has no counterpart for
-    ('{ "materials": [ { "type": "fresnel_color" } ] }', "not supported"),
-    ('{ "lights": [ { "type": "spotlight" } ] }', "not supported"),
     ('{ "materials": [ { "type": "dumb_based", "diffuse_texture": { "png": "t.png" } } ] }', "textures"),
+    ('{ "materials": [ { "type": "fresnel_color", "texture": { "png": "t.png" } } ] }', "textures"),
     ('{ "materials": [ { "type": "dumb_based", "fresnel_texture": "named" } ] }', "textures"),
     # the reference leaves primitives unimplemented (and dereferences a missing mesh afterwards)
     ('{ "objects": [ { "mesh": { "primitive": "sphere" }, "material": { "type": "dumb_based" } } ] }', "primitive"),
