@@ -136,6 +136,12 @@ def lib() -> ctypes.CDLL:
     L.dr_renderer_set_profiling.argtypes = [vp, i32]
     L.dr_renderer_kernel_times.restype = i32
     L.dr_renderer_kernel_times.argtypes = [vp, vp, vp]
+    L.dr_renderer_kernel_busy.restype = i32
+    L.dr_renderer_kernel_busy.argtypes = [vp, vp]
+    L.dr_renderer_set_lanes.restype = i32
+    L.dr_renderer_set_lanes.argtypes = [vp, i32]
+    L.dr_renderer_lanes.restype = i32
+    L.dr_renderer_lanes.argtypes = [vp]
     L.dr_renderer_set_counting.restype = i32
     L.dr_renderer_set_counting.argtypes = [vp, i32]
     L.dr_renderer_counters.restype = i32
@@ -539,10 +545,12 @@ def cast(scene: Scene, origins, directions, ignore=None, cull_backfaces=True, co
 class Renderer:
     """Owns the wavefront scratch of one caller (dr_renderer)."""
 
-    def __init__(self, wave_paths: int = 0):
+    def __init__(self, wave_paths: int = 0, lanes: int = 0):
         h = ctypes.c_void_p()
         check(lib().dr_renderer_create(int(wave_paths), ctypes.byref(h)))
         self._h = h
+        if lanes:
+            self.set_lanes(lanes)
 
     @property
     def handle(self):
@@ -560,6 +568,20 @@ class Renderer:
         n = np.zeros(5, np.int64)
         check(lib().dr_renderer_kernel_times(self._h, ms.ctypes.data, n.ctypes.data))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("camera", "trace", "shade", "shadow", "resolve"))}
+
+    def kernel_busy(self):
+        """{class: ms}: union of each class's launch intervals over all lanes since profiling began."""
+        b = np.zeros(5, np.float64)
+        check(lib().dr_renderer_kernel_busy(self._h, b.ctypes.data))
+        return {k: float(b[i]) for i, k in enumerate(("camera", "trace", "shade", "shadow", "resolve"))}
+
+    def set_lanes(self, lanes: int):
+        """Concurrent wave pipelines of one render (dr_renderer_set_lanes)."""
+        check(lib().dr_renderer_set_lanes(self._h, int(lanes)))
+
+    @property
+    def lanes(self) -> int:
+        return int(lib().dr_renderer_lanes(self._h))
 
     def set_counting(self, enable: bool):
         check(lib().dr_renderer_set_counting(self._h, 1 if enable else 0))

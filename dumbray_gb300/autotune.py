@@ -69,9 +69,10 @@ def tune_leaf_threshold(make_scene, scenes_by_class, camera_for, probe=(512, 512
     return best, table
 
 
-def tune_wave(batch, candidates=(1 << 20, 1 << 21, 1 << 22, 1 << 23), use_graph=True):
+def tune_wave(batch, candidates=(1 << 20, 1 << 21, 1 << 22, 1 << 23), use_graph=True, lanes=0):
     """Times one batch render per candidate wave size; returns (best, {wave: ms}, renderer of the best).
-    Candidates above the batch's path count are skipped (a wave never exceeds the batch)."""
+    Candidates above the batch's path count are skipped (a wave never exceeds the batch).  ``lanes``:
+    concurrent wave pipelines of the renderers (0 = library default)."""
     import dumbray_gb300 as dr
 
     table = {}
@@ -80,7 +81,7 @@ def tune_wave(batch, candidates=(1 << 20, 1 << 21, 1 << 22, 1 << 23), use_graph=
     for w in candidates:
         if w > 2 * max(total, 1):
             continue
-        r = dr.Renderer(w)
+        r = dr.Renderer(w, lanes)
         ms = _time_ms(lambda: batch.render(r, use_graph=use_graph), reps=1)
         table[w] = round(ms, 2)
         if ms < best_ms:

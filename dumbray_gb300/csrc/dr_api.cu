@@ -90,6 +90,41 @@ struct dr_octree {
     drb::FlatOctree tree;
 };
 
+// The scratch of one wave pipeline: double-buffered ray queues, hits, shadow queue, control block.
+struct WaveScratch {
+    float4 *q[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
+    int4 *q3[2] = {nullptr, nullptr};
+    float2 *hits = nullptr;
+    float4 *s[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    void *ctrl = nullptr;
+    cudaStream_t stream = nullptr;  // extra lanes only
+    cudaEvent_t done = nullptr;     // extra lanes only
+
+    cudaError_t alloc(size_t wave, size_t shadow) {
+        cudaError_t e = cudaSuccess;
+        for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+            for (int j = 0; j < 3 && e == cudaSuccess; j++) e = cudaMalloc((void **)&q[k][j], sizeof(float4) * wave);
+            if (e == cudaSuccess) e = cudaMalloc((void **)&q3[k], sizeof(int4) * wave);
+        }
+        if (e == cudaSuccess) e = cudaMalloc((void **)&hits, sizeof(float2) * wave);
+        for (int j = 0; j < 5 && e == cudaSuccess; j++) e = cudaMalloc((void **)&s[j], sizeof(float4) * shadow);
+        if (e == cudaSuccess) e = cudaMalloc(&ctrl, drk::ctrl_bytes());
+        return e;
+    }
+    void release() {
+        for (int k = 0; k < 2; k++) {
+            for (int j = 0; j < 3; j++) cudaFree(q[k][j]);
+            cudaFree(q3[k]);
+        }
+        cudaFree(hits);
+        for (auto *p : s) cudaFree(p);
+        cudaFree(ctrl);
+        if (done) cudaEventDestroy(done);
+        if (stream) cudaStreamDestroy(stream);
+        *this = WaveScratch();
+    }
+};
+
 struct dr_renderer {
     int capacity = 0;
     float4 *q[2][3] = {{nullptr, nullptr, nullptr}, {nullptr, nullptr, nullptr}};
@@ -106,6 +141,13 @@ struct dr_renderer {
     bool counting = false;
     int *prefix = nullptr;          // adjoint: per-path vertex triangles
     int prefix_paths = 0;
+    // Concurrent wave pipelines of dr_render_blocks: the renderer's own scratch on the caller's
+    // stream plus lanes - 1 extra scratch sets, each on its own stream, taking alternate waves of
+    // one render and adding into the same accumulator (one kernel's tail overlaps another
+    // pipeline's work).  Extra lanes are allocated on first use.
+    int lanes = 1;
+    std::vector<WaveScratch> extra;
+    cudaEvent_t fork = nullptr;
     // Identifies the current set of scratch buffers: a new value at creation and whenever a buffer a
     // captured batch graph points into is reallocated (process-unique, so a renderer created at
     // the address of a destroyed one never matches a graph captured for the old one).
@@ -127,6 +169,8 @@ struct dr_renderer {
         for (auto *p : s) cudaFree(p);
         cudaFree(accum);
         cudaFree(ctrl);
+        for (auto &l : extra) l.release();
+        if (fork) cudaEventDestroy(fork);
     }
 };
 
@@ -528,6 +572,7 @@ dr_status dr_renderer_create(int32_t wave_paths, dr_renderer **out) {
     if (!r) return fail(DR_E_NOMEM, "dr_renderer_create: out of host memory");
     r->capacity = wave_paths;
     r->shadow_capacity = wave_paths * 2;
+    r->lanes = DR_DEFAULT_LANES;
     size_t W = (size_t)wave_paths;
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < 2 && e == cudaSuccess; k++) {
@@ -551,10 +596,27 @@ int64_t dr_renderer_launch_count(const dr_renderer *r) { return r ? r->launches 
 
 dr_status dr_renderer_set_profiling(dr_renderer *r, int32_t enable) {
     if (!r) return fail(DR_E_ARG, "dr_renderer_set_profiling: renderer is NULL");
-    r->prof.reset();
+    r->prof.reset(enable != 0);
     r->prof.enabled = enable != 0;
     return DR_OK;
 }
+
+dr_status dr_renderer_kernel_busy(dr_renderer *r, double *busy_ms) {
+    if (!r || !busy_ms) return fail(DR_E_ARG, "dr_renderer_kernel_busy: NULL argument");
+    cudaError_t e = r->prof.harvest();
+    if (e != cudaSuccess) return cuda_fail(e, "dr_renderer_kernel_busy");
+    r->prof.busy(busy_ms);
+    return DR_OK;
+}
+
+dr_status dr_renderer_set_lanes(dr_renderer *r, int32_t lanes) {
+    if (!r) return fail(DR_E_ARG, "dr_renderer_set_lanes: renderer is NULL");
+    if (lanes < 1 || lanes > DR_MAX_LANES) return fail(DR_E_ARG, "dr_renderer_set_lanes: lanes must be in [1, 8]");
+    r->lanes = lanes;
+    return DR_OK;
+}
+
+int32_t dr_renderer_lanes(const dr_renderer *r) { return r ? r->lanes : 0; }
 
 dr_status dr_renderer_kernel_times(dr_renderer *r, double *ms, int64_t *launches) {
     if (!r) return fail(DR_E_ARG, "dr_renderer_kernel_times: renderer is NULL");
@@ -671,16 +733,87 @@ static void wave_buffers(dr_renderer *r, drk::WaveDesc &W) {
     W.prefix = r->prefix;
 }
 
+// Wave size for `lanes` concurrent pipelines: at most `wave`, and small enough that a render of
+// `total` paths splits into about `lanes` balanced waves, but not below kMinLaneWave paths (smaller
+// waves cannot fill the GPU; such renders keep fewer lanes).
+constexpr long long kMinLaneWave = 1 << 18;
+static long long lane_wave(long long total, long long wave, int lanes) {
+    if (lanes <= 1) return wave;
+    long long w = (total + lanes - 1) / lanes;
+    w = std::max<long long>(w, kMinLaneWave);
+    w = ((w + 31) / 32) * 32;
+    return std::min<long long>(wave, w);
+}
+
+// Lanes a render of `total` paths in waves of `wave` uses: no more than it has waves.
+static int lanes_used(long long total, long long wave, int lanes) {
+    const long long n_waves = (total + wave - 1) / wave;
+    return (int)std::max<long long>(1, std::min<long long>(lanes, n_waves));
+}
+
+// Allocates the renderer's extra lanes up to `n` (same wave capacity as the renderer).
+static dr_status ensure_lanes(dr_renderer *r, int n) {
+    cudaError_t e = cudaSuccess;
+    if (!r->fork) e = cudaEventCreateWithFlags(&r->fork, cudaEventDisableTiming);
+    while (e == cudaSuccess && (int)r->extra.size() < n) {
+        WaveScratch l;
+        e = l.alloc((size_t)r->capacity, (size_t)r->shadow_capacity);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.done, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            l.release();
+            break;
+        }
+        r->extra.push_back(l);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "render: lane scratch");
+    return DR_OK;
+}
+
 // Issues the waves (and the resolve unless adjoint) of `total` paths over `total_slots` slots.
+// With lanes > 1, wave i runs on lane i % lanes: lane 0 is the renderer's own scratch on `stream`,
+// the others fork from and join back into `stream` through events.
 static dr_status run_waves(dr_renderer *r, drk::WaveDesc &W, long long total, long long wave, int total_slots, cudaStream_t stream,
-                           drk::Profiler *prof, bool count, bool resolve) {
+                           drk::Profiler *prof, bool count, bool resolve, int lanes = 1) {
     cudaError_t e = cudaMemsetAsync(r->accum, 0, sizeof(float4) * (size_t)std::max(total_slots, 1), stream);
     if (e != cudaSuccess) return cuda_fail(e, "render: clear accumulator");
-    for (long long b = 0; b < total; b += wave) {
-        W.wave_begin = b;
-        W.wave_count = (int)std::min<long long>(wave, total - b);
-        e = drk::launch_wave(W, stream, &r->launches, prof, count ? r->counters : nullptr);
+    const int L = lanes_used(total, wave, lanes);
+    if (L > 1) {
+        dr_status st = ensure_lanes(r, L - 1);
+        if (st != DR_OK) return st;
+        e = cudaEventRecord(r->fork, stream);
+        for (int k = 0; k < L - 1 && e == cudaSuccess; k++) e = cudaStreamWaitEvent(r->extra[k].stream, r->fork, 0);
+        if (e != cudaSuccess) return cuda_fail(e, "render: fork lanes");
+    }
+    long long i = 0;
+    for (long long b = 0; b < total; b += wave, i++) {
+        const int l = (int)(i % L);
+        drk::WaveDesc Wl = W;
+        cudaStream_t sl = stream;
+        if (l > 0) {
+            const WaveScratch &x = r->extra[l - 1];
+            for (int k = 0; k < 2; k++) {
+                Wl.q_p0[k] = x.q[k][0];
+                Wl.q_p1[k] = x.q[k][1];
+                Wl.q_p2[k] = x.q[k][2];
+                Wl.q_p3[k] = x.q3[k];
+            }
+            Wl.hits = x.hits;
+            for (int j = 0; j < 5; j++) Wl.s[j] = x.s[j];
+            Wl.ctrl = x.ctrl;
+            sl = x.stream;
+        }
+        Wl.wave_begin = b;
+        Wl.wave_count = (int)std::min<long long>(wave, total - b);
+        e = drk::launch_wave(Wl, sl, &r->launches, prof, count ? r->counters : nullptr);
         if (e != cudaSuccess) return cuda_fail(e, "render: wave");
+    }
+    if (L > 1) {
+        for (int k = 0; k < L - 1 && e == cudaSuccess; k++) {
+            e = cudaEventRecord(r->extra[k].done, r->extra[k].stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, r->extra[k].done, 0);
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "render: join lanes");
     }
     if (resolve) {
         e = drk::launch_resolve(W, total_slots, stream, &r->launches, prof);
@@ -713,8 +846,9 @@ dr_status dr_render_blocks(dr_renderer *r, const dr_scene *sc, const dr_camera *
     W.adjoint = false;
     wave_buffers(r, W);
     const int lights = (I.mode == DR_MODE_REFERENCE) ? I.S.shadow_photons : 1;
-    return run_waves(r, W, (long long)I.n_slots * I.spp, wave_size(r, lights, 1LL << 40), I.n_slots, stream, &r->prof, r->counting,
-                     true);
+    const long long total = (long long)I.n_slots * I.spp;
+    const long long wave = lane_wave(total, wave_size(r, lights, 1LL << 40), r->lanes);
+    return run_waves(r, W, total, wave, I.n_slots, stream, &r->prof, r->counting, true, r->lanes);
 }
 
 dr_status dr_render_adjoint(dr_renderer *r, const dr_scene *sc, const dr_camera *cam, const float *dl_dfb, int32_t start_block,
@@ -768,6 +902,7 @@ struct dr_batch {
     std::vector<dr_render_params> params;
     unsigned long long graph_scratch = 0;   // scratch_id of the renderer the graph was captured with
     long long graph_wave = 0;
+    int graph_lanes = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long graph_launches = 0;
@@ -940,7 +1075,8 @@ dr_status dr_batch_render(dr_renderer *r, dr_batch *b, int32_t use_graph, void *
     W.max_bounces = b->max_bounces;
     W.adjoint = false;
     wave_buffers(r, W);
-    const long long wave = wave_size(r, b->mode == DR_MODE_REFERENCE ? b->max_lights : 1, 1LL << 40);
+    const long long wave = lane_wave(b->total_paths, wave_size(r, b->mode == DR_MODE_REFERENCE ? b->max_lights : 1, 1LL << 40),
+                                     r->lanes);
     if (!b->done) {
         cudaError_t e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
         if (e != cudaSuccess) {
@@ -948,12 +1084,19 @@ dr_status dr_batch_render(dr_renderer *r, dr_batch *b, int32_t use_graph, void *
             return cuda_fail(e, "dr_batch_render: event");
         }
     }
+    const int lanes = lanes_used(b->total_paths, wave, r->lanes);
     if (!use_graph) {
-        st = run_waves(r, W, b->total_paths, wave, b->total_slots, stream, &r->prof, r->counting, true);
+        st = run_waves(r, W, b->total_paths, wave, b->total_slots, stream, &r->prof, r->counting, true, lanes);
         if (st == DR_OK) cudaEventRecord(b->done, stream);
         return st;
     }
-    if (b->exec == nullptr || b->graph_scratch != r->scratch_id || b->graph_wave != wave) {
+    if (b->exec == nullptr || b->graph_scratch != r->scratch_id || b->graph_wave != wave || b->graph_lanes != lanes) {
+        // lane scratch is allocated before the capture (no allocation while capturing); the lanes'
+        // streams join the capture through the fork event and leave it through their done events
+        if (lanes > 1) {
+            st = ensure_lanes(r, lanes - 1);
+            if (st != DR_OK) return st;
+        }
         b->drop_graph();
         cudaError_t e = cudaSuccess;
         if (!b->capture_stream) e = cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking);
@@ -962,7 +1105,7 @@ dr_status dr_batch_render(dr_renderer *r, dr_batch *b, int32_t use_graph, void *
         e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return cuda_fail(e, "dr_batch_render: begin capture");
         long long launches = r->launches;
-        st = run_waves(r, W, b->total_paths, wave, b->total_slots, cs, nullptr, false, true);
+        st = run_waves(r, W, b->total_paths, wave, b->total_slots, cs, nullptr, false, true, lanes);
         cudaGraph_t g = nullptr;
         e = cudaStreamEndCapture(cs, &g);   // always ends the capture, also after a failed launch
         r->launches = launches;
@@ -980,6 +1123,7 @@ dr_status dr_batch_render(dr_renderer *r, dr_batch *b, int32_t use_graph, void *
         b->graph = g;
         b->graph_scratch = r->scratch_id;
         b->graph_wave = wave;
+        b->graph_lanes = lanes;
         size_t nodes = 0;
         cudaGraphGetNodes(g, nullptr, &nodes);
         b->graph_launches = 0;

@@ -16,6 +16,7 @@
 // atomic per warp.  Queue counts live in a device control block, so a whole wave is a fixed launch
 // sequence with no host synchronisation (and can be captured in a CUDA graph).  Every path record
 // carries the index of its render job, so the paths of many scenes can share a wave (batches).
+#include <algorithm>
 #include "dr_kernels.h"
 #include "dr_shading.cuh"
 #include "dr_trace.cuh"
@@ -936,6 +937,7 @@ size_t ctrl_bytes() { return sizeof(Ctrl); }
 Profiler::~Profiler() {
     reset();
     for (cudaEvent_t e : pool_) cudaEventDestroy(e);
+    if (base_) cudaEventDestroy(base_);
 }
 cudaEvent_t Profiler::take() {
     if (!pool_.empty()) {
@@ -964,21 +966,56 @@ cudaError_t Profiler::harvest() {
     cudaError_t err = cudaSuccess;
     for (auto &p : pending_) {
         cudaError_t e = cudaEventSynchronize(p.second.second);
-        float t = 0.0f;
+        float t = 0.0f, t0 = 0.0f, t1 = 0.0f;
         if (e == cudaSuccess) e = cudaEventElapsedTime(&t, p.second.first, p.second.second);
+        if (e == cudaSuccess && base_) {
+            e = cudaEventElapsedTime(&t0, base_, p.second.first);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t1, base_, p.second.second);
+        }
         if (e != cudaSuccess) err = e;
-        else ms[p.first] += t;
+        else {
+            ms[p.first] += t;
+            if (base_) intervals_[p.first].push_back({t0, t1});
+        }
         pool_.push_back(p.second.first);
         pool_.push_back(p.second.second);
     }
     pending_.clear();
     return err;
 }
-void Profiler::reset() {
+void Profiler::reset(bool base) {
     harvest();
     for (int k = 0; k < KC_COUNT; k++) {
         ms[k] = 0.0;
         launches[k] = 0;
+        intervals_[k].clear();
+    }
+    if (base) {
+        // every launch recorded from now on completes after the base event
+        if (!base_) cudaEventCreate(&base_);
+        cudaDeviceSynchronize();
+        cudaEventRecord(base_, 0);
+        cudaEventSynchronize(base_);
+    }
+}
+void Profiler::busy(double *out) const {
+    for (int k = 0; k < KC_COUNT; k++) {
+        std::vector<std::pair<float, float>> iv = intervals_[k];
+        std::sort(iv.begin(), iv.end());
+        double total = 0.0, lo = 0.0, hi = 0.0;
+        bool open = false;
+        for (const auto &x : iv) {
+            if (!open || x.first > hi) {
+                if (open) total += hi - lo;
+                lo = x.first;
+                hi = x.second;
+                open = true;
+            } else if (x.second > hi) {
+                hi = x.second;
+            }
+        }
+        if (open) total += hi - lo;
+        out[k] = total;
     }
 }
 

@@ -55,16 +55,23 @@ struct WaveDesc {
 // Kernel classes for per-class timing.
 enum KernelClass { KC_CAMERA = 0, KC_TRACE = 1, KC_SHADE = 2, KC_SHADOW = 3, KC_RESOLVE = 4, KC_COUNT = 5 };
 
-// CUDA-event timing of kernel launches on their own stream, accumulated per kernel class.
+// CUDA-event timing of kernel launches on their own stream, accumulated per kernel class: the sum
+// of launch durations (ms) and, for launches that overlap on several streams, the busy time (the
+// length of the union of a class's launch intervals, measured from a base event that precedes all
+// of them).
 class Profiler {
   public:
     bool enabled = false;
     ~Profiler();
     void begin(int cls, cudaStream_t s);
     void end(int cls, cudaStream_t s);
-    // Waits for the recorded events, adds their elapsed times to ms[] and recycles them.
+    // Waits for the recorded events, adds their elapsed times to ms[], keeps their intervals and
+    // recycles them.
     cudaError_t harvest();
-    void reset();
+    // Clears the totals; with `base`, waits for the device and records the base event.
+    void reset(bool base = false);
+    // Union length of each class's harvested launch intervals.
+    void busy(double *out) const;
     double ms[KC_COUNT] = {0, 0, 0, 0, 0};
     long long launches[KC_COUNT] = {0, 0, 0, 0, 0};
 
@@ -72,7 +79,9 @@ class Profiler {
     cudaEvent_t take();
     std::vector<cudaEvent_t> pool_;
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending_;
+    std::vector<std::pair<float, float>> intervals_[KC_COUNT];
     cudaEvent_t open_[KC_COUNT] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t base_ = nullptr;
 };
 
 size_t ctrl_bytes();

@@ -275,6 +275,18 @@ dr_status dr_cast_counted(const dr_scene *scene, const float *origin, const floa
 dr_status dr_renderer_create(int32_t wave_paths, dr_renderer **out);
 void dr_renderer_destroy(dr_renderer *r);
 
+/* Concurrent wave pipelines ("lanes") of one dr_render_blocks call, 1..DR_MAX_LANES (default
+ * DR_DEFAULT_LANES): the waves of a render alternate over `lanes` scratch sets, each on its own
+ * stream forked from and joined back into the caller's stream, adding into one accumulator, so one
+ * pipeline's kernels fill the tails of another's (the reference runs several GPU worker threads
+ * per device for the same reason, Renderer::ThreadConfiguration).  Each extra lane allocates a
+ * scratch set like the renderer's own on first use.  Results do not depend on the lane count
+ * beyond float accumulation order.  Batches and the adjoint use one lane. */
+#define DR_DEFAULT_LANES 4
+#define DR_MAX_LANES 8
+dr_status dr_renderer_set_lanes(dr_renderer *r, int32_t lanes);
+int32_t dr_renderer_lanes(const dr_renderer *r);
+
 /* Replaces DumbRenderer::renderBlocksGPU (DumbRenderer.cu:87-113): renders blocks
  * [start_block, end_block) of a width x height image into the caller's device frame buffer
  * (BlockBasedFrameBuffer<8,16> layout, float4), setting (iteration <= 1) or blending (1/iteration)
@@ -355,6 +367,11 @@ dr_status dr_renderer_set_profiling(dr_renderer *r, int32_t enable);
 /* Waits for the recorded events and returns, per kernel class, the summed launch durations in
  * milliseconds and the number of timed launches (arrays of DR_KERNEL_CLASSES; either may be NULL). */
 dr_status dr_renderer_kernel_times(dr_renderer *r, double *ms, int64_t *launches);
+
+/* Per kernel class, the busy time in milliseconds since profiling was enabled: the length of the
+ * union of the class's launch intervals over all lanes (equal to the summed durations with one
+ * lane; less when launches of several lanes overlap).  busy_ms[DR_KERNEL_CLASSES]. */
+dr_status dr_renderer_kernel_busy(dr_renderer *r, double *busy_ms);
 
 /* Counting pass: while enabled, trace and shadow kernels also count, per cast, the reference's
  * child-box slab tests and triangle tests (see dr_cast_counted).  Slower; never on a timed path. */
