@@ -178,6 +178,8 @@ def lib() -> ctypes.CDLL:
     L.dr_mesh_file_object_data.argtypes = [vp, i32, vp, vp, vp]
     L.dr_mesh_file_destroy.restype = None
     L.dr_mesh_file_destroy.argtypes = [vp]
+    L.dr_png_read.restype = i32
+    L.dr_png_read.argtypes = [ctypes.c_char_p, P(i32), P(i32), vp]
     L.dr_scene_file_load.restype = i32
     L.dr_scene_file_load.argtypes = [ctypes.c_char_p, P(vp)]
     L.dr_scene_file_counts.restype = i32

@@ -399,6 +399,12 @@ dr_status dr_image_write_png(const float *rgba, int32_t width, int32_t height, c
 /* Portable float map (RGB, little-endian, rows bottom-up): the unclamped radiance. */
 dr_status dr_image_write_pfm(const float *rgba, int32_t width, int32_t height, const char *path);
 
+/* PNG decoding for textures (Images::getTexturePNG, Images.cu:38-56, which takes lodepng's 8-bit RGBA
+ * output): every colour type and bit depth, tRNS, Adam7.  Writes width / height and, when rgba8 is
+ * not NULL, uint8[height][width][4] (row 0 = the file's first row); call with rgba8 = NULL first for
+ * the size.  Texture texels are these bytes / 255. */
+dr_status dr_png_read(const char *path, int32_t *width, int32_t *height, uint8_t *rgba8);
+
 /* ---- OBJ meshes (host) -----------------------------------------------------------------------
  * Replace MeshReader::readObj + PolyMesh::bake (__source__/Namespaces/MeshReader/MeshReader.impl.h:
  * 160-367, __source__/DataStructures/Objects/Meshes/PolyMesh/PolyMesh.impl.h:140-152) with the same

@@ -25,6 +25,8 @@
 #include "DataStructures/Objects/Components/Shaders/FresnelShader/FresnelShader.cuh"
 #include "DataStructures/Objects/Components/Shaders/DefaultShader/DefaultShader.cuh"
 #include "Namespaces/Images/Images.cuh"
+#include "Namespaces/Images/lodepng.h"
+#include <cstring>
 #include "Namespaces/MeshReader/MeshReader.h"
 #include <thread>
 #include <vector>
@@ -226,6 +228,18 @@ void dref_obj_free(void *h) { delete (RefObj *)h; }
 
 // Writes a row-major float4 image through the reference's own Images::saveBufferPNG (lodepng), via
 // a host BlockBuffer filled with FrameBuffer::setColor.  Returns the Images::Error code (0 = ok).
+// lodepng::decode to 8-bit RGBA (what Images::getTexturePNG decodes textures with): returns the
+// lodepng error code (0 = success), writes width / height and, when rgba8 is not NULL, the pixels.
+int dref_png_decode(const char *path, int *width, int *height, unsigned char *rgba8) {
+	std::vector<unsigned char> px;
+	unsigned int w = 0, h = 0;
+	unsigned int err = lodepng::decode(px, w, h, std::string(path));
+	*width = (int)w;
+	*height = (int)h;
+	if (!err && rgba8 != NULL) std::memcpy(rgba8, px.data(), px.size());
+	return (int)err;
+}
+
 int dref_save_png(const float *rgba, int width, int height, const char *path) {
 	FrameBufferManager fb;
 	fb.cpuHandle()->use<BlockBuffer>();
