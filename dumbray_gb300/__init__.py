@@ -46,7 +46,32 @@ class DrBuildParams(ctypes.Structure):
 class DrMaterial(ctypes.Structure):
     _fields_ = [("type", ctypes.c_int32), ("color", _F3), ("fresnel", _F3), ("specular", ctypes.c_float),
                 ("metal", ctypes.c_float), ("diffuse", ctypes.c_float), ("smoothness", ctypes.c_float),
-                ("shininess", ctypes.c_float), ("roughness", ctypes.c_float), ("emission", _F3)]
+                ("shininess", ctypes.c_float), ("roughness", ctypes.c_float), ("emission", _F3),
+                ("texture", ctypes.c_int32 * 4), ("tiling", (ctypes.c_float * 2) * 4), ("offset", (ctypes.c_float * 2) * 4),
+                ("normal_color", _F3), ("alpha_threshold", ctypes.c_float)]
+
+
+class DrTexture(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("filtering", ctypes.c_int32),
+                ("rgba", ctypes.c_void_p)]
+
+
+TEX_COLOR, TEX_FRESNEL, TEX_NORMAL, TEX_ALPHA = range(4)
+FILTER_NONE, FILTER_BILINEAR = 0, 1
+
+
+def textured(m: "DrMaterial", channel: int, texture: int, tiling=(1.0, 1.0), offset=(0.0, 0.0)) -> "DrMaterial":
+    """Gives material ``m`` texture ``texture`` (0-based index into the textures passed to
+    Scene.set_textures) on ``channel`` (TEX_COLOR / TEX_FRESNEL / TEX_NORMAL / TEX_ALPHA); sets the
+    reference's defaults for the normal-map colour (1, 1, 1) and the alpha threshold (0.5) if unset."""
+    m.texture[channel] = texture + 1
+    m.tiling[channel][:] = tiling
+    m.offset[channel][:] = offset
+    if channel == TEX_NORMAL and not any(m.normal_color):
+        m.normal_color[:] = (1.0, 1.0, 1.0)
+    if channel == TEX_ALPHA and m.alpha_threshold == 0.0:
+        m.alpha_threshold = 0.5
+    return m
 
 
 class DrLight(ctypes.Structure):
@@ -180,6 +205,8 @@ def lib() -> ctypes.CDLL:
     L.dr_mesh_file_destroy.argtypes = [vp]
     L.dr_png_read.restype = i32
     L.dr_png_read.argtypes = [ctypes.c_char_p, P(i32), P(i32), vp]
+    L.dr_scene_set_textures.restype = i32
+    L.dr_scene_set_textures.argtypes = [vp, vp, i32, vp]
     L.dr_scene_file_load.restype = i32
     L.dr_scene_file_load.argtypes = [ctypes.c_char_p, P(vp)]
     L.dr_scene_file_counts.restype = i32
@@ -194,6 +221,12 @@ def lib() -> ctypes.CDLL:
     L.dr_scene_file_camera.argtypes = [vp, vp]
     L.dr_scene_file_render_params.restype = i32
     L.dr_scene_file_render_params.argtypes = [vp, vp]
+    L.dr_scene_file_textures.restype = i32
+    L.dr_scene_file_textures.argtypes = [vp]
+    L.dr_scene_file_texture.restype = i32
+    L.dr_scene_file_texture.argtypes = [vp, i32, P(i32), P(i32), P(i32), vp]
+    L.dr_scene_file_texcoords.restype = i32
+    L.dr_scene_file_texcoords.argtypes = [vp, vp]
     L.dr_scene_file_create_scene.restype = i32
     L.dr_scene_file_create_scene.argtypes = [vp, vp, P(vp)]
     L.dr_scene_file_destroy.restype = None
@@ -460,6 +493,18 @@ class Scene:
     def set_triangle_params(self, albedo=None, emission=None, roughness=None):
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float32) for a in (albedo, emission, roughness)]
         check(lib().dr_scene_set_triangle_params(self.handle, *[None if a is None else a.ctypes.data for a in arrs]))
+
+    def set_textures(self, textures, uv=None):
+        """dr_scene_set_textures: ``textures`` = [(rgba float [h, w, 4], filtering)], ``uv`` = float
+        [n, 3, 2] corner texture coordinates (None: zeros)."""
+        imgs = [np.ascontiguousarray(t, dtype=np.float32) for t, _ in textures]
+        arr = (DrTexture * max(1, len(imgs)))()
+        for i, (img, (_, filt)) in enumerate(zip(imgs, textures)):
+            arr[i].width, arr[i].height, arr[i].filtering = img.shape[1], img.shape[0], int(filt)
+            arr[i].rgba = img.ctypes.data
+        u = None if uv is None else np.ascontiguousarray(uv, dtype=np.float32).reshape(-1, 3, 2)
+        check(lib().dr_scene_set_textures(self.handle, ctypes.addressof(arr) if imgs else None, len(imgs),
+                                          None if u is None else u.ctypes.data))
 
     def close(self):
         if self._h is not None:
@@ -893,8 +938,9 @@ class Progressive:
 
 class SceneFile:
     """A DumbRay scene file (.dumb) read by dr_scene_file_load, like DumbRenderContext::fromFile:
-    triangles in push order (``tris``, per-corner ``normals``, ``mat_id``), ``materials``, ``lights``,
-    the file's ``camera`` and reference-mode ``params`` (width / height left 0)."""
+    triangles in push order (``tris``, per-corner ``normals``, ``uv``, ``mat_id``), ``materials``,
+    ``lights``, ``textures`` [(rgba, filtering)], the file's ``camera`` and reference-mode ``params``
+    (width / height left 0)."""
 
     def __init__(self, path):
         L = lib()
@@ -920,6 +966,16 @@ class SceneFile:
             check(L.dr_scene_file_camera(h, ctypes.byref(self.camera)))
             self.params = DrRenderParams()
             check(L.dr_scene_file_render_params(h, ctypes.byref(self.params)))
+            self.uv = np.zeros((n, 3, 2), np.float32)
+            if n:
+                check(L.dr_scene_file_texcoords(h, self.uv.ctypes.data))
+            self.textures = []
+            for i in range(L.dr_scene_file_textures(h)):
+                w, hh, f = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+                check(L.dr_scene_file_texture(h, i, ctypes.byref(w), ctypes.byref(hh), ctypes.byref(f), None))
+                img = np.zeros((hh.value, w.value, 4), np.float32)
+                check(L.dr_scene_file_texture(h, i, None, None, None, img.ctypes.data))
+                self.textures.append((img, f.value))
         finally:
             L.dr_scene_file_destroy(h)
 
@@ -931,12 +987,25 @@ class SceneFile:
     def scene(self, **build) -> "Scene":
         """The octree scene over the file's geometry (DumbRenderContext::buildFromFile); ``build``
         takes Scene's build keywords."""
-        return Scene(self.tris, normals=self.normals, mat_id=self.mat_id, materials=self.materials,
-                     lights=self.lights, **build)
+        sc = Scene(self.tris, normals=self.normals, mat_id=self.mat_id, materials=self.materials,
+                   lights=self.lights, **build)
+        if self.textures:
+            sc.set_textures(self.textures, self.uv)
+        return sc
 
 
 def load_scene_file(path) -> SceneFile:
     return SceneFile(path)
+
+
+def read_png(path) -> np.ndarray:
+    """dr_png_read: float RGBA [h, w, 4] = the file's 8-bit channels / 255 (Images::getTexturePNG)."""
+    L = lib()
+    w, h = ctypes.c_int32(), ctypes.c_int32()
+    check(L.dr_png_read(str(path).encode(), ctypes.byref(w), ctypes.byref(h), None))
+    px = np.zeros((h.value, w.value, 4), np.uint8)
+    check(L.dr_png_read(str(path).encode(), ctypes.byref(w), ctypes.byref(h), px.ctypes.data))
+    return px.astype(np.float32) / np.float32(255.0)
 
 
 def read_obj(path):

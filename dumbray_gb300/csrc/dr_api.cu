@@ -74,9 +74,17 @@ struct dr_scene {
     float *emission_dev = nullptr;
     float *light_pdf_dev = nullptr;
     int64_t node_f4 = 0, leaf_f4 = 0;    // float4 counts of the device node and leaf-triangle arrays
+    int32_t max_texture = 0;             // largest 1-based texture index the materials use
+    int32_t n_textures = 0;
+    float4 *texels_dev = nullptr;
+    int4 *tex_info_dev = nullptr;
+    float2 *uv_dev = nullptr;
 
     ~dr_scene() {
         for (void *p : allocs) cudaFree(p);
+        cudaFree(texels_dev);
+        cudaFree(tex_info_dev);
+        cudaFree(uv_dev);
         cudaFree(shade);
         cudaFree(emissive);
         cudaFree(emissive_cdf);
@@ -287,8 +295,11 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
     for (int32_t i = 0; mat_id && i < n; i++)
         if (mat_id[i] < 0 || (n_mats > 0 && mat_id[i] >= n_mats) || (n_mats == 0 && mat_id[i] != 0))
             return fail(DR_E_ARG, "dr_scene_create: material id out of range at triangle " + std::to_string(i));
-    for (int32_t i = 0; i < n_mats; i++)
+    for (int32_t i = 0; i < n_mats; i++) {
         if (mats[i].type < 0 || mats[i].type > DR_MAT_DEFAULT) return fail(DR_E_ARG, "dr_scene_create: bad material type");
+        for (int k = 0; k < 4; k++)
+            if (mats[i].texture[k] < 0) return fail(DR_E_ARG, "dr_scene_create: negative texture index");
+    }
     for (int32_t i = 0; i < n_lights; i++)
         if (lights[i].type < 0 || lights[i].type > DR_LIGHT_SPOTLIGHT) return fail(DR_E_ARG, "dr_scene_create: bad light type");
 
@@ -366,6 +377,16 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
         d.smoothness = m.smoothness;
         d.shininess = m.shininess;
         d.roughness = m.roughness;
+        for (int k = 0; k < 4; k++) {
+            d.texture[k] = m.texture[k] - 1;
+            d.tiling[k][0] = m.tiling[k][0];
+            d.tiling[k][1] = m.tiling[k][1];
+            d.offset[k][0] = m.offset[k][0];
+            d.offset[k][1] = m.offset[k][1];
+            sc->max_texture = std::max(sc->max_texture, m.texture[k]);
+        }
+        for (int k = 0; k < 3; k++) d.normal_color[k] = m.normal_color[k];
+        d.alpha_threshold = m.alpha_threshold;
     }
     if (n_mats == 0) dm[0].type = DR_MAT_LAMBERT;
     std::vector<drd::Light> dl(std::max(n_lights, 1));
@@ -452,6 +473,52 @@ dr_status dr_scene_set_triangle_params(dr_scene *sc, const float *albedo, const 
     if (emission) std::copy(emission, emission + 3 * n, sc->emission.begin());
     if (roughness) std::copy(roughness, roughness + n, sc->roughness.begin());
     return upload_shading(sc);
+}
+
+dr_status dr_scene_set_textures(dr_scene *sc, const dr_texture *tex, int32_t n, const float *uv) {
+    if (!sc || n < 0 || (n > 0 && !tex)) return fail(DR_E_ARG, "dr_scene_set_textures: bad arguments");
+    if (sc->max_texture > n) return fail(DR_E_ARG, "dr_scene_set_textures: a material uses texture " +
+                                                       std::to_string(sc->max_texture) + " of " + std::to_string(n));
+    std::vector<float4> texels;
+    std::vector<int4> info;
+    for (int32_t t = 0; t < n; t++) {
+        const dr_texture &x = tex[t];
+        if (x.width <= 0 || x.height <= 0 || !x.rgba || (x.filtering != DR_FILTER_NONE && x.filtering != DR_FILTER_BILINEAR))
+            return fail(DR_E_ARG, "dr_scene_set_textures: bad texture " + std::to_string(t));
+        const size_t texel_count = (size_t)x.width * (size_t)x.height;
+        if (texels.size() + texel_count > (size_t)INT32_MAX) return fail(DR_E_ARG, "dr_scene_set_textures: too many texels");
+        info.push_back(make_int4((int)texels.size(), x.width, x.height, x.filtering));
+        for (size_t k = 0; k < texel_count; k++)
+            texels.push_back(make_float4(x.rgba[4 * k], x.rgba[4 * k + 1], x.rgba[4 * k + 2], x.rgba[4 * k + 3]));
+    }
+    std::vector<float2> uv2((size_t)3 * (size_t)std::max<int64_t>(sc->n, 1), make_float2(0.0f, 0.0f));
+    if (uv)
+        for (int64_t i = 0; i < 3 * sc->n; i++) uv2[(size_t)i] = make_float2(uv[2 * i], uv[2 * i + 1]);
+    float4 *d_texels = nullptr;
+    int4 *d_info = nullptr;
+    float2 *d_uv = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!texels.empty()) e = upload(&d_texels, texels.data(), texels.size());
+    if (e == cudaSuccess && !info.empty()) e = upload(&d_info, info.data(), info.size());
+    if (e == cudaSuccess) e = upload(&d_uv, uv2.data(), uv2.size());
+    if (e != cudaSuccess) {
+        cudaFree(d_texels);
+        cudaFree(d_info);
+        cudaFree(d_uv);
+        return cuda_fail(e, "dr_scene_set_textures");
+    }
+    // replaced buffers stay allocated until the scene is destroyed: batches created earlier hold
+    // copies of the scene's device view
+    for (void *old : {(void *)sc->texels_dev, (void *)sc->tex_info_dev, (void *)sc->uv_dev})
+        if (old) sc->allocs.push_back(old);
+    sc->texels_dev = d_texels;
+    sc->tex_info_dev = d_info;
+    sc->uv_dev = d_uv;
+    sc->n_textures = n;
+    sc->dev.texels = d_texels;
+    sc->dev.tex_info = d_info;
+    sc->dev.uv = d_uv;
+    return DR_OK;
 }
 
 dr_status dr_scene_triangle_params_device(dr_scene *sc, float **albedo, float **emission) {
@@ -657,6 +724,8 @@ dr_status dr_renderer_counters(dr_renderer *r, int64_t *counts) {
 static dr_status make_item(const dr_scene *sc, const dr_camera *cam, float *fb, int32_t start_block, int32_t end_block,
                            const dr_render_params *p, const char *who, drk::Item &I) {
     if (!sc || !cam || !fb || !p) return fail(DR_E_ARG, std::string(who) + ": NULL argument");
+    if (sc->max_texture > sc->n_textures)
+        return fail(DR_E_ARG, std::string(who) + ": the scene's materials use textures it does not have (dr_scene_set_textures)");
     if (p->mode != DR_MODE_REFERENCE && p->mode != DR_MODE_PHYSICAL) return fail(DR_E_ARG, std::string(who) + ": bad mode");
     if (p->width <= 0 || p->height <= 0) return fail(DR_E_ARG, std::string(who) + ": bad resolution");
     const int nblocks = dr_block_count(p->width, p->height);
@@ -1150,5 +1219,7 @@ void dr_batch_destroy(dr_batch *b) { delete b; }
 }  // extern "C"
 
 const drd::Scene *dr_internal_scene_device(const dr_scene *scene) { return scene ? &scene->dev : nullptr; }
+
+bool dr_internal_scene_textures_ok(const dr_scene *scene) { return scene && scene->max_texture <= scene->n_textures; }
 
 void dr_internal_set_error(const char *msg) { g_err = msg ? msg : ""; }

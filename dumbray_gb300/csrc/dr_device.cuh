@@ -28,6 +28,10 @@ struct Material {
     float fresnel[3];
     float specular, metal, diffuse, smoothness, shininess, roughness;
     float emission[3];
+    int texture[4];              // 0-based texture per channel (colour, fresnel, normal, alpha), -1 = none
+    float tiling[4][2], offset[4][2];
+    float normal_color[3];
+    float alpha_threshold;
 };
 
 struct Light {
@@ -59,6 +63,9 @@ struct Scene {
     const float *light_pdf;     // physical: [n] area pdf of picking a point of this triangle by NEE
     const int *emissive;        // emissive triangle ids
     const float *emissive_cdf;  // inclusive prefix sums of power (at table build time)
+    const float4 *texels;       // all textures' RGBA texels, row-major per texture
+    const int4 *tex_info;       // per texture: {first texel, width, height, filtering}
+    const float2 *uv;           // [n][3] corner texture coordinates (null: none set)
     float root_lo[3], root_hi[3];
     int root_child;             // node group of the root's 8 children (0 for a standalone scene, the
                                 // scene's offset in a batch arena), -1 = the root is a leaf

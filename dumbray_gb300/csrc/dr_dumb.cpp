@@ -23,8 +23,10 @@
 //    BakedTriFace >> Transform (Meshes/BakedTriMesh/BakedTriMesh.impl.h:16-18);
 //  * the camera (parseCamera, :491-530; SimpleStochasticLense / SphericalSegmentLense ::fromDson)
 //    and renderer settings (parseRenderer, :531-633).
-// Textures (no counterpart in this renderer) and mesh primitives (unimplemented in the reference)
-// fail with a message.
+//  * textures (getImageId, DumbRenderContext.cu:374-450; ColoredTexture::fromDson, DumbStructs.cu:7-37):
+//    PNG files decoded by dr_png_read, named or by path, nearest or bilinear filtering; texture
+//    coordinates from the OBJ files.
+// Mesh primitives (left unimplemented by the reference) fail with a message.
 #include <cerrno>
 #include <climits>
 #include <cmath>
@@ -343,6 +345,11 @@ Xf transform_from(const JValue &v) {
 struct Face {
     float v[9];
     float n[9];
+    float uv[6];  // corner texture coordinates (BakedTriFace::tex x / y)
+};
+struct Tex {
+    int w = 0, h = 0, filter = DR_FILTER_BILINEAR;
+    std::vector<float> rgba;
 };
 struct Unit {
     Face f;
@@ -405,6 +412,7 @@ class Loader {
     std::vector<dr_material> materials;
     std::vector<dr_light> lights;
     std::vector<Unit> units;
+    std::vector<Tex> textures;
     int lens = -1;  // -1: none set yet
     float lens_angle[2] = {60.0f, 60.0f}, lens_focal = 128.0f, lens_soft = 1.0f, lens_filter[3] = {1, 1, 1};
     Xf camera;
@@ -431,6 +439,7 @@ class Loader {
   private:
     std::string source_;  // directory of the file being read (with its trailing separator)
     std::unordered_map<std::string, int> material_names_;
+    std::unordered_map<std::string, int> texture_names_;  // "name::" / "png::" keys, as the reference keeps them
     std::map<std::string, ObjFile> obj_files_;
     std::map<std::string, Group> groups_;
 
@@ -480,17 +489,68 @@ class Loader {
         return id;
     }
 
-    // A coloured-texture entry: colour, texture (none unless a string or dictionary), tiling, offset.
-    static void colored(const JValue &v, const char *color_key, const char *texture_key, const char *tiling_key,
-                        const char *offset_key, V &color) {
-        if (const JValue *c = v.get(color_key)) color = vector_from(*c, color_key);
-        if (const JValue *t = v.get(texture_key)) {
-            if (t->kind == JValue::STR || t->kind == JValue::DICT)
-                raise(std::string("textures are not supported by this renderer (\"") + texture_key + "\")");
-            if (t->kind == JValue::ARR) raise(std::string("unsupported value for \"") + texture_key + "\"");
+    // DumbRenderContext::getImageId (DumbRenderContext.cu:374-450): -1 for null / bool / number; a
+    // string names a texture ("name::" then "png::" keys); a dictionary loads its "png" file (path
+    // relative to the scene file first), with "filtering" and "name".  Returns the 0-based id.
+    int image_id(const JValue &v) {
+        if (v.kind == JValue::BOOL || v.kind == JValue::NUL || v.kind == JValue::NUM) return -1;
+        if (v.kind == JValue::STR) {
+            auto it = texture_names_.find("name::" + v.str);
+            if (it == texture_names_.end()) it = texture_names_.find("png::" + v.str);
+            if (it == texture_names_.end()) raise("texture \"" + v.str + "\" not found");
+            return it->second;
         }
-        if (const JValue *t = v.get(tiling_key)) vector_from(*t, tiling_key);
-        if (const JValue *t = v.get(offset_key)) vector_from(*t, offset_key);
+        if (v.kind != JValue::DICT) raise("unsupported value for a texture");
+        const JValue *png = v.get("png");
+        if (!png) raise("image dict incomplete");
+        const std::string &file = as_string(*png, "image 'png' entry");
+        const std::string path = resolve(file);
+        int32_t w = 0, h = 0;
+        if (dr_png_read(path.c_str(), &w, &h, nullptr) != DR_OK) raise("could not read file: \"" + path + "\"");
+        std::vector<uint8_t> px((size_t)w * h * 4);
+        if (dr_png_read(path.c_str(), &w, &h, px.data()) != DR_OK) raise("could not read file: \"" + path + "\"");
+        Tex t;
+        t.w = w;
+        t.h = h;
+        t.rgba.resize(px.size());
+        for (size_t k = 0; k < px.size(); k++) t.rgba[k] = (((float)px[k]) / 255.0f);
+        const int id = (int)textures.size();
+        textures.push_back(std::move(t));
+        texture_names_["png::" + path] = id;
+        texture_names_["png::" + file] = id;
+        if (const JValue *f = v.get("filtering")) {
+            const std::string &filter = as_string(*f, "image 'filtering' entry");
+            if (filter == "none") textures[(size_t)id].filter = DR_FILTER_NONE;
+            else if (filter == "bilinear") textures[(size_t)id].filter = DR_FILTER_BILINEAR;
+            else raise("image filter can be only \"none\"/[\"bilinear\"] (got: \"" + filter + "\")");
+        }
+        if (const JValue *n = v.get("name")) texture_names_["name::" + as_string(*n, "image name entry")] = id;
+        return id;
+    }
+
+    // ColoredTexture::fromDson (DumbStructs.cu:7-37): colour, texture, tiling, offset entries of one
+    // channel of `m` (texture ids stored 1-based, tiling and offset as the first two numbers).
+    void colored(const JValue &v, const char *color_key, const char *texture_key, const char *tiling_key,
+                 const char *offset_key, V &color, dr_material &m, int ch) {
+        if (const JValue *c = v.get(color_key)) color = vector_from(*c, color_key);
+        if (const JValue *t = v.get(texture_key)) m.texture[ch] = image_id(*t) + 1;
+        if (const JValue *t = v.get(tiling_key)) {
+            V x = vector_from(*t, tiling_key);
+            m.tiling[ch][0] = x.x, m.tiling[ch][1] = x.y;
+        }
+        if (const JValue *t = v.get(offset_key)) {
+            V x = vector_from(*t, offset_key);
+            m.offset[ch][0] = x.x, m.offset[ch][1] = x.y;
+        }
+    }
+    static void untextured(dr_material &m) {
+        for (int k = 0; k < 4; k++) {
+            m.texture[k] = 0;
+            m.tiling[k][0] = m.tiling[k][1] = 1.0f;
+            m.offset[k][0] = m.offset[k][1] = 0.0f;
+        }
+        m.normal_color[0] = m.normal_color[1] = m.normal_color[2] = 1.0f;
+        m.alpha_threshold = 0.5f;
     }
 
     // DumbBasedShader constructor state: fresnel, spec, diffuse (scaled by 1 - metal), metal.
@@ -503,7 +563,7 @@ class Loader {
         return DumbState{fresnel, vmulf(diffuse, 1.0f - metal), spec, metal};
     }
 
-    static void dumb_based(const JValue &v, dr_material &m) {
+    void dumb_based(const JValue &v, dr_material &m) {
         DumbState s = dumb_ctor(V{0.2f, 0.2f, 0.2f}, 8.0f, V{0.2f, 0.2f, 0.2f}, 0.5f);
         if (const JValue *p = v.get("preset")) {
             const std::string &preset = as_string(*p, "dumb_based preset");
@@ -520,14 +580,17 @@ class Loader {
         float metal = s.metal, specular = s.spec;
         float inv = 1.0f / ((metal == 1.0f) ? 1.0f : (1.0f - metal));
         V diffuse = vmulf(s.diffuse, inv);
-        V unused{0, 0, 0};
-        colored(v, "fresnel", "fresnel_texture", "fresnel_tiling", "fresnel_offset", fresnel);
-        colored(v, "diffuse", "diffuse_texture", "diffuse_tiling", "diffuse_offset", diffuse);
-        colored(v, "normal_color", "normal_texture", "normal_tiling", "normal_offset", unused);
-        colored(v, "alpha_cutout_color", "alpha_cutout_texture", "alpha_cutout_tiling", "alpha_cutout_offset", unused);
-        if (const JValue *p = v.get("alpha_cutout_threshold")) as_float(*p, "dumb_based alpha_cutout_threshold");
+        V normal{1.0f, 1.0f, 1.0f}, cutout{1.0f, 1.0f, 1.0f};
+        untextured(m);
+        colored(v, "fresnel", "fresnel_texture", "fresnel_tiling", "fresnel_offset", fresnel, m, DR_TEX_FRESNEL);
+        colored(v, "diffuse", "diffuse_texture", "diffuse_tiling", "diffuse_offset", diffuse, m, DR_TEX_COLOR);
+        colored(v, "normal_color", "normal_texture", "normal_tiling", "normal_offset", normal, m, DR_TEX_NORMAL);
+        colored(v, "alpha_cutout_color", "alpha_cutout_texture", "alpha_cutout_tiling", "alpha_cutout_offset", cutout, m,
+                DR_TEX_ALPHA);
+        if (const JValue *p = v.get("alpha_cutout_threshold")) m.alpha_threshold = as_float(*p, "dumb_based alpha_cutout_threshold");
         if (const JValue *p = v.get("specular")) specular = as_float(*p, "dumb_based specular");
         if (const JValue *p = v.get("metal")) metal = as_float(*p, "dumb_based metal");
+        m.normal_color[0] = normal.x, m.normal_color[1] = normal.y, m.normal_color[2] = normal.z;
         m.type = DR_MAT_DUMB_BASED;
         m.fresnel[0] = fresnel.x, m.fresnel[1] = fresnel.y, m.fresnel[2] = fresnel.z;
         m.color[0] = diffuse.x, m.color[1] = diffuse.y, m.color[2] = diffuse.z;
@@ -535,7 +598,8 @@ class Loader {
         m.metal = metal;
     }
 
-    static void simple_stochastic(const JValue &v, dr_material &m) {
+    void simple_stochastic(const JValue &v, dr_material &m) {
+        untextured(m);
         // constructor state of SimpleStochasticShader() = ((1,1,1), 0.05, 0.95, 2)
         float total = 0.05f + 0.95f;
         float mul = ((total > 1.0f) ? (1.0f / total) : 1.0f);
@@ -554,7 +618,8 @@ class Loader {
 
     // Shaders::FresnelShader::fromDson (FresnelShader.impl.cuh:20-24): white, then an "engine_color"
     // preset (DumbStructs.cuh:143-169; the reference ignores a bad one), then the colour entries.
-    static void fresnel_color(const JValue &v, dr_material &m) {
+    void fresnel_color(const JValue &v, dr_material &m) {
+        untextured(m);
         V color{1.0f, 1.0f, 1.0f};
         if (const JValue *e = v.get("engine_color")) {
             if (e->kind == JValue::STR) {
@@ -566,7 +631,7 @@ class Loader {
                 else if (n == "silver") color = V{0.95f, 0.93f, 0.88f};
             }
         }
-        colored(v, "color", "texture", "tiling", "offset", color);
+        colored(v, "color", "texture", "tiling", "offset", color, m, DR_TEX_COLOR);
         m.type = DR_MAT_FRESNEL;
         m.color[0] = color.x, m.color[1] = color.y, m.color[2] = color.z;
     }
@@ -673,12 +738,16 @@ class Loader {
         for (int32_t i = 0; i < dr_mesh_file_objects(mf); i++) {
             std::string oname = dr_mesh_file_object_name(mf, i);
             int32_t n = dr_mesh_file_object_triangles(mf, i);
-            std::vector<float> xyz((size_t)n * 9), nrm((size_t)n * 9);
-            dr_mesh_file_object_data(mf, i, xyz.data(), nrm.data(), nullptr);
+            std::vector<float> xyz((size_t)n * 9), nrm((size_t)n * 9), uvw((size_t)n * 9);
+            dr_mesh_file_object_data(mf, i, xyz.data(), nrm.data(), uvw.data());
             std::vector<Face> faces((size_t)n);
             for (int32_t k = 0; k < n; k++) {
                 std::memcpy(faces[k].v, &xyz[(size_t)k * 9], sizeof(float) * 9);
                 std::memcpy(faces[k].n, &nrm[(size_t)k * 9], sizeof(float) * 9);
+                for (int c = 0; c < 3; c++) {
+                    faces[k].uv[2 * c] = uvw[(size_t)k * 9 + 3 * c];
+                    faces[k].uv[2 * c + 1] = uvw[(size_t)k * 9 + 3 * c + 1];
+                }
             }
             if (of.objects.find(oname) == of.objects.end()) of.order.push_back(oname);
             of.objects[oname] = std::move(faces);
@@ -996,15 +1065,44 @@ dr_status dr_scene_file_render_params(const dr_scene_file *f, dr_render_params *
     return DR_OK;
 }
 
+int32_t dr_scene_file_textures(const dr_scene_file *f) { return f ? (int32_t)f->L.textures.size() : 0; }
+
+dr_status dr_scene_file_texture(const dr_scene_file *f, int32_t i, int32_t *width, int32_t *height, int32_t *filtering,
+                                float *rgba) {
+    if (!f || i < 0 || i >= (int32_t)f->L.textures.size()) return fail(DR_E_ARG, "dr_scene_file_texture: bad texture");
+    const Tex &t = f->L.textures[(size_t)i];
+    if (width) *width = t.w;
+    if (height) *height = t.h;
+    if (filtering) *filtering = t.filter;
+    if (rgba) std::memcpy(rgba, t.rgba.data(), sizeof(float) * t.rgba.size());
+    return DR_OK;
+}
+
+dr_status dr_scene_file_texcoords(const dr_scene_file *f, float *uv) {
+    if (!f || !uv) return fail(DR_E_ARG, "dr_scene_file_texcoords: NULL argument");
+    for (size_t i = 0; i < f->L.units.size(); i++) std::memcpy(uv + 6 * i, f->L.units[i].f.uv, sizeof(float) * 6);
+    return DR_OK;
+}
+
 dr_status dr_scene_file_create_scene(const dr_scene_file *f, const dr_build_params *bp, dr_scene **out) {
     if (!f || !out) return fail(DR_E_ARG, "dr_scene_file_create_scene: NULL argument");
     const Loader &L = f->L;
     const size_t n = L.units.size();
-    std::vector<float> xyz(n * 9), nrm(n * 9);
+    std::vector<float> xyz(n * 9), nrm(n * 9), uv(n * 6);
     std::vector<int32_t> mat(n);
     dr_scene_file_geometry(f, xyz.data(), nrm.data(), mat.data());
-    return dr_scene_create(xyz.data(), nrm.data(), mat.data(), (int32_t)n, L.materials.data(), (int32_t)L.materials.size(),
-                           L.lights.data(), (int32_t)L.lights.size(), bp, out);
+    dr_status st = dr_scene_create(xyz.data(), nrm.data(), mat.data(), (int32_t)n, L.materials.data(),
+                                   (int32_t)L.materials.size(), L.lights.data(), (int32_t)L.lights.size(), bp, out);
+    if (st != DR_OK || L.textures.empty()) return st;
+    std::vector<dr_texture> tex;
+    for (const Tex &t : L.textures) tex.push_back(dr_texture{t.w, t.h, t.filter, t.rgba.data()});
+    if (n) dr_scene_file_texcoords(f, uv.data());
+    st = dr_scene_set_textures(*out, tex.data(), (int32_t)tex.size(), uv.data());
+    if (st != DR_OK) {
+        dr_scene_destroy(*out);
+        *out = nullptr;
+    }
+    return st;
 }
 
 void dr_scene_file_destroy(dr_scene_file *f) { delete f; }

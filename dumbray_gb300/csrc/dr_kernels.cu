@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
                 const Material &m = S.mats[__ldg(S.mat_id + tri)];
                 TriV v = load_tri(S.tris, tri), nt = load_tri(S.nrms, tri);
                 int ctype = 0;
-                if (m.type == 0) child = dumb_based_request(m, v, nt, hp, d, key, (uint32_t)b, cd, ctype);
+                if (m.type == 0) child = dumb_based_request(S, tri, m, v, nt, hp, d, key, (uint32_t)b, cd, ctype);
                 else if (m.type == DR_MAT_FRESNEL) child = false;
                 else if (m.type == DR_MAT_DEFAULT) {
                     cd = default_request(v, nt, hp, d);

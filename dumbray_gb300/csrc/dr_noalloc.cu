@@ -101,6 +101,8 @@ extern "C" dr_status dr_render_blocks_noalloc(const dr_scene *sc, const dr_camer
     if ((p->mode == DR_MODE_REFERENCE) != (cam->lens <= DR_LENS_SPHERICAL_SEGMENT))
         return nfail(DR_E_ARG, "dr_render_blocks_noalloc: lens does not belong to the render mode");
     if (drk::ctrl_bytes() > kCtrl) return nfail(DR_E_CAPACITY, "dr_render_blocks_noalloc: control block too large");
+    if (!dr_internal_scene_textures_ok(sc))
+        return nfail(DR_E_ARG, "dr_render_blocks_noalloc: the scene's materials use textures it does not have");
     if (start_block == end_block) return DR_OK;
     const drd::Scene *S = dr_internal_scene_device(sc);
     cudaStream_t stream = (cudaStream_t)stream_ptr;

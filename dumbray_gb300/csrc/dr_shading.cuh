@@ -78,14 +78,89 @@ __device__ __forceinline__ f3 point_on_sphere(float u0, float u1, float radius) 
     return f3{(sinPhi * cosf(theta)) * radius, (sinPhi * sinf(theta)) * radius, cosPhi * radius};
 }
 
+// ---- textures (Texture.impl.cuh:81-95; ColoredTexture, DumbStructs.cuh:88-131) ------------------
+__device__ __forceinline__ float4 texel(const Scene &S, int4 info, uint32_t x, uint32_t y) {
+    return __ldg(S.texels + info.x + (size_t)y * (uint32_t)info.y + x);
+}
+__device__ __forceinline__ float4 f4add(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ float4 f4mul(float4 a, float f) { return make_float4(a.x * f, a.y * f, a.z * f, a.w * f); }
+// Texture::operator()(Vector2): u, v wrapped into [0, 1), v flipped, nearest or bilinear texel(s).
+__device__ inline float4 tex_lookup(const Scene &S, int t, float u, float v) {
+    const int4 info = __ldg(S.tex_info + t);
+    const uint32_t w = (uint32_t)info.y, h = (uint32_t)info.z;
+    float x = (u + ((float)(((int)(-u)) + 2)));
+    x -= ((float)((int)x));
+    float y = (v + ((float)(((int)(-v)) + 2)));
+    y -= ((float)((int)y));
+    y = (1.0f - y);
+    const float px = (x * ((float)w)), py = (y * ((float)h));
+    const uint32_t min_x = (((uint32_t)px) % w), min_y = (((uint32_t)py) % h);
+    const uint32_t max_x = ((min_x + 1) % w), max_y = ((min_y + 1) % h);
+    const float off_x = (px - ((float)min_x)), off_y = (py - ((float)min_y));
+    if (info.w == DR_FILTER_NONE) return texel(S, info, (off_x <= 0.5f) ? min_x : max_x, (off_y <= 0.5f) ? min_y : max_y);
+    return f4add(f4add(f4add(f4mul(texel(S, info, min_x, min_y), ((1.0f - off_x) * (1.0f - off_y))),
+                             f4mul(texel(S, info, min_x, max_y), ((1.0f - off_x) * off_y))),
+                       f4mul(texel(S, info, max_x, min_y), (off_x * (1.0f - off_y)))),
+                 f4mul(texel(S, info, max_x, max_y), (off_x * off_y)));
+}
+// Texture coordinate of a hit: the corner coordinates weighted by the hit's masses (tex.massCenter).
+__device__ __forceinline__ float2 hit_uv(const Scene &S, int tri, f3 m) {
+    const float2 a = __ldg(S.uv + 3 * (size_t)tri), b = __ldg(S.uv + 3 * (size_t)tri + 1), c = __ldg(S.uv + 3 * (size_t)tri + 2);
+    return make_float2(((a.x * m.x) + (b.x * m.y)) + (c.x * m.z), ((a.y * m.x) + (b.y * m.y)) + (c.y * m.z));
+}
+// The texel a material channel reads at `uv`: texture(uv x tiling + offset).
+__device__ __forceinline__ float4 channel_texel(const Scene &S, const Material &m, int ch, float2 uv) {
+    return tex_lookup(S, m.texture[ch], (uv.x * m.tiling[ch][0]) + m.offset[ch][0], (uv.y * m.tiling[ch][1]) + m.offset[ch][1]);
+}
+__device__ __forceinline__ bool any_texture(const Material &m) {
+    return m.texture[0] >= 0 || m.texture[1] >= 0 || m.texture[2] >= 0 || m.texture[3] >= 0;
+}
+// Alpha cutout: the surface lets paths through where alpha_threshold >= alpha (colour alpha 1).
+__device__ __forceinline__ bool cut_out(const Scene &S, const Material &m, float2 uv) {
+    return m.texture[DR_TEX_ALPHA] >= 0 && m.alpha_threshold >= (1.0f * channel_texel(S, m, DR_TEX_ALPHA, uv).w);
+}
+// Shading normal: the interpolated normal, or with a normal map (ColoredTexture::getNormal) the
+// mapped normal in the frame of that normal, a tangent from the corner texture coordinates and
+// their cross product.
+__device__ inline f3 shading_normal(const Scene &S, const Material &m, int tri, const TriV &v, const TriV &nt, f3 masses, float2 uv) {
+    f3 n = norm3(mass_center(nt, masses));
+    if (m.texture[DR_TEX_NORMAL] < 0) return n;
+    float2 td;
+    f3 vd;
+    const f3 mc = mass_center(v, masses);
+    if (masses.x < 0.999f) {
+        const float2 a = __ldg(S.uv + 3 * (size_t)tri);
+        td = make_float2(a.x - uv.x, a.y - uv.y);
+        vd = sub3(v.a, mc);
+    } else {
+        const float2 b = __ldg(S.uv + 3 * (size_t)tri + 1);
+        td = make_float2(b.x - uv.x, b.y - uv.y);
+        vd = sub3(v.b, mc);
+    }
+    const f3 co = norm3(cross3(vd, n));
+    vd = cross3(co, n);
+    const f3 u = norm3(sub3(mul3(vd, td.y), mul3(co, td.x)));
+    const f3 w = cross3(u, n);
+    const float4 rgb = channel_texel(S, m, DR_TEX_NORMAL, uv);
+    const f3 k = f3{m.normal_color[1] * rgb.z, m.normal_color[0] * ((rgb.x * 2.0f) - 1.0f), m.normal_color[2] * ((rgb.y * 2.0f) - 1.0f)};
+    return norm3(add3(add3(mul3(n, k.x), mul3(u, k.y)), mul3(w, k.z)));
+}
+
 // ---- DumbBasedShader -------------------------------------------------------------------------
-__device__ inline bool dumb_based_request(const Material &m, const TriV &v, const TriV &nt, f3 hit, f3 raydir, uint32_t key,
-                                          uint32_t bounce, f3 &dir, int &type) {
+__device__ inline bool dumb_based_request(const Scene &S, int tri, const Material &m, const TriV &v, const TriV &nt, f3 hit,
+                                          f3 raydir, uint32_t key, uint32_t bounce, f3 &dir, int &type) {
     f3 normal = norm3(tri_normal(v));
     f3 masses = get_masses(v, hit);
+    const bool textured = any_texture(m);
+    const float2 uv = textured ? hit_uv(S, tri, masses) : make_float2(0.0f, 0.0f);
+    if (textured && cut_out(S, m, uv)) {
+        dir = raydir;
+        type = 3;
+        return true;
+    }
     float metal = fmaxf(fminf(m.metal, 1.0f), 0.0f);
     if (rnd(key, bounce, 0) <= metal) {
-        f3 n = norm3(mass_center(nt, masses));
+        f3 n = shading_normal(S, m, tri, v, nt, masses, uv);
         if (dot3(n, raydir) >= 0.0f) return false;
         f3 r = norm3(reflect3(raydir, n));
         if (dot3(r, normal) < 0) normal = mul3(normal, -1.0f);
@@ -114,13 +189,19 @@ __device__ inline bool dumb_based_request(const Material &m, const TriV &v, cons
     return true;
 }
 
-__device__ inline c3 dumb_based_reflect(const Material &m, const TriV &v, const TriV &nt, f3 hit, f3 photon_dir, f3 observer,
-                                        bool direct, int sample_type) {
+__device__ inline c3 dumb_based_reflect(const Scene &S, int tri, const Material &m, const TriV &v, const TriV &nt, f3 hit,
+                                        f3 photon_dir, f3 observer, bool direct, int sample_type) {
     f3 masses = get_masses(v, hit);
+    const bool textured = any_texture(m);
+    const float2 uv = textured ? hit_uv(S, tri, masses) : make_float2(0.0f, 0.0f);
+    if (textured && cut_out(S, m, uv)) {
+        const float pass = (dot3(norm3(observer), norm3(photon_dir)) >= 0.9999f) ? 1.0f : 0.0f;
+        return mkc(pass, pass, pass);
+    }
     if (dot3(norm3(tri_normal(v)), photon_dir) > 0.0f)
         if (!direct) return mkc(1, 1, 1);
     if (dot3(mass_center(nt, masses), observer) < 0.0f) return mkc(0, 0, 0);
-    f3 n = norm3(mass_center(nt, masses));
+    f3 n = shading_normal(S, m, tri, v, nt, masses, uv);
     f3 wi = neg3(norm3(photon_dir));
     float metal = fmaxf(fminf(m.metal, 1.0f), 0.0f);
     float spec = m.specular;
@@ -132,8 +213,12 @@ __device__ inline c3 dumb_based_reflect(const Material &m, const TriV &v, const 
         float val = (1.0f - dot3(wh, wi));
         float sq = val * val;
         float f5 = sq * sq * val;
-        c3 fwi = mkc(m.fresnel[0] + (1 - m.fresnel[0]) * f5, m.fresnel[1] + (1 - m.fresnel[1]) * f5,
-                     m.fresnel[2] + (1 - m.fresnel[2]) * f5);
+        c3 fres = mkc(m.fresnel[0], m.fresnel[1], m.fresnel[2]);
+        if (m.texture[DR_TEX_FRESNEL] >= 0) {
+            const float4 t = channel_texel(S, m, DR_TEX_FRESNEL, uv);
+            fres = mkc(fres.r * t.x, fres.g * t.y, fres.b * t.z);
+        }
+        c3 fwi = mkc(fres.r + (1 - fres.r) * f5, fres.g + (1 - fres.g) * f5, fres.b + (1 - fres.b) * f5);
         float multiplier;
         if (direct) {
             float dwh = ((spec + 2) / (2.0f * 3.14159265359f)) * powf(dot3(n, wh), spec);
@@ -146,6 +231,10 @@ __device__ inline c3 dumb_based_reflect(const Material &m, const TriV &v, const 
     }
     bool diffuseMatters = (direct || sample_type == 2);
     c3 diff = cscale(mkc(m.color[0], m.color[1], m.color[2]), 1.0f - metal);
+    if (m.texture[DR_TEX_COLOR] >= 0) {
+        const float4 t = channel_texel(S, m, DR_TEX_COLOR, uv);
+        diff = mkc(diff.r * t.x, diff.g * t.y, diff.b * t.z);
+    }
     c3 diffuse = diffuseMatters ? cscale(diff, dot3(n, wi)) : mkc(0, 0, 0);
     if (brdfMatters && diffuseMatters)
         return mkc(fmaxf(0.0f, fminf((brdf.r * metal) + diffuse.r, 1.0f)), fmaxf(0.0f, fminf((brdf.g * metal) + diffuse.g, 1.0f)),
@@ -184,15 +273,20 @@ __device__ inline c3 ss_reflect(const Material &m, const TriV &v, const TriV &nt
 
 // ---- FresnelShader: no indirect samples; DumbTools::fresnel(colour, interpolated normal, -photon
 // direction) (FresnelShader.impl.cuh:11-19, DumbStructs.cuh:136-140); the normal is not normalised.
-__device__ inline c3 fresnel_reflect(const Material &m, const TriV &v, const TriV &nt, f3 hit, f3 photon_dir) {
+__device__ inline c3 fresnel_reflect(const Scene &S, int tri, const Material &m, const TriV &v, const TriV &nt, f3 hit,
+                                     f3 photon_dir) {
     f3 masses = get_masses(v, hit);
     f3 light = neg3(norm3(photon_dir));
     f3 normal = mass_center(nt, masses);
+    c3 col = mkc(m.color[0], m.color[1], m.color[2]);
+    if (m.texture[DR_TEX_COLOR] >= 0) {
+        const float4 t = channel_texel(S, m, DR_TEX_COLOR, hit_uv(S, tri, masses));
+        col = mkc(col.r * t.x, col.g * t.y, col.b * t.z);
+    }
     float val = (1.0f - dot3(normal, light));
     float sq = (val * val);
     float f = sq * sq * val;
-    return mkc(m.color[0] + ((1.0f - m.color[0]) * f), m.color[1] + ((1.0f - m.color[1]) * f),
-               m.color[2] + ((1.0f - m.color[2]) * f));
+    return mkc(col.r + ((1.0f - col.r) * f), col.g + ((1.0f - col.g) * f), col.b + ((1.0f - col.b) * f));
 }
 
 // ---- DefaultShaderGeneric (DefaultShader.impl.cuh:3-52): one sample along the reflection of the
@@ -219,8 +313,8 @@ __device__ inline c3 default_reflect(const Material &m, const TriV &v, const Tri
 __device__ inline c3 ref_reflect(const Scene &S, int tri, f3 hit, f3 photon_dir, f3 observer, bool direct, int sample_type) {
     const Material &m = S.mats[__ldg(S.mat_id + tri)];
     TriV v = load_tri(S.tris, tri), nt = load_tri(S.nrms, tri);
-    if (m.type == 0) return dumb_based_reflect(m, v, nt, hit, photon_dir, observer, direct, sample_type);
-    if (m.type == DR_MAT_FRESNEL) return fresnel_reflect(m, v, nt, hit, photon_dir);
+    if (m.type == 0) return dumb_based_reflect(S, tri, m, v, nt, hit, photon_dir, observer, direct, sample_type);
+    if (m.type == DR_MAT_FRESNEL) return fresnel_reflect(S, tri, m, v, nt, hit, photon_dir);
     if (m.type == DR_MAT_DEFAULT) return default_reflect(m, v, nt, hit, photon_dir, observer);
     return ss_reflect(m, v, nt, hit, photon_dir, observer);
 }

@@ -82,6 +82,20 @@ typedef struct {
 #define DR_MAT_FRESNEL 5
 #define DR_MAT_DEFAULT 6
 
+/* Reference-mode textures (ColoredTexture, __source__/.../Components/DumbStructs.cuh:70-131): a
+ * textured channel is its colour x the texel at (uv x tiling + offset), uv interpolated from the
+ * triangle's corner coordinates (dr_scene_set_textures).  texture[k] is a 1-based index into the
+ * scene's textures, 0 = none (so zero-initialised materials are untextured).  Channels:
+ *   DR_TEX_COLOR   DUMB_BASED diffuse, FRESNEL colour
+ *   DR_TEX_FRESNEL DUMB_BASED fresnel
+ *   DR_TEX_NORMAL  DUMB_BASED normal map (tangent frame from the corner uv; normal_color weights it)
+ *   DR_TEX_ALPHA   DUMB_BASED alpha cutout: where the texel's alpha <= alpha_threshold the surface
+ *                  passes paths and photons straight through */
+#define DR_TEX_COLOR 0
+#define DR_TEX_FRESNEL 1
+#define DR_TEX_NORMAL 2
+#define DR_TEX_ALPHA 3
+
 typedef struct {
     int32_t type;
     float color[3];
@@ -93,6 +107,11 @@ typedef struct {
     float shininess;
     float roughness;
     float emission[3];
+    int32_t texture[4];
+    float tiling[4][2];
+    float offset[4][2];
+    float normal_color[3];
+    float alpha_threshold;
 } dr_material;
 
 /* ---- lights (reference semantics; Light function pack, Light.cuh:14-59) -----------------
@@ -236,6 +255,25 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
  * emission float[n][3], roughness float[n]. */
 dr_status dr_scene_set_triangle_params(dr_scene *scene, const float *albedo, const float *emission,
                                        const float *roughness);
+
+/* Texture images (Texture, __source__/.../Components/Texture/Texture.impl.cuh:81-95): host RGBA
+ * float[height][width][4], row 0 = the image's first row (texture[y][x]); lookups wrap u and v into
+ * [0, 1), flip v and take the nearest texel (DR_FILTER_NONE) or blend four (DR_FILTER_BILINEAR), as
+ * the reference does. */
+#define DR_FILTER_NONE 0
+#define DR_FILTER_BILINEAR 1
+typedef struct {
+    int32_t width;
+    int32_t height;
+    int32_t filtering;
+    const float *rgba;
+} dr_texture;
+
+/* Sets the scene's textures (copied to the device; replaces earlier ones) and per-corner texture
+ * coordinates uv: host float[n][3][2] (BakedTriFace::tex x / y), or NULL for all zeros.  Every
+ * material texture index must be <= n_textures; renders of a scene whose materials use textures
+ * fail until they are set.  Batches created before a later call keep the earlier textures. */
+dr_status dr_scene_set_textures(dr_scene *scene, const dr_texture *textures, int32_t n_textures, const float *uv);
 
 /* Device pointers to the scene's per-triangle albedo and emission (float[n][3] each), for
  * callers that update them in place (e.g. an optimiser).  Emissive-triangle sampling tables are
@@ -431,9 +469,9 @@ void dr_mesh_file_destroy(dr_mesh_file *m);
  * pixel, backface culling; the thread / block settings are validated and not used).  Relative paths
  * resolve against the directory of the file that names them, then the working directory.
  * Materials: dumb_based, simple_stochastic, fresnel_color; lights: simple_soft_directional,
- * simple_spherical, spotlight (everything the reference's registry holds).  Textures (no
- * counterpart in this renderer) and mesh primitives (left unimplemented by the reference) fail the
- * load with a message naming them.  The triangles come out in the reference's push order (an object that
+ * simple_spherical, spotlight (everything the reference's registry holds); textures from PNG files
+ * (by path or name, nearest or bilinear).  Mesh primitives (left unimplemented by the reference)
+ * fail the load with a message.  The triangles come out in the reference's push order (an object that
  * names no OBJ object takes every object of the file, in file order; the reference's order there
  * is that of a hash map). */
 typedef struct dr_scene_file dr_scene_file;
@@ -449,7 +487,15 @@ dr_status dr_scene_file_lights(const dr_scene_file *f, dr_light *lights);
  * iteration 1, seed 0). */
 dr_status dr_scene_file_camera(const dr_scene_file *f, dr_camera *camera);
 dr_status dr_scene_file_render_params(const dr_scene_file *f, dr_render_params *params);
-/* dr_scene_create over the file's geometry, materials and lights (DumbRenderContext::buildFromFile). */
+/* The file's textures (PNG files its materials name; ids in dr_material.texture are 1-based into
+ * this list): count, then size / filtering / texels (float[height][width][4], bytes / 255) of each. */
+int32_t dr_scene_file_textures(const dr_scene_file *f);
+dr_status dr_scene_file_texture(const dr_scene_file *f, int32_t i, int32_t *width, int32_t *height, int32_t *filtering,
+                                float *rgba);
+/* Per-corner texture coordinates of the triangles, float[n][3][2] (from the OBJ files). */
+dr_status dr_scene_file_texcoords(const dr_scene_file *f, float *uv);
+/* dr_scene_create over the file's geometry, materials and lights, then dr_scene_set_textures with
+ * its textures and texture coordinates (DumbRenderContext::buildFromFile). */
 dr_status dr_scene_file_create_scene(const dr_scene_file *f, const dr_build_params *bp, dr_scene **out);
 void dr_scene_file_destroy(dr_scene_file *f);
 

@@ -679,21 +679,101 @@ struct Scene {
     std::vector<dr_material> mats;
     std::vector<dr_light> lights;
     std::vector<struct Spot> spots;                // per light; spotlight constructor state
+    struct Tex {
+        int w, h, filter;
+        std::vector<float> rgba;  // [h][w][4]
+    };
+    std::vector<Tex> tex;                          // dro_scene_set_textures
+    std::vector<float> uv;                         // [n][3][2] corner texture coordinates
     std::vector<float> albedo, emission, rough;  // physical-mode per-triangle params
     std::vector<int> emissive;                   // emissive triangle ids
     std::vector<double> emissive_cdf;            // by power (luminance-free: r+g+b) x area
     double emissive_total = 0.0;
 };
 
+// ---- textures (Texture.impl.cuh:81-95; ColoredTexture, DumbStructs.cuh:88-131) ------------------
+struct F4 {
+    float x, y, z, w;
+};
+inline F4 f4add(F4 a, F4 b) { return F4{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
+inline F4 f4mul(F4 a, float f) { return F4{a.x * f, a.y * f, a.z * f, a.w * f}; }
+inline F4 texel(const Scene::Tex &t, uint32_t x, uint32_t y) {
+    const float *p = &t.rgba[4 * ((size_t)y * (size_t)t.w + x)];
+    return F4{p[0], p[1], p[2], p[3]};
+}
+F4 tex_lookup(const Scene &S, int ti, float u, float v) {
+    const Scene::Tex &t = S.tex[(size_t)ti];
+    const uint32_t w = (uint32_t)t.w, h = (uint32_t)t.h;
+    float x = (u + ((float)(((int)(-u)) + 2)));
+    x -= ((float)((int)x));
+    float y = (v + ((float)(((int)(-v)) + 2)));
+    y -= ((float)((int)y));
+    y = (1.0f - y);
+    const float px = (x * ((float)w)), py = (y * ((float)h));
+    const uint32_t min_x = (((uint32_t)px) % w), min_y = (((uint32_t)py) % h);
+    const uint32_t max_x = ((min_x + 1) % w), max_y = ((min_y + 1) % h);
+    const float off_x = (px - ((float)min_x)), off_y = (py - ((float)min_y));
+    if (t.filter == DR_FILTER_NONE) return texel(t, (off_x <= 0.5f) ? min_x : max_x, (off_y <= 0.5f) ? min_y : max_y);
+    return f4add(f4add(f4add(f4mul(texel(t, min_x, min_y), ((1.0f - off_x) * (1.0f - off_y))),
+                             f4mul(texel(t, min_x, max_y), ((1.0f - off_x) * off_y))),
+                       f4mul(texel(t, max_x, min_y), (off_x * (1.0f - off_y)))),
+                 f4mul(texel(t, max_x, max_y), (off_x * off_y)));
+}
+struct UV {
+    float u, v;
+};
+UV hit_uv(const Scene &S, int tri, V3 m) {
+    const float *p = &S.uv[6 * (size_t)tri];
+    return UV{((p[0] * m.x) + (p[2] * m.y)) + (p[4] * m.z), ((p[1] * m.x) + (p[3] * m.y)) + (p[5] * m.z)};
+}
+bool any_texture(const dr_material &m) { return m.texture[0] > 0 || m.texture[1] > 0 || m.texture[2] > 0 || m.texture[3] > 0; }
+F4 channel_texel(const Scene &S, const dr_material &m, int ch, UV uv) {
+    return tex_lookup(S, m.texture[ch] - 1, (uv.u * m.tiling[ch][0]) + m.offset[ch][0], (uv.v * m.tiling[ch][1]) + m.offset[ch][1]);
+}
+bool cut_out(const Scene &S, const dr_material &m, UV uv) {
+    return m.texture[DR_TEX_ALPHA] > 0 && m.alpha_threshold >= (1.0f * channel_texel(S, m, DR_TEX_ALPHA, uv).w);
+}
+// ColoredTexture::getNormal (DumbStructs.cuh:99-131): the interpolated normal, or the normal map in
+// the frame of that normal, a tangent from the corner texture coordinates and their cross product.
+V3 shading_normal(const Scene &S, const dr_material &m, int tri, const Tri &v, const Tri &nt, V3 masses, UV uv) {
+    V3 n = normalized(mass_center(nt, masses));
+    if (m.texture[DR_TEX_NORMAL] <= 0) return n;
+    const float *p = &S.uv[6 * (size_t)tri];
+    UV td;
+    V3 vd;
+    const V3 mc = mass_center(v, masses);
+    if (masses.x < 0.999f) {
+        td = UV{p[0] - uv.u, p[1] - uv.v};
+        vd = v.a - mc;
+    } else {
+        td = UV{p[2] - uv.u, p[3] - uv.v};
+        vd = v.b - mc;
+    }
+    const V3 co = normalized(cross(vd, n));
+    vd = cross(co, n);
+    const V3 u = normalized((vd * td.v) - (co * td.u));
+    const V3 w = cross(u, n);
+    const F4 rgb = channel_texel(S, m, DR_TEX_NORMAL, uv);
+    const V3 k = v3(m.normal_color[1] * rgb.z, m.normal_color[0] * ((rgb.x * 2.0f) - 1.0f), m.normal_color[2] * ((rgb.y * 2.0f) - 1.0f));
+    return normalized(((n * k.x) + (u * k.y)) + (w * k.z));
+}
+
 // DumbBasedShader::requestIndirectSamples (DumbBasedShader.impl.cuh:18-62).  Returns false when no
 // sample is produced (specular branch with n.ray >= 0); `type` gets the sample type (1 or 2).
-bool dumb_based_request(const dr_material &m, const Tri &v, const Tri &nt, V3 hit, V3 raydir, uint32_t key, uint32_t bounce,
-                        V3 &dir, int &type) {
+bool dumb_based_request(const Scene &S, int tri, const dr_material &m, const Tri &v, const Tri &nt, V3 hit, V3 raydir,
+                        uint32_t key, uint32_t bounce, V3 &dir, int &type) {
     V3 normal = normalized(tri_normal(v));
     V3 masses = get_masses(v, hit);
+    const bool textured = any_texture(m);
+    const UV uv = textured ? hit_uv(S, tri, masses) : UV{0.0f, 0.0f};
+    if (textured && cut_out(S, m, uv)) {
+        dir = raydir;
+        type = 3;
+        return true;
+    }
     float metal = std::fmax(std::fmin(m.metal, 1.0f), 0.0f);
     if (rnd(key, bounce, 0) <= metal) {
-        V3 n = normalized(mass_center(nt, masses));
+        V3 n = shading_normal(S, m, tri, v, nt, masses, uv);
         if (dot(n, raydir) >= 0.0f) return false;
         V3 r = normalized(reflection(raydir, n));
         if (dot(r, normal) < 0) normal = normal * -1.0f;
@@ -724,14 +804,20 @@ bool dumb_based_request(const dr_material &m, const Tri &v, const Tri &nt, V3 hi
 
 // DumbBasedShader::getReflectedColor (DumbBasedShader.impl.cuh:63-122); photon colour factored out
 // (the result is linear in it).  `direct` selects PHOTON_TYPE_DIRECT_ILLUMINATION.
-Col dumb_based_reflect(const dr_material &m, const Tri &v, const Tri &nt, V3 hit, V3 photon_dir, V3 observer, bool direct,
-                       int sample_type, bool &passthrough) {
+Col dumb_based_reflect(const Scene &S, int tri, const dr_material &m, const Tri &v, const Tri &nt, V3 hit, V3 photon_dir,
+                       V3 observer, bool direct, int sample_type, bool &passthrough) {
     passthrough = false;
     V3 masses = get_masses(v, hit);
+    const bool textured = any_texture(m);
+    const UV uv = textured ? hit_uv(S, tri, masses) : UV{0.0f, 0.0f};
+    if (textured && cut_out(S, m, uv)) {
+        const float pass = (dot(normalized(observer), normalized(photon_dir)) >= 0.9999f) ? 1.0f : 0.0f;
+        return Col{pass, pass, pass};
+    }
     if (dot(normalized(tri_normal(v)), photon_dir) > 0.0f)
         if (!direct) { passthrough = true; return Col{1, 1, 1}; }
     if (dot(mass_center(nt, masses), observer) < 0.0f) return Col{0, 0, 0};
-    V3 n = normalized(mass_center(nt, masses));
+    V3 n = shading_normal(S, m, tri, v, nt, masses, uv);
     V3 wi = -normalized(photon_dir);
     float metal = std::fmax(std::fmin(m.metal, 1.0f), 0.0f);
     float spec = m.specular;
@@ -741,6 +827,10 @@ Col dumb_based_reflect(const dr_material &m, const Tri &v, const Tri &nt, V3 hit
         V3 w0 = normalized(observer);
         V3 wh = normalized(w0 + wi);
         Col fres = col(m.fresnel);
+        if (m.texture[DR_TEX_FRESNEL] > 0) {
+            const F4 t = channel_texel(S, m, DR_TEX_FRESNEL, uv);
+            fres = Col{fres.r * t.x, fres.g * t.y, fres.b * t.z};
+        }
         float val = (1.0f - dot(wh, wi));
         float sq = val * val;
         Col fwi = fres + (Col{1 - fres.r, 1 - fres.g, 1 - fres.b} * (sq * sq * val));
@@ -755,6 +845,10 @@ Col dumb_based_reflect(const dr_material &m, const Tri &v, const Tri &nt, V3 hit
     }
     bool diffuseMatters = (direct || sample_type == 2);
     Col diff = col(m.color) * (1.0f - metal);
+    if (m.texture[DR_TEX_COLOR] > 0) {
+        const F4 t = channel_texel(S, m, DR_TEX_COLOR, uv);
+        diff = Col{diff.r * t.x, diff.g * t.y, diff.b * t.z};
+    }
     Col diffuse = diffuseMatters ? diff * dot(n, wi) : Col{0, 0, 0};
     if (brdfMatters && diffuseMatters)
         return Col{std::fmax(0.0f, std::fmin((brdf.r * metal) + diffuse.r, 1.0f)),
@@ -794,14 +888,18 @@ Col ss_reflect(const dr_material &m, const Tri &v, const Tri &nt, V3 hit, V3 pho
 
 // Shaders::FresnelShader::getReflectedColor (FresnelShader.impl.cuh:14-19, DumbStructs.cuh:136-140):
 // Schlick term of the interpolated (not normalised) normal and the reversed photon direction.
-Col fresnel_reflect(const dr_material &m, const Tri &v, const Tri &nt, V3 hit, V3 photon_dir) {
+Col fresnel_reflect(const Scene &S, int tri, const dr_material &m, const Tri &v, const Tri &nt, V3 hit, V3 photon_dir) {
     V3 masses = get_masses(v, hit);
     V3 light = -normalized(photon_dir);
     V3 normal = mass_center(nt, masses);
+    Col c = col(m.color);
+    if (m.texture[DR_TEX_COLOR] > 0) {
+        const F4 t = channel_texel(S, m, DR_TEX_COLOR, hit_uv(S, tri, masses));
+        c = Col{c.r * t.x, c.g * t.y, c.b * t.z};
+    }
     float val = (1.0f - dot(normal, light));
     float sq = (val * val);
     float f = sq * sq * val;
-    Col c = col(m.color);
     return Col{c.r + ((1.0f - c.r) * f), c.g + ((1.0f - c.g) * f), c.b + ((1.0f - c.b) * f)};
 }
 
@@ -824,8 +922,8 @@ Col reflect(const Scene &S, int tri, V3 hit, V3 photon_dir, V3 observer, bool di
     const dr_material &m = S.mats[S.mat[tri]];
     pass = false;
     if (m.type == DR_MAT_DUMB_BASED)
-        return dumb_based_reflect(m, S.tree.tri[tri], S.nrm[tri], hit, photon_dir, observer, direct, sample_type, pass);
-    if (m.type == DR_MAT_FRESNEL) return fresnel_reflect(m, S.tree.tri[tri], S.nrm[tri], hit, photon_dir);
+        return dumb_based_reflect(S, tri, m, S.tree.tri[tri], S.nrm[tri], hit, photon_dir, observer, direct, sample_type, pass);
+    if (m.type == DR_MAT_FRESNEL) return fresnel_reflect(S, tri, m, S.tree.tri[tri], S.nrm[tri], hit, photon_dir);
     if (m.type == DR_MAT_DEFAULT) return default_reflect(m, S.tree.tri[tri], S.nrm[tri], hit, photon_dir, observer);
     return ss_reflect(m, S.tree.tri[tri], S.nrm[tri], hit, photon_dir, observer);
 }
@@ -987,7 +1085,7 @@ Col ref_path(const Scene &S, const Cam &cam, const dr_render_params &p, float sx
         const dr_material &m = S.mats[S.mat[hit]];
         if (layer < p.max_bounces) {
             if (m.type == DR_MAT_DUMB_BASED)
-                have_child = dumb_based_request(m, S.tree.tri[hit], S.nrm[hit], hp, d, key, (uint32_t)layer, cd, ctype);
+                have_child = dumb_based_request(S, hit, m, S.tree.tri[hit], S.nrm[hit], hp, d, key, (uint32_t)layer, cd, ctype);
             else if (m.type == DR_MAT_FRESNEL)
                 have_child = false;
             else if (m.type == DR_MAT_DEFAULT) {
@@ -1308,6 +1406,19 @@ void *dro_scene_create(const float *xyz, const float *nrm, const int *mat, int n
     }
     S->tree.build(threads > 0 ? threads : (int)std::thread::hardware_concurrency());
     return S;
+}
+
+// Textures and per-corner texture coordinates (float[n][3][2] or NULL for zeros), as dr_scene_set_textures.
+void dro_scene_set_textures(void *h, const dr_texture *tex, int n, const float *uv) {
+    Scene *S = (Scene *)h;
+    S->tex.clear();
+    for (int i = 0; i < n; i++) {
+        Scene::Tex t{tex[i].width, tex[i].height, tex[i].filtering, {}};
+        t.rgba.assign(tex[i].rgba, tex[i].rgba + 4 * (size_t)tex[i].width * (size_t)tex[i].height);
+        S->tex.push_back(std::move(t));
+    }
+    S->uv.assign(6 * S->tree.tri.size(), 0.0f);
+    if (uv) std::memcpy(S->uv.data(), uv, sizeof(float) * S->uv.size());
 }
 
 void dro_scene_set_triangle_params(void *h, const float *albedo, const float *emission, const float *rough) {

@@ -35,7 +35,7 @@
 typedef Renderable<BakedTriFace> RefUnit;
 typedef Octree<RefUnit> RefOctree;
 
-static BakedTriFace make_face(const float *v, const float *n) {
+static BakedTriFace make_face(const float *v, const float *n, const float *uv = NULL) {
 	Triangle vert(Vector3(v[0], v[1], v[2]), Vector3(v[3], v[4], v[5]), Vector3(v[6], v[7], v[8]));
 	Triangle norm;
 	if (n != NULL) norm = Triangle(Vector3(n[0], n[1], n[2]), Vector3(n[3], n[4], n[5]), Vector3(n[6], n[7], n[8]));
@@ -45,27 +45,58 @@ static BakedTriFace make_face(const float *v, const float *n) {
 		norm = Triangle(fn, fn, fn);
 	}
 	Triangle tex(Vector3(0, 0, 0), Vector3(1, 0, 0), Vector3(0, 1, 0));
+	if (uv != NULL) tex = Triangle(Vector3(uv[0], uv[1], 0), Vector3(uv[2], uv[3], 0), Vector3(uv[4], uv[5], 0));
 	return BakedTriFace(vert, norm, tex);
 }
 
-// Records (16 floats) of the reference objects the scene holds, built through their constructors.
-//   material: [0] 0 DumbBasedShader (fresnel [1..3], specular [4], diffuse [5..7], metal [8]),
-//             1 SimpleStochasticShader (colour [1..3], diffuse [4], smoothness [5], shininess [6]),
-//             2 Shaders::FresnelShader (colour [1..3]), 3 DefaultShader (as 1)
+// Records of the reference objects the scene holds, built through their constructors.
+//   material (48 floats): [0] 0 DumbBasedShader (fresnel [1..3], specular [4], diffuse [5..7],
+//             metal [8]), 1 SimpleStochasticShader (colour [1..3], diffuse [4], smoothness [5],
+//             shininess [6]), 2 Shaders::FresnelShader (colour [1..3]), 3 DefaultShader (as 1);
+//             textures: [16..19] 1-based texture of the diffuse / fresnel / normal / alpha-cutout
+//             ColoredTexture (0 = none; the Fresnel shader's colour is the first), [20..27] their
+//             tilings, [28..35] offsets, [36..38] normal-map colour, [39] alpha-cutout threshold
+//   light (16 floats):
 //   light:    [0] 0 SphericalLightEmitter (colour [1..3], position [4..6], radius [7]),
 //             1 SimpleSoftDirectionalLight (colour, direction [4..6], distance [7], softness [8]),
 //             2 SimpleDirectionalLight (colour, direction, distance [7]),
 //             3 Lights::Spotlight (colour, position [4..6], direction [7..9], luminosity [10], hotspot
 //               [11] and falloff [12] angles, falloff power [13], emitter size [14], flags [15]:
 //               1 emit from sphere, 2 cast shadows, samples << 2)
+namespace {
+// DumbBasedShader sets its alpha cutout only in fromDson; explicit instantiation (exempt from access
+// checks) reaches the two members.
+template <class Tag, typename Tag::type M>
+struct RobRef {
+	friend typename Tag::type get(Tag) { return M; }
+};
+struct RobCut { typedef ColoredTexture DumbBasedShader::*type; friend type get(RobCut); };
+template struct RobRef<RobCut, &DumbBasedShader::alphaCutout>;
+struct RobCutThr { typedef float DumbBasedShader::*type; friend type get(RobCutThr); };
+template struct RobRef<RobCutThr, &DumbBasedShader::alphaCutoutThreshold>;
+
+// Channel k of a material record as a ColoredTexture of colour c.
+ColoredTexture channel(const float *m, int k, Color c) {
+	const int t = (int)m[16 + k];
+	if (t <= 0) return ColoredTexture(c);
+	return ColoredTexture(c, t - 1, Vector2(m[20 + 2 * k], m[21 + 2 * k]), Vector2(m[28 + 2 * k], m[29 + 2 * k]));
+}
+}  // namespace
+
 void ref_material(Material<BakedTriFace> &dst, const float *m) {
 	const int type = (int)m[0];
-	if (type == 0)
-		dst.use<DumbBasedShader>((ColoredTexture)ColorRGB(m[1], m[2], m[3]), m[4], (ColoredTexture)ColorRGB(m[5], m[6], m[7]), m[8]);
+	if (type == 0) {
+		const Color white(1.0f, 1.0f, 1.0f, 1.0f);
+		const ColoredTexture normal = channel(m, 2, Color(m[36], m[37], m[38], 1.0f));
+		DumbBasedShader *d = dst.use<DumbBasedShader>(channel(m, 1, Color(m[1], m[2], m[3], 1.0f)), m[4],
+			channel(m, 0, Color(m[5], m[6], m[7], 1.0f)), m[8], normal);
+		if ((int)m[19] > 0) d->*get(RobCut()) = channel(m, 3, white);
+		d->*get(RobCutThr()) = m[39];
+	}
 	else if (type == 1)
 		dst.use<SimpleStochasticShader>(ColorRGB(m[1], m[2], m[3]), m[4], m[5], m[6]);
 	else if (type == 2)
-		dst.use<Shaders::FresnelShader>(ColoredTexture(Color(m[1], m[2], m[3], 1.0f)));
+		dst.use<Shaders::FresnelShader>(channel(m, 0, Color(m[1], m[2], m[3], 1.0f)));
 	else
 		dst.use<DefaultShader>(ColorRGB(m[1], m[2], m[3]), m[4], m[5], m[6]);
 }
@@ -141,12 +172,13 @@ struct RefScene {
 	DumbRenderer::CameraManager camera;
 };
 
-void *dref_scene_create(const float *xyz, const float *nrm, const int *mat, int n,
-                        const float *mats, int n_mats, const float *lights, int n_lights, const float *cam) {
+// uv: per-corner texture coordinates float[n][3][2] or NULL (the fixed (0,0) (1,0) (0,1) corners).
+void *dref_scene_create_uv(const float *xyz, const float *nrm, const float *uv, const int *mat, int n,
+                           const float *mats, int n_mats, const float *lights, int n_lights, const float *cam) {
 	RefScene *s = new RefScene();
 	s->scene.materials.cpuHandle()->flush(n_mats);
 	for (int i = 0; i < n_mats; i++) {
-		const float *m = mats + 16 * i;
+		const float *m = mats + 48 * i;
 		Material<BakedTriFace> &dst = s->scene.materials.cpuHandle()->operator[](i);
 		ref_material(dst, m);
 	}
@@ -162,9 +194,35 @@ void *dref_scene_create(const float *xyz, const float *nrm, const int *mat, int 
 	s->camera.cpuHandle()->transform = Transform(Vector3(cam[8], cam[9], cam[10]), Vector3(cam[11], cam[12], cam[13]), Vector3(1.0f, 1.0f, 1.0f));
 	RefOctree *tree = s->scene.geometry.cpuHandle();
 	for (int i = 0; i < n; i++)
-		tree->push(RefUnit(make_face(xyz + 9 * i, (nrm != NULL) ? (nrm + 9 * i) : NULL), (mat != NULL) ? mat[i] : 0));
+		tree->push(RefUnit(make_face(xyz + 9 * i, (nrm != NULL) ? (nrm + 9 * i) : NULL, (uv != NULL) ? (uv + 6 * i) : NULL),
+			(mat != NULL) ? mat[i] : 0));
 	tree->build();
 	return (void *)s;
+}
+
+void *dref_scene_create(const float *xyz, const float *nrm, const int *mat, int n,
+                        const float *mats, int n_mats, const float *lights, int n_lights, const float *cam) {
+	return dref_scene_create_uv(xyz, nrm, NULL, mat, n, mats, n_mats, lights, n_lights, cam);
+}
+
+// The scene's textures: texture t is width whf[3t] x height whf[3t+1] with Texture::Filtering
+// whf[3t+2], texels rgba[t] (float[h][w][4], row 0 first).
+void dref_scene_set_textures(void *h, int n, const int *whf, const float *const *rgba) {
+	RefScene *s = (RefScene *)h;
+	Stacktor<Texture> *tex = s->scene.textures.cpuHandle();
+	tex->clear();
+	tex->flush(n);
+	for (int t = 0; t < n; t++) {
+		Texture &x = (*tex)[t];
+		const int w = whf[3 * t], hh = whf[3 * t + 1];
+		x.setReolution((uint32_t)w, (uint32_t)hh);
+		x.setFiltering((Texture::Filtering)whf[3 * t + 2]);
+		for (int y = 0; y < hh; y++)
+			for (int xx = 0; xx < w; xx++) {
+				const float *p = rgba[t] + 4 * ((size_t)y * w + xx);
+				x((uint32_t)xx, (uint32_t)y) = Color(p[0], p[1], p[2], p[3]);
+			}
+	}
 }
 
 void dref_scene_destroy(void *h) { delete (RefScene *)h; }

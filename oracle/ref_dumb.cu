@@ -100,15 +100,21 @@ bool is_type(const Generic_ &g) {
 	return std::memcmp(&g.functions(), &probe.functions(), sizeof(Pack)) == 0;
 }
 
-// Canonical dumps (float[16]); the same layout for both sides of the comparison.
-//   material: [0]=type (0 DumbBasedShader, 1 SimpleStochasticShader, -1 other)
+// Canonical dumps; the same layout for both sides of the comparison.
+//   material (float[48]): [0]=type (0 DumbBasedShader, 1 SimpleStochasticShader, -1 other)
 //     DumbBased: [1..3] fresnelColor, [4..6] diffuseColor (constructor-scaled), [7] spec,
-//       [8] specMass, [9] alphaCutoutThreshold, [10..13] texture ids fresnel/diffuse/normal/alpha
+//       [8] specMass, [9] alphaCutoutThreshold, [10..13] texture ids fresnel/diffuse/normal/alpha,
+//       [16..35] those four channels' (id, tiling, offset), [36..38] normal colour, [39..42] cutout colour
 //     SimpleStochastic: [1..3] albedo, [4] diff, [5] gloss, [6] shine
-//     (2) FresnelShader: [1..3] colour, [4] texture id;  (3) DefaultShader: [1..3] albedo, [4] diff,
+//     (2) FresnelShader: [1..3] colour, [4] texture id, [16..20] (id, tiling, offset);  (3) DefaultShader: [1..3] albedo, [4] diff,
 //       [5] gloss, [6] shininess
+// Texture channel c of a ColoredTexture into o: [0] texture id, [1..2] tiling, [3..4] offset.
+void dump_channel(const ColoredTexture &c, float *o) {
+	o[0] = (float)c.textureId;
+	o[1] = c.tiling.x; o[2] = c.tiling.y; o[3] = c.offset.x; o[4] = c.offset.y;
+}
 void dump_material(const Material<BakedTriFace> &m, float *o) {
-	std::memset(o, 0, 16 * sizeof(float));
+	std::memset(o, 0, 48 * sizeof(float));
 	typedef Shader<BakedTriFace> Pack;
 	if (is_type<Pack, Material<BakedTriFace>, DumbBasedShader>(m)) {
 		const DumbBasedShader *s = m.getObject<DumbBasedShader>();
@@ -119,6 +125,10 @@ void dump_material(const Material<BakedTriFace> &m, float *o) {
 		o[7] = s->*get(RobSpec()); o[8] = s->*get(RobSpecMass()); o[9] = s->*get(RobAlphaThr());
 		o[10] = (float)f.textureId; o[11] = (float)d.textureId;
 		o[12] = (float)(s->*get(RobNormal())).textureId; o[13] = (float)(s->*get(RobAlpha())).textureId;
+		const ColoredTexture &nc = s->*get(RobNormal()), &ac = s->*get(RobAlpha());
+		dump_channel(f, o + 16); dump_channel(d, o + 21); dump_channel(nc, o + 26); dump_channel(ac, o + 31);
+		o[36] = nc.color.r; o[37] = nc.color.g; o[38] = nc.color.b;
+		o[39] = ac.color.r; o[40] = ac.color.g; o[41] = ac.color.b; o[42] = ac.color.a;
 	} else if (is_type<Pack, Material<BakedTriFace>, SimpleStochasticShader>(m)) {
 		const SimpleStochasticShader *s = m.getObject<SimpleStochasticShader>();
 		const ColorRGB &a = s->*get(RobAlbedo());
@@ -129,6 +139,7 @@ void dump_material(const Material<BakedTriFace> &m, float *o) {
 		const ColoredTexture &c = m.getObject<Shaders::FresnelShader>()->*get(RobFresnelColor());
 		o[0] = 2;
 		o[1] = c.color.r; o[2] = c.color.g; o[3] = c.color.b; o[4] = (float)c.textureId;
+		dump_channel(c, o + 16);
 	} else if (is_type<Pack, Material<BakedTriFace>, DefaultShader>(m)) {
 		const DefaultShader *s = m.getObject<DefaultShader>();
 		const ColorRGB &a = s->*get(RobDefAlbedo());
@@ -247,9 +258,33 @@ void dref_dumb_geometry(void *h, float *xyz, float *nrm, int *mat) {
 	}
 }
 
+// Texture coordinates of the pushed triangles (tex corners x, y): uv[n][3][2].
+void dref_dumb_texcoords(void *h, float *uv) {
+	DumbRenderContextData *d = ctx_data(&((RefDumb *)h)->ctx);
+	const Stacktor<Renderable<BakedTriFace> > &units = d->scene.geometry.cpuHandle()->getData();
+	for (int i = 0; i < units.size(); i++) {
+		const Triangle &t = units[i].object.tex;
+		const Vector3 *c[3] = { &t.a, &t.b, &t.c };
+		for (int k = 0; k < 3; k++) { uv[6 * i + 2 * k] = c[k]->x; uv[6 * i + 2 * k + 1] = c[k]->y; }
+	}
+}
+// Texture count, then texture i's size, filtering and texels (float[h][w][4]) when rgba is not NULL.
+int dref_dumb_texture_count(void *h) { return ctx_data(&((RefDumb *)h)->ctx)->scene.textures.cpuHandle()->size(); }
+void dref_dumb_texture(void *h, int i, int *whf, float *rgba) {
+	const Texture &t = (*ctx_data(&((RefDumb *)h)->ctx)->scene.textures.cpuHandle())[i];
+	whf[0] = (int)t.width(); whf[1] = (int)t.height(); whf[2] = (int)t.filtering();
+	if (rgba == NULL) return;
+	for (uint32_t y = 0; y < t.height(); y++)
+		for (uint32_t x = 0; x < t.width(); x++) {
+			const Color &c = t(x, y);
+			float *p = rgba + 4 * ((size_t)y * t.width() + x);
+			p[0] = c.r; p[1] = c.g; p[2] = c.b; p[3] = c.a;
+		}
+}
+
 void dref_dumb_material(void *h, int i, float *out) {
 	DumbRenderContextData *d = ctx_data(&((RefDumb *)h)->ctx);
-	dump_material((*d->scene.materials.cpuHandle())[i], out);
+	dump_material((*d->scene.materials.cpuHandle())[i], out);  // float[48]
 }
 void dref_dumb_light(void *h, int i, float *out) {
 	DumbRenderContextData *d = ctx_data(&((RefDumb *)h)->ctx);

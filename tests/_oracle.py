@@ -28,6 +28,7 @@ def oracle():
         L.dro_scene_create.restype = vp
         L.dro_scene_create.argtypes = [vp, vp, vp, ci, vp, ci, vp, ci, ci, ci, ci]
         L.dro_scene_set_triangle_params.argtypes = [vp, vp, vp, vp]
+        L.dro_scene_set_textures.argtypes = [vp, vp, ci, vp]
         L.dro_scene_destroy.argtypes = [vp]
         L.dro_node_count.restype = ctypes.c_longlong
         L.dro_node_count.argtypes = [vp]
@@ -116,6 +117,17 @@ class OracleScene:
         oracle().dro_scene_set_triangle_params(self.h, *[None if a is None else a.ctypes.data for a in arrs])
         self._keep = arrs
 
+    def set_textures(self, textures, uv=None):
+        """As dumbray_gb300.Scene.set_textures."""
+        self._tex = [np.ascontiguousarray(t, dtype=np.float32) for t, _ in textures]
+        arr = (dr.DrTexture * max(1, len(self._tex)))()
+        for i, (img, (_, filt)) in enumerate(zip(self._tex, textures)):
+            arr[i].width, arr[i].height, arr[i].filtering = img.shape[1], img.shape[0], int(filt)
+            arr[i].rgba = img.ctypes.data
+        self._uv = None if uv is None else np.ascontiguousarray(uv, dtype=np.float32).reshape(-1, 3, 2)
+        oracle().dro_scene_set_textures(self.h, ctypes.addressof(arr), len(self._tex),
+                                        None if self._uv is None else self._uv.ctypes.data)
+
     def node_count(self):
         return oracle().dro_node_count(self.h)
 
@@ -179,8 +191,13 @@ def ref_cast(tris, o, d, cull=True, threads=8):
 
 
 def ref_material_record(m: dr.DrMaterial) -> np.ndarray:
-    """Constructor record for oracle/ref_driver.cu's ref_material."""
-    r = np.zeros(16, np.float32)
+    """Constructor record (48 floats) for oracle/ref_driver.cu's ref_material."""
+    r = np.zeros(48, np.float32)
+    r[16:20] = list(m.texture)
+    r[20:28] = [m.tiling[k][j] for k in range(4) for j in range(2)]
+    r[28:36] = [m.offset[k][j] for k in range(4) for j in range(2)]
+    r[36:39] = list(m.normal_color)
+    r[39] = m.alpha_threshold
     if m.type == dr.MAT_DUMB_BASED:
         r[:9] = [0, *m.fresnel, m.specular, *m.color, m.metal]
     elif m.type == dr.MAT_SIMPLE_STOCHASTIC:
@@ -223,8 +240,9 @@ def ref_camera_record(c: dr.DrCamera) -> np.ndarray:
 
 
 def ref_render(tris, mat_id, materials, lights, cam, width, height, fsaa=(1, 1), max_bounces=2, cull=True, iterations=1,
-               threads=8, normals=None):
-    """Reference DumbRenderer on CPU threads; returns (row-major RGBA image, seconds)."""
+               threads=8, normals=None, uv=None, textures=()):
+    """Reference DumbRenderer on CPU threads; returns (row-major RGBA image, seconds).  ``uv``: corner
+    texture coordinates [n, 3, 2]; ``textures``: [(rgba float [h, w, 4], filtering)]."""
     L = reference()
     tris = np.ascontiguousarray(tris, np.float32)
     mat = np.ascontiguousarray(mat_id, np.int32)
@@ -232,8 +250,18 @@ def ref_render(tris, mat_id, materials, lights, cam, width, height, fsaa=(1, 1),
     lrec = np.ascontiguousarray(np.stack([ref_light_record(l) for l in lights]))
     crec = ref_camera_record(cam)
     nrm = None if normals is None else np.ascontiguousarray(normals, np.float32)
-    h = L.dref_scene_create(tris.ctypes.data, None if nrm is None else nrm.ctypes.data, mat.ctypes.data, len(tris),
-                            mrec.ctypes.data, len(mrec), lrec.ctypes.data, len(lrec), crec.ctypes.data)
+    uvs = None if uv is None else np.ascontiguousarray(uv, np.float32).reshape(-1, 3, 2)
+    L.dref_scene_create_uv.restype = vp
+    L.dref_scene_create_uv.argtypes = [vp, vp, vp, vp, ci, vp, ci, vp, ci, vp]
+    h = L.dref_scene_create_uv(tris.ctypes.data, None if nrm is None else nrm.ctypes.data,
+                               None if uvs is None else uvs.ctypes.data, mat.ctypes.data, len(tris),
+                               mrec.ctypes.data, len(mrec), lrec.ctypes.data, len(lrec), crec.ctypes.data)
+    if textures:
+        imgs = [np.ascontiguousarray(t, np.float32) for t, _ in textures]
+        whf = np.array([[im.shape[1], im.shape[0], int(f)] for im, (_, f) in zip(imgs, textures)], np.int32)
+        ptrs = (ctypes.c_void_p * len(imgs))(*[im.ctypes.data for im in imgs])
+        L.dref_scene_set_textures.argtypes = [vp, ci, vp, vp]
+        L.dref_scene_set_textures(h, len(imgs), whf.ctypes.data, ptrs)
     try:
         img = np.zeros((height, width, 4), np.float32)
         sec = L.dref_render(h, width, height, fsaa[0], fsaa[1], max_bounces, 1 if cull else 0, iterations, threads,
@@ -290,7 +318,7 @@ def ref_scene_file_dump(path):
         nrm = np.zeros((n, 9), np.float32)
         mat = np.zeros(n, np.int32)
         L.dref_dumb_geometry(h, xyz.ctypes.data, nrm.ctypes.data, mat.ctypes.data)
-        mats = np.zeros((int(c[1]), 16), np.float32)
+        mats = np.zeros((int(c[1]), 48), np.float32)
         for i in range(int(c[1])):
             L.dref_dumb_material(h, i, mats[i].ctypes.data)
         lights = np.zeros((int(c[2]), 16), np.float32)
@@ -300,7 +328,21 @@ def ref_scene_file_dump(path):
         L.dref_dumb_camera(h, cam.ctypes.data)
         settings = np.zeros(8, np.int32)
         L.dref_dumb_settings(h, settings.ctypes.data)
-        return dict(xyz=xyz, nrm=nrm, mat=mat, materials=mats, lights=lights, camera=cam[:29], settings=settings[:6])
+        uv = np.zeros((n, 6), np.float32)
+        L.dref_dumb_texcoords.argtypes = [vp, vp]
+        L.dref_dumb_texcoords(h, uv.ctypes.data)
+        L.dref_dumb_texture_count.restype = ci
+        L.dref_dumb_texture_count.argtypes = [vp]
+        L.dref_dumb_texture.argtypes = [vp, ci, vp, vp]
+        textures = []
+        for i in range(L.dref_dumb_texture_count(h)):
+            whf = np.zeros(3, np.int32)
+            L.dref_dumb_texture(h, i, whf.ctypes.data, None)
+            img = np.zeros((whf[1], whf[0], 4), np.float32)
+            L.dref_dumb_texture(h, i, whf.ctypes.data, img.ctypes.data)
+            textures.append((img, int(whf[2])))
+        return dict(xyz=xyz, nrm=nrm, mat=mat, materials=mats, lights=lights, camera=cam[:29], settings=settings[:6],
+                    uv=uv, textures=textures)
     finally:
         L.dref_dumb_free(h)
 
@@ -310,7 +352,7 @@ def scene_file_dump(f):
     reference's constructors (dref_record_*), the transform fields are the camera's own."""
     L = reference()
     n = len(f.tris)
-    mats = np.zeros((len(f.materials), 16), np.float32)
+    mats = np.zeros((len(f.materials), 48), np.float32)
     for i, m in enumerate(f.materials):
         rec = ref_material_record(m)
         L.dref_record_material(rec.ctypes.data, mats[i].ctypes.data)
@@ -332,7 +374,7 @@ def scene_file_dump(f):
     p = f.params
     settings = np.array([p.boxing, p.max_bounces, p.samples_x, p.samples_y, 1, p.cull_backfaces], np.int32)
     return dict(xyz=f.tris.reshape(n, 9), nrm=f.normals.reshape(n, 9), mat=f.mat_id, materials=mats, lights=lights,
-                camera=cam[:29], settings=settings)
+                camera=cam[:29], settings=settings, uv=f.uv.reshape(n, 6), textures=list(f.textures))
 
 
 def ref_dumb_render(path, width, height, iterations, threads=8):

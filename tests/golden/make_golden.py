@@ -11,11 +11,17 @@
                    of each reference shader (DumbBased diffuse / metal, SimpleStochastic, Fresnel,
                    Default) under a spherical light, and under spotlights (disc emitter with shadows;
                    sphere emitter without shadows beside a soft directional light).
+  render_tex_*.npz the same reference renders of textured scenes (texture_scene: textured diffuse
+                   and fresnel channels with tiling / offset, a normal map, an alpha-cutout screen,
+                   a textured Fresnel shader; nearest and bilinear filtering), 32x32.
   scene_file/      a scene file (scene.dumb including materials.dumb, meshes in props.obj) that uses
                    presets, groups with fallback / override materials, rotated and scaled items and a
                    rotated spherical-segment camera; render_scene_file.npz holds the reference's renders
                    of it, loaded by the reference's own DumbRenderContext::fromFile (four runs of 512
                    iterations, 32x24).
+  scene_file_tex/  a textured scene file (PNG textures by path and by name, nearest / bilinear, tiling
+                   and offsets, a normal map, an alpha-cutout screen, a textured fresnel_color; an OBJ
+                   with texture coordinates); render_scene_file_tex.npz as above, 32x32.
 
 Run from the repository root after `bash oracle/build_ref.sh`:  python tests/golden/make_golden.py
 """
@@ -109,6 +115,108 @@ def render_fixtures(iterations=512, runs=4, size=32, bounces=2, kinds=RENDER_KIN
         print(kind, "reference seconds", secs, "mean", runs_arr[..., :3].mean())
 
 
+def _room_uv(room):
+    """Planar texture coordinates of the room's walls: the two coordinates along each face."""
+    uv = np.zeros((len(room), 3, 2), np.float32)
+    for i, t in enumerate(room):
+        n = np.abs(np.cross(t[1] - t[0], t[2] - t[0]))
+        ax = int(np.argmax(n))
+        a, b = [k for k in range(3) if k != ax]
+        uv[i, :, 0] = t[:, a] * 0.5 + 0.5
+        uv[i, :, 1] = t[:, b] * 0.5 + 0.5
+    return uv
+
+
+def _sphere_uv(sph):
+    """Spherical texture coordinates of the sphere's corners."""
+    p = sph.astype(np.float64)
+    r = np.linalg.norm(p, axis=-1)
+    u = 0.5 + np.arctan2(p[..., 2], p[..., 0]) / (2 * np.pi)
+    v = 0.5 + np.arcsin(np.clip(p[..., 1] / r, -1, 1)) / np.pi
+    return np.stack([u, v], axis=-1).astype(np.float32)
+
+
+def _texture(kind, size, seed):
+    rng = np.random.default_rng(seed)
+    h, w = size
+    yy, xx = np.mgrid[0:h, 0:w]
+    img = np.ones((h, w, 4), np.float32)
+    if kind == "checker":
+        c = ((xx // 2 + yy // 2) % 2).astype(np.float32)
+        img[..., :3] = 0.25 + 0.6 * c[..., None] * np.array([1.0, 0.8, 0.6], np.float32)
+    elif kind == "noise":
+        img[..., :3] = rng.uniform(0.2, 1.0, size=(h, w, 3)).astype(np.float32)
+    elif kind == "bumps":
+        a = 2 * np.pi * xx / w
+        b = 2 * np.pi * yy / h
+        img[..., 0] = 0.5 + 0.25 * np.sin(a * 2)
+        img[..., 1] = 0.5 + 0.25 * np.cos(b * 3)
+        img[..., 2] = 0.9
+    elif kind == "stripes":
+        img[..., :3] = 0.8
+        img[..., 3] = ((xx // 3) % 2).astype(np.float32)
+    return img
+
+
+def texture_scene(kind: str):
+    """Textured scenes: the render_scene room and sphere with texture coordinates (planar on the walls,
+    spherical on the sphere) and textures from _texture.  Returns (tris, mat, mats, lights, cam, uv,
+    textures); textures are [(rgba, filtering)]."""
+    room = scenes.box((2.0, 2.0, 2.0), inward=True)
+    sph = scenes.icosphere(2, 0.5)
+    parts = [room, sph]
+    uvs = [_room_uv(room), _sphere_uv(sph)]
+    white = dr.dumb_based(diffuse=(0.7, 0.7, 0.7), metal=0.0)
+    red = dr.dumb_based(diffuse=(0.7, 0.1, 0.1), metal=0.0)
+    textures = [(_texture("checker", (16, 16), 1), dr.FILTER_BILINEAR), (_texture("noise", (8, 8), 2), dr.FILTER_NONE),
+                (_texture("bumps", (32, 32), 3), dr.FILTER_BILINEAR), (_texture("stripes", (12, 12), 4), dr.FILTER_NONE)]
+    if kind == "tex_diffuse":
+        obj = dr.textured(dr.textured(dr.dumb_based(fresnel=(0.6, 0.5, 0.4), specular=32.0, diffuse=(0.9, 0.9, 0.9), metal=0.3),
+                                      dr.TEX_COLOR, 0, (2.0, 1.5), (0.1, -0.2)), dr.TEX_FRESNEL, 1)
+        white = dr.textured(white, dr.TEX_COLOR, 1, (3.0, 3.0))
+    elif kind == "tex_normal":
+        obj = dr.textured(dr.textured(dr.dumb_based(fresnel=(0.9, 0.8, 0.6), specular=24.0, diffuse=(0.8, 0.7, 0.6), metal=0.6),
+                                      dr.TEX_NORMAL, 2, (2.0, 2.0)), dr.TEX_COLOR, 0)
+        obj.normal_color[:] = (1.0, 0.8, 0.9)
+    elif kind == "tex_alpha":
+        obj = dr.dumb_based(diffuse=(0.5, 0.6, 0.7), metal=0.0)
+        screen = scenes.quad((0.0, 0.0, -0.6), (1.2, 1.2), (0.0, 0.0, -1.0), up=(0.0, 1.0, 0.0))
+        parts.append(screen)
+        uvs.append(np.array([[[x * 0.5 + 0.5, y * 0.5 + 0.5] for x, y, _ in t] for t in screen / 0.6], np.float32))
+    else:  # tex_fresnel
+        obj = dr.textured(dr.fresnel_shader((0.9, 0.6, 0.3)), dr.TEX_COLOR, 0, (4.0, 2.0))
+    tris = np.concatenate(parts)
+    uv = np.concatenate(uvs)
+    mat = np.zeros(len(tris), np.int32)
+    mat[0:2] = 1
+    mat[len(room):len(room) + len(sph)] = 2
+    mats = [white, red, obj]
+    if kind == "tex_alpha":
+        mat[len(room) + len(sph):] = 3
+        mats.append(dr.textured(dr.dumb_based(diffuse=(0.9, 0.4, 0.2), metal=0.0), dr.TEX_ALPHA, 3, (1.0, 1.0)))
+    lights = [dr.spherical_light((1.5, 1.5, 1.5), (0.0, 0.8, 0.0), 0.1)]
+    cam = dr.camera(dr.LENS_SIMPLE_STOCHASTIC, position=(0.0, 0.0, -0.95), angle=60.0)
+    return tris, mat, mats, lights, cam, uv, textures
+
+
+TEXTURE_KINDS = ("tex_diffuse", "tex_normal", "tex_alpha", "tex_fresnel")
+
+
+def texture_fixtures(iterations=512, runs=4, size=32, bounces=2, kinds=TEXTURE_KINDS):
+    for kind in kinds:
+        tris, mat, mats, lights, cam, uv, textures = texture_scene(kind)
+        out, secs = [], 0.0
+        for _ in range(runs):
+            img, t = O.ref_render(tris, mat, mats, lights, cam, size, size, max_bounces=bounces, iterations=iterations,
+                                  uv=uv, textures=textures)
+            out.append(img)
+            secs += t
+        runs_arr = np.stack(out)
+        np.savez_compressed(OUT / f"render_{kind}.npz", runs=runs_arr, iterations=np.int64(iterations),
+                            size=np.int64(size), bounces=np.int64(bounces), seconds=np.float64(secs))
+        print(kind, "reference seconds", secs, "mean", runs_arr[..., :3].mean())
+
+
 SCENE_FILE_DIR = OUT / "scene_file"
 
 SCENE_FILE_MATERIALS = """{
@@ -164,17 +272,22 @@ SCENE_FILE_MAIN = """{
 """
 
 
-def _obj_text(objects):
+def _obj_text(objects, uvs=None):
     """OBJ text with one `g` group per (name, triangles); x is written negated because the reader
-    mirrors it back."""
+    mirrors it back.  ``uvs``: optional per-object corner texture coordinates [n, 3, 2] (`vt` lines)."""
     lines, base = [], 1
-    for name, tris in objects:
+    for k, (name, tris) in enumerate(objects):
         lines.append(f"g {name}")
         for t in tris:
             for v in t:
                 lines.append(f"v {-float(v[0]):.9g} {float(v[1]):.9g} {float(v[2]):.9g}")
+        if uvs is not None:
+            for t in uvs[k]:
+                for c in t:
+                    lines.append(f"vt {float(c[0]):.9g} {float(c[1]):.9g}")
         for i in range(len(tris)):
-            lines.append(f"f {base + 3 * i} {base + 3 * i + 1} {base + 3 * i + 2}")
+            a, b, c = base + 3 * i, base + 3 * i + 1, base + 3 * i + 2
+            lines.append(f"f {a}/{a} {b}/{b} {c}/{c}" if uvs is not None else f"f {a} {b} {c}")
         base += 3 * len(tris)
     return "\n".join(lines) + "\n"
 
@@ -187,6 +300,54 @@ def write_scene_file(directory=SCENE_FILE_DIR):
     (directory / "props.obj").write_text(_obj_text(objects))
     (directory / "materials.dumb").write_text(SCENE_FILE_MATERIALS)
     (directory / "scene.dumb").write_text(SCENE_FILE_MAIN)
+    return directory / "scene.dumb"
+
+
+SCENE_FILE_TEX_DIR = OUT / "scene_file_tex"
+
+SCENE_FILE_TEX_MAIN = """{
+	"materials": [
+		{ "name": "walls", "type": "dumb_based", "preset": "matte",
+		  "diffuse": [ 0.8, 0.8, 0.8 ], "diffuse_texture": { "png": "checker.png", "name": "checker" }, "diffuse_tiling": [ 3, 3 ] },
+		{ "name": "gold", "type": "dumb_based", "preset": "gold", "specular": 24,
+		  "fresnel_texture": { "png": "noise.png", "filtering": "none" },
+		  "normal_texture": { "png": "bumps.png", "name": "bumps" }, "normal_color": [ 1, 0.8, 0.9 ], "normal_tiling": [ 2, 2 ] },
+		{ "name": "painted", "type": "dumb_based", "preset": "glossy", "diffuse": [ 0.9, 0.5, 0.3 ],
+		  "diffuse_texture": "checker", "diffuse_offset": [ 0.25, -0.1 ] },
+		{ "name": "screen", "type": "dumb_based", "diffuse": [ 0.9, 0.4, 0.2 ], "metal": 0,
+		  "alpha_cutout_texture": { "png": "stripes.png", "filtering": "none" }, "alpha_cutout_threshold": 0.4 },
+		{ "name": "tinted", "type": "fresnel_color", "engine_color": "copper", "texture": "noise.png", "tiling": [ 4, 2 ] }
+	],
+	"lights": [ { "type": "simple_spherical", "color": [ 1.5, 1.5, 1.5 ], "position": [ 0, 0.8, 0 ], "radius": 0.1 } ],
+	"objects": [
+		{ "mesh": { "obj": "textured.obj", "object": "room" }, "material": "walls" },
+		{ "mesh": { "obj": "textured.obj", "object": "sphere" }, "material": "gold", "transform": { "position": [ 0.2, -0.4, 0.3 ], "scale": [ 0.7, 0.7, 0.7 ] } },
+		{ "mesh": { "obj": "textured.obj", "object": "sphere" }, "material": "tinted", "transform": { "position": [ -0.5, 0.3, 0.4 ], "scale": [ 0.35, 0.35, 0.35 ] } },
+		{ "mesh": { "obj": "textured.obj", "object": "cube" }, "material": "painted", "transform": { "position": [ -0.5, -0.8, 0.2 ], "rotation": [ 0, 30, 0 ], "scale": [ 0.35, 0.35, 0.35 ] } },
+		{ "mesh": { "obj": "textured.obj", "object": "screen" }, "material": "screen" }
+	],
+	"camera": { "lense": { "type": "simple_stochastic", "angle": 60 }, "transform": { "position": [ 0, 0, -0.95 ] } },
+	"renderer": { "pixel": { "bounces": 2 } }
+}
+"""
+
+
+def write_scene_file_textured(directory=SCENE_FILE_TEX_DIR):
+    """The textured scene file: textures from _texture written as PNG, an OBJ with texture coordinates."""
+    directory = Path(directory)
+    directory.mkdir(parents=True, exist_ok=True)
+    room = scenes.box((2.0, 2.0, 2.0), inward=True)
+    sph = scenes.icosphere(2, 0.5)
+    cube = scenes.box((1.0, 1.0, 1.0))
+    screen = scenes.quad((0.0, 0.0, -0.6), (1.2, 1.2), (0.0, 0.0, -1.0), up=(0.0, 1.0, 0.0))
+    screen_uv = np.array([[[x * 0.5 + 0.5, y * 0.5 + 0.5] for x, y, _ in t] for t in screen / 0.6], np.float32)
+    objects = [("room", room), ("sphere", sph), ("cube", cube), ("screen", screen)]
+    uvs = [_room_uv(room), _sphere_uv(sph), _room_uv(cube * 2.0), screen_uv]
+    (directory / "textured.obj").write_text(_obj_text(objects, uvs))
+    for name, kind, size, seed in (("checker", "checker", (16, 16), 1), ("noise", "noise", (8, 8), 2),
+                                   ("bumps", "bumps", (32, 32), 3), ("stripes", "stripes", (12, 12), 4)):
+        dr.write_png(_texture(kind, size, seed), directory / f"{name}.png")
+    (directory / "scene.dumb").write_text(SCENE_FILE_TEX_MAIN)
     return directory / "scene.dumb"
 
 
@@ -203,6 +364,19 @@ def scene_file_fixtures(iterations=512, runs=4, width=32, height=24):
     print("scene file: reference seconds", secs, "mean", runs_arr[..., :3].mean())
 
 
+def scene_file_tex_fixtures(iterations=512, runs=4, width=32, height=32):
+    path = write_scene_file_textured()
+    out, secs = [], 0.0
+    for _ in range(runs):
+        img, t = O.ref_dumb_render(path, width, height, iterations)
+        out.append(img)
+        secs += t
+    runs_arr = np.stack(out)
+    np.savez_compressed(OUT / "render_scene_file_tex.npz", runs=runs_arr, iterations=np.int64(iterations),
+                        width=np.int64(width), height=np.int64(height), seconds=np.float64(secs))
+    print("textured scene file: reference seconds", secs, "mean", runs_arr[..., :3].mean())
+
+
 if __name__ == "__main__":
     if not O.reference_available():
         raise SystemExit("build the reference first: bash oracle/build_ref.sh")
@@ -211,9 +385,15 @@ if __name__ == "__main__":
         cast_fixtures()
     if not only or "render" in only:
         render_fixtures()
+    if not only or "textures" in only:
+        texture_fixtures()
     for k in only:
-        if k.startswith("render_"):
+        if k.startswith("render_tex_"):
+            texture_fixtures(kinds=(k[len("render_"):],))
+        elif k.startswith("render_"):
             render_fixtures(kinds=(k[len("render_"):],))
     if not only or "scene_file" in only:
         scene_file_fixtures()
+    if not only or "scene_file_tex" in only:
+        scene_file_tex_fixtures()
     print("golden fixtures written to", OUT)

@@ -65,3 +65,23 @@ def sys_path_golden():
     p = str(GOLD)
     if p not in sys.path:
         sys.path.insert(0, p)
+
+
+@pytest.mark.parametrize("kind", ["tex_diffuse", "tex_normal", "tex_alpha", "tex_fresnel"])
+def test_oracle_textured_render_matches_reference_statistically(kind):
+    """Textured scenes (ColoredTexture channels with tiling / offset, nearest and bilinear texture
+    filtering, a normal map, an alpha cutout, a textured Fresnel shader): 4 oracle runs vs the 4
+    reference runs of the golden fixture."""
+    sys_path_golden()
+    from make_golden import texture_scene
+    from _stats import compare_runs
+    g = np.load(GOLD / f"render_{kind}.npz")
+    size, bounces = int(g["size"]), int(g["bounces"])
+    tris, mat, mats, lights, cam, uv, textures = texture_scene(kind)
+    osc = O.OracleScene(tris, mat_id=mat, materials=mats, lights=lights)
+    osc.set_textures(textures, uv)
+    runs = []
+    for seed in (1, 2, 3, 4):
+        p = dr.render_params(size, size, dr.MODE_REFERENCE, samples=(16, 16), max_bounces=bounces, seed=seed)
+        runs.append(dr.blockmajor_to_image(osc.render_blocks(cam, p), size, size))
+    compare_runs(runs, g["runs"])

@@ -16,7 +16,7 @@ import _oracle as O
 
 GOLD = Path(__file__).resolve().parent / "golden"
 sys.path.insert(0, str(GOLD))
-from make_golden import _obj_text, write_scene_file  # noqa: E402
+from make_golden import _obj_text, write_scene_file, write_scene_file_textured  # noqa: E402
 
 from dumbray_gb300 import scenes  # noqa: E402
 
@@ -36,11 +36,6 @@ def _same(a, b):
 def _assert_matches_reference(path):
     ref = O.ref_scene_file_dump(path)
     ours = O.scene_file_dump(dr.load_scene_file(path))
-    # DumbBasedShader's alpha-cutout threshold only acts through an alpha-cutout texture, which the
-    # loader rejects (texture ids are compared: all -1)
-    dumb = ref["materials"][:, 0] == 0
-    assert (ref["materials"][dumb][:, 10:14] == -1).all()
-    ref["materials"][dumb, 9] = ours["materials"][dumb, 9]
     # A perspective / stochastic lens keeps x = 0.5 / tan(angle / 2).  The reference build folds that
     # at compile time for a default-constructed lens (correctly rounded tan) and evaluates tanf at run
     # time for a lens built from a value, 2 ulp apart at 60 degrees; the renderer evaluates it at run
@@ -49,8 +44,11 @@ def _assert_matches_reference(path):
         a, b = ref["camera"][1:2].view(np.int32), ours["camera"][1:2].view(np.int32)
         assert abs(int(a[0]) - int(b[0])) <= 2
         ref["camera"][1] = ours["camera"][1]
-    for k in ("xyz", "nrm", "mat", "materials", "lights", "camera"):
+    for k in ("xyz", "nrm", "mat", "materials", "lights", "camera", "uv"):
         assert _same(ref[k], ours[k]), k
+    assert len(ref["textures"]) == len(ours["textures"])
+    for (ri, rf), (oi, of) in zip(ref["textures"], ours["textures"]):
+        assert rf == of and _same(ri, oi)
     sel = [0, 1, 2, 3, 5]  # pixels_per_gpu_thread (4) is a scheduling hint with no counterpart
     assert np.array_equal(ref["settings"][sel], ours["settings"][sel])
 
@@ -215,6 +213,10 @@ ERRORS = [
     ('{ "renderer": { "resources": { "cpu": "most" } } }', "cpu"),
     ('{ "materials": [], "materials": [] }', "duplicate"),
     ('{ "materials": [ 1, ] }', ""),
+    ('{ "materials": [ { "type": "dumb_based", "diffuse_texture": { "png": "t.png" } } ] }', "could not read"),
+    ('{ "materials": [ { "type": "dumb_based", "fresnel_texture": "named" } ] }', "not found"),
+    ('{ "materials": [ { "type": "dumb_based", "diffuse_texture": { "name": "x" } } ] }', "incomplete"),
+    ('{ "materials": [ { "type": "dumb_based", "diffuse_texture": [ 1 ] } ] }', "texture"),
     ('{ "a": tru }', "categor"),
 ]
 
@@ -231,10 +233,6 @@ def test_errors(tmp_path, text, needle):
 
 
 @pytest.mark.parametrize("text,needle", [
-    # what this renderer has no counterpart for
-    ('{ "materials": [ { "type": "dumb_based", "diffuse_texture": { "png": "t.png" } } ] }', "textures"),
-    ('{ "materials": [ { "type": "fresnel_color", "texture": { "png": "t.png" } } ] }', "textures"),
-    ('{ "materials": [ { "type": "dumb_based", "fresnel_texture": "named" } ] }', "textures"),
     # the reference leaves primitives unimplemented (and dereferences a missing mesh afterwards)
     ('{ "objects": [ { "mesh": { "primitive": "sphere" }, "material": { "type": "dumb_based" } } ] }', "primitive"),
     # the reference recurses without end on a self-include and crashes on a non-string include
@@ -318,3 +316,34 @@ def test_whole_file_item_matches_reference_as_a_set(tmp_path):
         return a[np.lexsort(a.T[::-1])]
 
     assert np.array_equal(rows(ref), rows(ours))
+
+
+@need_ref
+def test_textured_fixture_matches_reference_loader():
+    """PNG textures by path and by name (and a path looked up as a name), nearest / bilinear
+    filtering, tilings, offsets, a normal map, an alpha cutout, a textured fresnel_color; texture
+    coordinates from the OBJ: material texture channels, texture coordinates and decoded texels
+    equal the reference loader's (lodepng, bytes / 255)."""
+    _assert_matches_reference(GOLD / "scene_file_tex" / "scene.dumb")
+
+
+@need_ref
+def test_oracle_renders_textured_scene_file_like_reference():
+    from _stats import compare_runs
+    g = np.load(GOLD / "render_scene_file_tex.npz")
+    W, H = int(g["width"]), int(g["height"])
+    f = dr.load_scene_file(GOLD / "scene_file_tex" / "scene.dumb")
+    osc = O.OracleScene(f.tris, normals=f.normals, mat_id=f.mat_id, materials=f.materials, lights=f.lights)
+    osc.set_textures(f.textures, f.uv)
+    runs = []
+    for seed in range(4):
+        p = f.render_params(W, H, seed=seed)
+        p.samples_x, p.samples_y = 16, 32
+        runs.append(dr.blockmajor_to_image(osc.render_blocks(f.camera, p), W, H))
+    compare_runs(runs, g["runs"])
+
+
+def test_textured_fixture_files_are_current(tmp_path):
+    path = write_scene_file_textured(tmp_path)
+    for name in ("scene.dumb", "textured.obj", "checker.png", "noise.png", "bumps.png", "stripes.png"):
+        assert (path.parent / name).read_bytes() == (GOLD / "scene_file_tex" / name).read_bytes(), name

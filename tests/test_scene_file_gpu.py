@@ -95,3 +95,34 @@ def test_create_scene_through_the_c_abi(cuda):
             L.dr_scene_destroy(s)
     finally:
         L.dr_scene_file_destroy(h)
+
+
+TEX_SCENE = GOLD / "scene_file_tex" / "scene.dumb"
+
+
+def test_textured_scene_file_matches_oracle(cuda):
+    f = dr.load_scene_file(TEX_SCENE)
+    assert len(f.textures) == 4
+    sc = f.scene()
+    osc = O.OracleScene(f.tris, normals=f.normals, mat_id=f.mat_id, materials=f.materials, lights=f.lights)
+    osc.set_textures(f.textures, f.uv)
+    p = f.render_params(40, 40, seed=4)
+    p.samples_x, p.samples_y = 2, 2
+    g = _render(sc, f.camera, p, cuda)[..., :3].astype(np.float64)
+    o = dr.blockmajor_to_image(osc.render_blocks(f.camera, p), 40, 40)[..., :3].astype(np.float64)
+    bad = np.abs(g - o) > 2e-3 * np.maximum(np.abs(o), 0.01)
+    assert bad.mean() <= 0.02, f"{bad.mean():.4f} of channels differ"
+    assert abs(g.mean() - o.mean()) <= 5e-3 * max(abs(o.mean()), 1e-6)
+
+
+def test_textured_scene_file_matches_reference_renderer_statistically(cuda):
+    g = np.load(GOLD / "render_scene_file_tex.npz")
+    W, H = int(g["width"]), int(g["height"])
+    f = dr.load_scene_file(TEX_SCENE)
+    sc = f.scene()
+    runs = []
+    for seed in range(400, 408):
+        p = f.render_params(W, H, seed=seed)
+        p.samples_x, p.samples_y = 32, 32
+        runs.append(_render(sc, f.camera, p, cuda))
+    compare_runs(runs, g["runs"])
