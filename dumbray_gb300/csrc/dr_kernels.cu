@@ -481,6 +481,10 @@ __device__ __forceinline__ bool photon_arrives(const Hit &h, int target, f3 hp) 
     return h.tri == target || xdot(dd, dd) <= (8.0f * kEps);
 }
 
+// The blocker's transparency colour of a photon cast: shading called out of line, so that its
+// registers do not weigh on the traversal it is reached from.
+__device__ __noinline__ c3 blocker_reflect(const Scene &S, int tri, f3 p, f3 ld) { return ref_reflect(S, tri, p, ld, ld, true, 0); }
+
 __device__ __forceinline__ int *photon_list(const WaveArgs &A, int b, int pass) {
     return (pass & 1) ? reinterpret_cast<int *>(A.hits) : reinterpret_cast<int *>(A.q[b & 1].p3);
 }
@@ -518,7 +522,7 @@ struct RefPhotonSource {
         }
         const Scene &S = job_of<MULTI>(*A, __float_as_int(s4.w)).S;
         const f3 ld = f3of(s1);
-        const c3 tr = cmul(ref_reflect(S, h.tri, h.p, ld, ld, true, 0), lc);
+        const c3 tr = cmul(blocker_reflect(S, h.tri, h.p, ld), lc);
         if ((tr.r + tr.g + tr.b) > kEps) {
             const f3 lo = add3(h.p, mul3(norm3(ld), 64.0f * kEps));
             sq.s0[r] = make_float4(lo.x, lo.y, lo.z, s0.w);
@@ -529,8 +533,14 @@ struct RefPhotonSource {
     }
 };
 
+// Reference photon casts: the transparency rule puts shading on the cast path, so this kernel gets
+// its own register budget (kShadowRefBlocksPerSM blocks of kTraceThreads per SM).  At 3 blocks (80
+// registers) it spills about 200 bytes; at 2 (up to 128 registers) none.  Reference-mode twin of the
+// path trace (Mpaths/s, two runs each): 3 blocks 50.5 / 51.0, 2 blocks 56.5 / 56.3.
+constexpr int kShadowRefBlocksPerSM = 2;
+
 template <bool COUNT, bool MULTI>
-__global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_shadow_ref(WaveArgs A, int b, int pass) {
+__global__ void __launch_bounds__(kTraceThreads, kShadowRefBlocksPerSM) k_shadow_ref(WaveArgs A, int b, int pass) {
     Ctrl *C = A.ctrl;
     const int n = pass == 0 ? *((volatile int *)&C->shadow_count[b]) : *((volatile int *)&C->photon_count[b][pass]);
     if (n == 0) return;
