@@ -85,6 +85,7 @@ class JParser {
   private:
     const std::string &s_;
     size_t i_ = 0;
+    int depth_ = 0;  // container nesting; bounded so hostile text cannot exhaust the stack
 
     static bool ws(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\v' || c == '\f'; }
     static bool structural(char c) { return c == '{' || c == '}' || c == '[' || c == ']' || c == ',' || c == ':' || c == '"'; }
@@ -102,8 +103,12 @@ class JParser {
         skip_ws();
         if (i_ >= s_.size()) fail("unexpected end of text");
         char c = s_[i_];
-        if (c == '{') return dict();
-        if (c == '[') return array();
+        if (c == '{' || c == '[') {
+            if (++depth_ > 512) fail("containers nested too deeply");
+            JValue v = (c == '{') ? dict() : array();
+            depth_--;
+            return v;
+        }
         if (c == '"') {
             JValue v;
             v.kind = JValue::STR;

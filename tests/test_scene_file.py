@@ -235,6 +235,8 @@ def test_errors(tmp_path, text, needle):
 @pytest.mark.parametrize("text,needle", [
     # the reference leaves primitives unimplemented (and dereferences a missing mesh afterwards)
     ('{ "objects": [ { "mesh": { "primitive": "sphere" }, "material": { "type": "dumb_based" } } ] }', "primitive"),
+    # containers nested deeper than 512 (the reference's recursive parser has no bound)
+    ('{ "a": ' + '[' * 600 + ']' * 600 + ' }', "nested"),
     # the reference recurses without end on a self-include and crashes on a non-string include
     ('{ "include": [ "s.dumb" ] }', "nested"),
     ('{ "include": [ 3 ] }', "string"),
