@@ -31,19 +31,22 @@ inline uint8_t channel_byte(float c) {
     return (uint8_t)v;
 }
 
-// CRC-32 (ISO 3309 / PNG, reflected polynomial 0xEDB88320), table built on first use.
-uint32_t crc32_update(uint32_t crc, const uint8_t *p, size_t n) {
-    static uint32_t table[256];
-    static bool ready = false;
-    if (!ready) {
+// CRC-32 (ISO 3309 / PNG, reflected polynomial 0xEDB88320), table built once on first use (a
+// function-local static: initialised once even when several threads write images).
+struct CrcTable {
+    uint32_t t[256];
+    CrcTable() {
         for (uint32_t i = 0; i < 256; i++) {
             uint32_t c = i;
             for (int k = 0; k < 8; k++) c = (c & 1u) ? (0xEDB88320u ^ (c >> 1)) : (c >> 1);
-            table[i] = c;
+            t[i] = c;
         }
-        ready = true;
     }
-    for (size_t i = 0; i < n; i++) crc = table[(crc ^ p[i]) & 0xFFu] ^ (crc >> 8);
+};
+
+uint32_t crc32_update(uint32_t crc, const uint8_t *p, size_t n) {
+    static const CrcTable table;
+    for (size_t i = 0; i < n; i++) crc = table.t[(crc ^ p[i]) & 0xFFu] ^ (crc >> 8);
     return crc;
 }
 

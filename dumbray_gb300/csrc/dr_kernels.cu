@@ -17,6 +17,7 @@
 // sequence with no host synchronisation (and can be captured in a CUDA graph).  Every path record
 // carries the index of its render job, so the paths of many scenes can share a wave (batches).
 #include <algorithm>
+#include <atomic>
 #include "dr_kernels.h"
 #include "dr_shading.cuh"
 #include "dr_trace.cuh"
@@ -917,15 +918,20 @@ namespace drk {
 
 using namespace drd;
 
-static int g_sms = 0;
+// SM count of the current device, cached per device (renderers on several threads and GPUs launch
+// concurrently).
 static int sm_count() {
-    if (g_sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms <= 0) g_sms = 148;
+    constexpr int kDevs = 64;
+    static std::atomic<int> cache[kDevs] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int v = (dev >= 0 && dev < kDevs) ? cache[dev].load(std::memory_order_relaxed) : 0;
+    if (v == 0) {
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        if (v <= 0) v = 148;
+        if (dev >= 0 && dev < kDevs) cache[dev].store(v, std::memory_order_relaxed);
     }
-    return g_sms;
+    return v;
 }
 
 cudaError_t launch_cast(const Scene &S, const float *o, const float *d, const int *ignore, int n, int clip, int *hit_tri,

@@ -272,7 +272,8 @@ typedef struct {
 /* Sets the scene's textures (copied to the device; replaces earlier ones) and per-corner texture
  * coordinates uv: host float[n][3][2] (BakedTriFace::tex x / y), or NULL for all zeros.  Every
  * material texture index must be <= n_textures; renders of a scene whose materials use textures
- * fail until they are set.  Batches created before a later call keep the earlier textures. */
+ * fail until they are set.  Batches created before a later call keep the earlier textures, so their
+ * device memory is released with the scene (dr_scene_destroy), not by the next call. */
 dr_status dr_scene_set_textures(dr_scene *scene, const dr_texture *textures, int32_t n_textures, const float *uv);
 
 /* Device pointers to the scene's per-triangle albedo and emission (float[n][3] each), for
