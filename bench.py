@@ -489,7 +489,8 @@ def run_raycast(dr, torch, dev, a, peak, peak_src):
     from dumbray_gb300 import scenes
 
     mesh = scenes.displaced_icosphere(a.level, 0.1, 1)
-    out = {"workload": f"displaced icosphere L{a.level} alone ({len(mesh):,} tris), closest hit, backface culling; "
+    out = {"workload": f"displaced icosphere L{a.level} alone ({len(mesh):,} tris), closest hit, backface culling "
+                       "(the renderer default; *_no_cull: the same rays without); "
                        "reference_tree = the reference's octree (casts bit-exact to Octree::cast), physical_tree = "
                        "padding 2^-18 x max |coordinate| (same closest hits up to float32 near-ties)",
            "counts": "c_box / c_tri from dr_cast_counted: on the reference tree the reference's own traversal (it "
@@ -524,7 +525,21 @@ def run_raycast(dr, torch, dev, a, peak, peak_src):
                                       "frac": round(achieved / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
                                       "kernel": "k_cast"}}
             hits[tree][name] = tri.cpu().numpy()
-            del ot, dt
+            # the same rays with backface culling off (dr_cast clip_backfaces = 0)
+            for _ in range(2):
+                dr.cast(sc, ot, dt, cull_backfaces=False)
+            ms0 = _events_ms(torch, lambda i: dr.cast(sc, ot, dt, cull_backfaces=False), K) / K
+            tri0, _, nb0, nt0 = dr.cast(sc, ot, dt, cull_backfaces=False, counted=True)
+            c_box0, c_tri0 = float(nb0.double().mean()), float(nt0.double().mean())
+            bpr0 = 40.0 + 32.0 * c_box0 + 36.0 * c_tri0
+            achieved0 = n * bpr0 / (ms0 / 1e3) / 1e9
+            res[name + "_no_cull"] = {"rays": n, "ms": round(ms0, 3), "mrays_s": round(n / (ms0 / 1e3) / 1e6, 1),
+                                      "hit_fraction": round(float((tri0 >= 0).float().mean()), 4),
+                                      "c_box": round(c_box0, 2), "c_tri": round(c_tri0, 2), "bytes_per_ray": round(bpr0, 1),
+                                      "roofline": {"bound": "hbm", "achieved": round(achieved0, 1), "peak": peak,
+                                                   "unit": "GB/s", "frac": round(achieved0 / peak, 4),
+                                                   "peak_source": f"{peak_src} hbm_gbs", "kernel": "k_cast"}}
+            del ot, dt, tri0, nb0, nt0
         out[tree] = res
         sc.close()
     out["physical_vs_reference_tree_hit_mismatch"] = {
