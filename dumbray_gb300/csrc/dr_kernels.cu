@@ -84,6 +84,7 @@ __device__ __forceinline__ void accum_add(float *acc, int slot, c3 c) {
 // ---------------------------------------------------------------------------------------------
 // dr_cast: warp w of the grid owns rays [w * kChunk, (w + 1) * kChunk) of one scene.
 struct BatchSource {
+    static constexpr float kOccludeBelow = 0.0f;
     const float *o, *d;
     const int *ignore;
     int *hit_tri, *nbox, *ntri;
@@ -315,6 +316,7 @@ __global__ void __launch_bounds__(256) k_camera(WaveArgs A) {
 
 template <bool MULTI>
 struct TraceSource {
+    static constexpr float kOccludeBelow = 0.0f;
     const WaveArgs *A;
     Queue Q;
     float2 *hits;
@@ -492,6 +494,7 @@ __device__ __forceinline__ int *photon_list(const WaveArgs &A, int b, int pass) 
 
 template <bool MULTI>
 struct RefPhotonSource {
+    static constexpr float kOccludeBelow = 0.0f;
     const WaveArgs *A;
     ShadowQ sq;
     int *fetch, *out_count, *out_list;
@@ -803,6 +806,8 @@ __global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
 
 template <bool MULTI, bool ADJ>
 struct ShadowPhysSource {
+    // visible unless something but the light triangle is hit before t = 0.999 (store below)
+    static constexpr float kOccludeBelow = 0.999f;
     const WaveArgs *A;
     ShadowQ sq;
     float *accum;

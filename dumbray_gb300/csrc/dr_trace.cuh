@@ -80,6 +80,8 @@ struct WarpLeafSlots {
 //   const Scene &scene(int job)               the scene of a job (MULTI only)
 //   bool clip(int job)                        backface culling of a job (MULTI = false: job 0 for all)
 //   void store(int i, const Hit &h, int nbox, int ntri)
+//   static constexpr float kOccludeBelow      > 0: visibility-only rays (any hit nearer than this
+//                                             settles them); 0: closest hit
 // MULTI = false: every ray belongs to scene `S`.  MULTI = true: rays of different scenes share the
 // warp; their trees live in one batch arena (S.nodes / S.leaf_tris are the arena's), so a lane only
 // takes its scene's root (bounds, child group or root leaf) when it starts a ray.  Backface culling
@@ -245,8 +247,11 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
             __syncwarp();
         }
         if (mode == kLeaf && L.r >= L.r_end) {
-            if (L.best != FLT_MAX && L.bp.x >= L.lx && L.bp.y >= L.ly && L.bp.z >= L.lz && L.bp.x <= L.hx && L.bp.y <= L.hy &&
-                L.bp.z <= L.hz) {
+            // occlusion sources end a ray at the first leaf holding a hit nearer than their limit, even
+            // one whose point lies in a later leaf: that hit's own leaf would end the ray there anyway
+            const bool occluded = Source::kOccludeBelow > 0.0f && L.best < Source::kOccludeBelow;
+            if (L.best != FLT_MAX && (occluded || (L.bp.x >= L.lx && L.bp.y >= L.ly && L.bp.z >= L.lz && L.bp.x <= L.hx &&
+                                                   L.bp.y <= L.hy && L.bp.z <= L.hz))) {
                 if (COUNT) {
                     L.nb -= 7 - L.kleaf;
                     for (int s = 0; s < L.sp; s++) L.nb -= 7 - (int)((stack[s] >> 8) & 7u);
