@@ -73,3 +73,15 @@ def test_block_major_layout_matches_reference_formula():
             if x < W and y < H:
                 assert np.array_equal(fb[block * 128 + pid], img[y, x])
     assert np.array_equal(dr.blockmajor_to_image(fb, W, H), img)
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """No CPU fallback: without the built library every entry into the API raises."""
+    monkeypatch.setattr(dr, "_lib", None)
+    monkeypatch.setattr(dr, "LIB_PATH", tmp_path / "libdumbray_gb300.so")
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        dr.lib()
+    with pytest.raises(RuntimeError, match="missing"):
+        dr.Scene(np.zeros((1, 3, 3), np.float32), materials=[dr.lambert()])
+    with pytest.raises(RuntimeError, match="missing"):
+        dr.Renderer()
