@@ -55,7 +55,8 @@ def parse():
     ap.add_argument("--lens", default="pinhole", choices=["pinhole", "fisheye", "spherical"])
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--wave", type=int, default=1 << 22)
+    ap.add_argument("--wave", type=int, default=1 << 24,
+                    help="paths per wave (renderer capacity); 16Mi: about 5 GB of scratch per lane")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer e2e pass (profiling cases)")
     ap.add_argument("--no-count", action="store_true", help="skip the traversal-counting pass (profiling cases)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched leg")

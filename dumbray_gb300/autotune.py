@@ -69,7 +69,7 @@ def tune_leaf_threshold(make_scene, scenes_by_class, camera_for, probe=(512, 512
     return best, table
 
 
-def tune_wave(batch, candidates=(1 << 20, 1 << 21, 1 << 22, 1 << 23), use_graph=True, lanes=0):
+def tune_wave(batch, candidates=(1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24), use_graph=True, lanes=0):
     """Times one batch render per candidate wave size; returns (best, {wave: ms}, renderer of the best).
     Candidates above the batch's path count are skipped (a wave never exceeds the batch).  ``lanes``:
     concurrent wave pipelines of the renderers (0 = library default)."""
