@@ -310,7 +310,9 @@ dr_status dr_cast_counted(const dr_scene *scene, const float *origin, const floa
 
 /* ---- block renderer ------------------------------------------------------------------------
  * A renderer owns the wavefront scratch (ray / hit / shadow queues, per-pixel accumulators) for
- * at most `wave_paths` paths in flight (0 = default 4M). */
+ * at most `wave_paths` paths in flight (0 = default 4Mi, about 1.2 GB of scratch per lane).  Large
+ * renders run faster with larger waves (fewer per-wave launch sequences): a 1920x1080 x 64 spp
+ * physical-mode frame renders about 4.5% faster with 16Mi (about 5 GB per lane). */
 dr_status dr_renderer_create(int32_t wave_paths, dr_renderer **out);
 void dr_renderer_destroy(dr_renderer *r);
 
