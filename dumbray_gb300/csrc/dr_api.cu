@@ -11,11 +11,14 @@
 #include <thread>
 #include <atomic>
 #include <vector>
+#include <new>
+#include <exception>
 
 #include "../../include/dr_api.h"
 #include "dr_kernels.h"
 #include "octree_build.h"
 #include "dr_internal.h"
+#include "dr_guard.h"
 
 namespace {
 
@@ -285,7 +288,7 @@ static void spotlight_state(const dr_light &l, drd::Light &d) {
 }
 
 dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat_id, int32_t n, const dr_material *mats,
-                          int32_t n_mats, const dr_light *lights, int32_t n_lights, const dr_build_params *bp, dr_scene **out) {
+                          int32_t n_mats, const dr_light *lights, int32_t n_lights, const dr_build_params *bp, dr_scene **out) try {
     if (out == nullptr) return fail(DR_E_ARG, "dr_scene_create: out is NULL");
     *out = nullptr;
     if (n < 0 || (n > 0 && xyz == nullptr)) return fail(DR_E_ARG, "dr_scene_create: bad triangle array");
@@ -464,18 +467,22 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
     if (st != DR_OK) { delete sc; return st; }
     *out = sc;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_create");
 }
 
-dr_status dr_scene_set_triangle_params(dr_scene *sc, const float *albedo, const float *emission, const float *roughness) {
+dr_status dr_scene_set_triangle_params(dr_scene *sc, const float *albedo, const float *emission, const float *roughness) try {
     if (!sc) return fail(DR_E_ARG, "dr_scene_set_triangle_params: scene is NULL");
     size_t n = (size_t)sc->n;
     if (albedo) std::copy(albedo, albedo + 3 * n, sc->albedo.begin());
     if (emission) std::copy(emission, emission + 3 * n, sc->emission.begin());
     if (roughness) std::copy(roughness, roughness + n, sc->roughness.begin());
     return upload_shading(sc);
+} catch (...) {
+    return dr_internal_exception("dr_scene_set_triangle_params");
 }
 
-dr_status dr_scene_set_textures(dr_scene *sc, const dr_texture *tex, int32_t n, const float *uv) {
+dr_status dr_scene_set_textures(dr_scene *sc, const dr_texture *tex, int32_t n, const float *uv) try {
     if (!sc || n < 0 || (n > 0 && !tex)) return fail(DR_E_ARG, "dr_scene_set_textures: bad arguments");
     if (sc->max_texture > n) return fail(DR_E_ARG, "dr_scene_set_textures: a material uses texture " +
                                                        std::to_string(sc->max_texture) + " of " + std::to_string(n));
@@ -519,13 +526,17 @@ dr_status dr_scene_set_textures(dr_scene *sc, const dr_texture *tex, int32_t n, 
     sc->dev.tex_info = d_info;
     sc->dev.uv = d_uv;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_set_textures");
 }
 
-dr_status dr_scene_triangle_params_device(dr_scene *sc, float **albedo, float **emission) {
+dr_status dr_scene_triangle_params_device(dr_scene *sc, float **albedo, float **emission) try {
     if (!sc) return fail(DR_E_ARG, "dr_scene_triangle_params_device: scene is NULL");
     if (albedo) *albedo = sc->albedo_dev;
     if (emission) *emission = sc->emission_dev;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_triangle_params_device");
 }
 
 static void tree_stats(const drb::FlatOctree &T, int64_t *nodes, int64_t *leaves, int64_t *refs, int32_t *depth) {
@@ -556,19 +567,23 @@ static void tree_export(const drb::FlatOctree &T, float *node_box, int32_t *node
     if (leaf_tri) std::copy(T.leaf_refs.begin(), T.leaf_refs.end(), leaf_tri);
 }
 
-dr_status dr_scene_stats(const dr_scene *sc, int64_t *nodes, int64_t *leaves, int64_t *refs, int32_t *depth) {
+dr_status dr_scene_stats(const dr_scene *sc, int64_t *nodes, int64_t *leaves, int64_t *refs, int32_t *depth) try {
     if (!sc) return fail(DR_E_ARG, "dr_scene_stats: scene is NULL");
     tree_stats(sc->tree, nodes, leaves, refs, depth);
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_stats");
 }
 
-dr_status dr_scene_export_tree(const dr_scene *sc, float *node_box, int32_t *node_child, int32_t *node_leaf, int32_t *leaf_tri) {
+dr_status dr_scene_export_tree(const dr_scene *sc, float *node_box, int32_t *node_child, int32_t *node_leaf, int32_t *leaf_tri) try {
     if (!sc) return fail(DR_E_ARG, "dr_scene_export_tree: scene is NULL");
     tree_export(sc->tree, node_box, node_child, node_leaf, leaf_tri);
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_export_tree");
 }
 
-dr_status dr_octree_create_host(const float *xyz, int32_t n, const dr_build_params *bp, dr_octree **out) {
+dr_status dr_octree_create_host(const float *xyz, int32_t n, const dr_build_params *bp, dr_octree **out) try {
     if (!out) return fail(DR_E_ARG, "dr_octree_create_host: out is NULL");
     *out = nullptr;
     if (n < 0 || (n > 0 && !xyz)) return fail(DR_E_ARG, "dr_octree_create_host: bad triangle array");
@@ -589,18 +604,24 @@ dr_status dr_octree_create_host(const float *xyz, int32_t n, const dr_build_para
     }
     *out = t;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_octree_create_host");
 }
 
-dr_status dr_octree_stats(const dr_octree *t, int64_t *nodes, int64_t *leaves, int64_t *refs, int32_t *depth) {
+dr_status dr_octree_stats(const dr_octree *t, int64_t *nodes, int64_t *leaves, int64_t *refs, int32_t *depth) try {
     if (!t) return fail(DR_E_ARG, "dr_octree_stats: tree is NULL");
     tree_stats(t->tree, nodes, leaves, refs, depth);
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_octree_stats");
 }
 
-dr_status dr_octree_export(const dr_octree *t, float *node_box, int32_t *node_child, int32_t *node_leaf, int32_t *leaf_tri) {
+dr_status dr_octree_export(const dr_octree *t, float *node_box, int32_t *node_child, int32_t *node_leaf, int32_t *leaf_tri) try {
     if (!t) return fail(DR_E_ARG, "dr_octree_export: tree is NULL");
     tree_export(t->tree, node_box, node_child, node_leaf, leaf_tri);
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_octree_export");
 }
 
 void dr_octree_destroy(dr_octree *t) { delete t; }
@@ -619,17 +640,21 @@ static dr_status cast_impl(const dr_scene *sc, const float *o, const float *d, c
 }
 
 dr_status dr_cast(const dr_scene *sc, const float *o, const float *d, const int32_t *ignore, int32_t n, int32_t clip,
-                  int32_t *hit_tri, float *hit_t, void *stream) {
+                  int32_t *hit_tri, float *hit_t, void *stream) try {
     return cast_impl(sc, o, d, ignore, n, clip, hit_tri, hit_t, nullptr, nullptr, stream);
+} catch (...) {
+    return dr_internal_exception("dr_cast");
 }
 
 dr_status dr_cast_counted(const dr_scene *sc, const float *o, const float *d, const int32_t *ignore, int32_t n, int32_t clip,
-                          int32_t *hit_tri, float *hit_t, int32_t *nbox, int32_t *ntri, void *stream) {
+                          int32_t *hit_tri, float *hit_t, int32_t *nbox, int32_t *ntri, void *stream) try {
     if (!nbox || !ntri) return fail(DR_E_ARG, "dr_cast_counted: NULL counter buffer");
     return cast_impl(sc, o, d, ignore, n, clip, hit_tri, hit_t, nbox, ntri, stream);
+} catch (...) {
+    return dr_internal_exception("dr_cast_counted");
 }
 
-dr_status dr_renderer_create(int32_t wave_paths, dr_renderer **out) {
+dr_status dr_renderer_create(int32_t wave_paths, dr_renderer **out) try {
     if (!out) return fail(DR_E_ARG, "dr_renderer_create: out is NULL");
     *out = nullptr;
     if (wave_paths < 0) return fail(DR_E_ARG, "dr_renderer_create: negative wave size");
@@ -655,37 +680,45 @@ dr_status dr_renderer_create(int32_t wave_paths, dr_renderer **out) {
     }
     *out = r;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_renderer_create");
 }
 
 void dr_renderer_destroy(dr_renderer *r) { delete r; }
 
 int64_t dr_renderer_launch_count(const dr_renderer *r) { return r ? r->launches : 0; }
 
-dr_status dr_renderer_set_profiling(dr_renderer *r, int32_t enable) {
+dr_status dr_renderer_set_profiling(dr_renderer *r, int32_t enable) try {
     if (!r) return fail(DR_E_ARG, "dr_renderer_set_profiling: renderer is NULL");
     r->prof.reset(enable != 0);
     r->prof.enabled = enable != 0;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_renderer_set_profiling");
 }
 
-dr_status dr_renderer_kernel_busy(dr_renderer *r, double *busy_ms) {
+dr_status dr_renderer_kernel_busy(dr_renderer *r, double *busy_ms) try {
     if (!r || !busy_ms) return fail(DR_E_ARG, "dr_renderer_kernel_busy: NULL argument");
     cudaError_t e = r->prof.harvest();
     if (e != cudaSuccess) return cuda_fail(e, "dr_renderer_kernel_busy");
     r->prof.busy(busy_ms);
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_renderer_kernel_busy");
 }
 
-dr_status dr_renderer_set_lanes(dr_renderer *r, int32_t lanes) {
+dr_status dr_renderer_set_lanes(dr_renderer *r, int32_t lanes) try {
     if (!r) return fail(DR_E_ARG, "dr_renderer_set_lanes: renderer is NULL");
     if (lanes < 1 || lanes > DR_MAX_LANES) return fail(DR_E_ARG, "dr_renderer_set_lanes: lanes must be in [1, 8]");
     r->lanes = lanes;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_renderer_set_lanes");
 }
 
 int32_t dr_renderer_lanes(const dr_renderer *r) { return r ? r->lanes : 0; }
 
-dr_status dr_renderer_kernel_times(dr_renderer *r, double *ms, int64_t *launches) {
+dr_status dr_renderer_kernel_times(dr_renderer *r, double *ms, int64_t *launches) try {
     if (!r) return fail(DR_E_ARG, "dr_renderer_kernel_times: renderer is NULL");
     cudaError_t e = r->prof.harvest();
     if (e != cudaSuccess) return cuda_fail(e, "dr_renderer_kernel_times");
@@ -694,9 +727,11 @@ dr_status dr_renderer_kernel_times(dr_renderer *r, double *ms, int64_t *launches
         if (launches) launches[k] = r->prof.launches[k];
     }
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_renderer_kernel_times");
 }
 
-dr_status dr_renderer_set_counting(dr_renderer *r, int32_t enable) {
+dr_status dr_renderer_set_counting(dr_renderer *r, int32_t enable) try {
     if (!r) return fail(DR_E_ARG, "dr_renderer_set_counting: renderer is NULL");
     if (!r->counters) {
         cudaError_t e = cudaMalloc((void **)&r->counters, 6 * sizeof(unsigned long long));
@@ -706,9 +741,11 @@ dr_status dr_renderer_set_counting(dr_renderer *r, int32_t enable) {
     if (e != cudaSuccess) return cuda_fail(e, "dr_renderer_set_counting");
     r->counting = enable != 0;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_renderer_set_counting");
 }
 
-dr_status dr_renderer_counters(dr_renderer *r, int64_t *counts) {
+dr_status dr_renderer_counters(dr_renderer *r, int64_t *counts) try {
     if (!r || !counts) return fail(DR_E_ARG, "dr_renderer_counters: NULL argument");
     unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
     if (r->counters) {
@@ -718,6 +755,8 @@ dr_status dr_renderer_counters(dr_renderer *r, int64_t *counts) {
     }
     for (int k = 0; k < 6; k++) counts[k] = (int64_t)h[k];
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_renderer_counters");
 }
 
 // Validates one render job and fills its Item (everything but the slot / path offsets).
@@ -897,7 +936,7 @@ static long long wave_size(const dr_renderer *r, int lights_per_path, long long 
 }
 
 dr_status dr_render_blocks(dr_renderer *r, const dr_scene *sc, const dr_camera *cam, float *fb, int32_t start_block,
-                           int32_t end_block, const dr_render_params *p, void *stream_ptr) {
+                           int32_t end_block, const dr_render_params *p, void *stream_ptr) try {
     if (!r) return fail(DR_E_ARG, "dr_render_blocks: NULL argument");
     drk::WaveDesc W;
     std::memset(&W, 0, sizeof(W));
@@ -918,11 +957,13 @@ dr_status dr_render_blocks(dr_renderer *r, const dr_scene *sc, const dr_camera *
     const long long total = (long long)I.n_slots * I.spp;
     const long long wave = lane_wave(total, wave_size(r, lights, 1LL << 40), r->lanes);
     return run_waves(r, W, total, wave, I.n_slots, stream, &r->prof, r->counting, true, r->lanes);
+} catch (...) {
+    return dr_internal_exception("dr_render_blocks");
 }
 
 dr_status dr_render_adjoint(dr_renderer *r, const dr_scene *sc, const dr_camera *cam, const float *dl_dfb, int32_t start_block,
                             int32_t end_block, const dr_render_params *p, float *grad_albedo, float *grad_emission,
-                            void *stream_ptr) {
+                            void *stream_ptr) try {
     if (!r || !dl_dfb || !grad_albedo || !grad_emission) return fail(DR_E_ARG, "dr_render_adjoint: NULL argument");
     drk::WaveDesc W;
     std::memset(&W, 0, sizeof(W));
@@ -956,6 +997,8 @@ dr_status dr_render_adjoint(dr_renderer *r, const dr_scene *sc, const dr_camera 
     W.adjoint = true;
     wave_buffers(r, W);
     return run_waves(r, W, (long long)I.n_slots * I.spp, wave, I.n_slots, stream, &r->prof, false, false);
+} catch (...) {
+    return dr_internal_exception("dr_render_adjoint");
 }
 
 }  // extern "C"
@@ -1057,7 +1100,7 @@ static dr_status build_arena(dr_batch *b) {
     return DR_OK;
 }
 
-dr_status dr_batch_create(const dr_batch_item *items, int32_t n, dr_batch **out) {
+dr_status dr_batch_create(const dr_batch_item *items, int32_t n, dr_batch **out) try {
     if (!out) return fail(DR_E_ARG, "dr_batch_create: out is NULL");
     *out = nullptr;
     if (!items || n <= 0) return fail(DR_E_ARG, "dr_batch_create: empty batch");
@@ -1112,9 +1155,11 @@ dr_status dr_batch_create(const dr_batch_item *items, int32_t n, dr_batch **out)
     }
     *out = b;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_batch_create");
 }
 
-dr_status dr_batch_set_iteration(dr_batch *b, int32_t iteration) {
+dr_status dr_batch_set_iteration(dr_batch *b, int32_t iteration) try {
     if (!b) return fail(DR_E_ARG, "dr_batch_set_iteration: batch is NULL");
     for (size_t i = 0; i < b->items.size(); i++) {
         drk::Item &I = b->items[i];
@@ -1126,9 +1171,11 @@ dr_status dr_batch_set_iteration(dr_batch *b, int32_t iteration) {
         e = cudaMemcpy(b->items_dev, b->items.data(), sizeof(drk::Item) * b->items.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(e, "dr_batch_set_iteration");
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_batch_set_iteration");
 }
 
-dr_status dr_batch_render(dr_renderer *r, dr_batch *b, int32_t use_graph, void *stream_ptr) {
+dr_status dr_batch_render(dr_renderer *r, dr_batch *b, int32_t use_graph, void *stream_ptr) try {
     if (!r || !b) return fail(DR_E_ARG, "dr_batch_render: NULL argument");
     if (r->counting && b->arena_node_count >= (int64_t(1) << 24))
         return fail(DR_E_CAPACITY, "dr_batch_render: traversal counting supports at most 2^24 octree nodes per batch");
@@ -1210,6 +1257,8 @@ dr_status dr_batch_render(dr_renderer *r, dr_batch *b, int32_t use_graph, void *
     cudaEventRecord(b->done, stream);
     r->launches += b->graph_launches;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_batch_render");
 }
 
 int64_t dr_batch_paths(const dr_batch *b) { return b ? b->total_paths : 0; }
@@ -1223,3 +1272,22 @@ const drd::Scene *dr_internal_scene_device(const dr_scene *scene) { return scene
 bool dr_internal_scene_textures_ok(const dr_scene *scene) { return scene && scene->max_texture <= scene->n_textures; }
 
 void dr_internal_set_error(const char *msg) { g_err = msg ? msg : ""; }
+
+dr_status dr_internal_exception(const char *where) noexcept {
+    const char *what = "unexpected exception";
+    dr_status s = DR_E_STATE;
+    try {
+        throw;
+    } catch (const std::bad_alloc &) {
+        what = "out of host memory";
+        s = DR_E_NOMEM;
+    } catch (const std::exception &e) {
+        what = e.what();
+    } catch (...) {
+    }
+    try {
+        g_err = std::string(where) + ": " + what;
+    } catch (...) {  // no memory left even for the message: keep the status
+    }
+    return s;
+}

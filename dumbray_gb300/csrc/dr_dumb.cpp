@@ -42,6 +42,7 @@
 #include <vector>
 
 #include "../../include/dr_api.h"
+#include "dr_guard.h"
 
 void dr_internal_set_error(const char *msg);
 
@@ -981,7 +982,7 @@ struct dr_scene_file {
 
 extern "C" {
 
-dr_status dr_scene_file_load(const char *path, dr_scene_file **out) {
+dr_status dr_scene_file_load(const char *path, dr_scene_file **out) try {
     if (!out) return fail(DR_E_ARG, "dr_scene_file_load: out is NULL");
     *out = nullptr;
     if (!path) return fail(DR_E_ARG, "dr_scene_file_load: path is NULL");
@@ -996,17 +997,21 @@ dr_status dr_scene_file_load(const char *path, dr_scene_file **out) {
     }
     *out = f.release();
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_file_load");
 }
 
-dr_status dr_scene_file_counts(const dr_scene_file *f, int32_t *counts) {
+dr_status dr_scene_file_counts(const dr_scene_file *f, int32_t *counts) try {
     if (!f || !counts) return fail(DR_E_ARG, "dr_scene_file_counts: NULL argument");
     counts[0] = (int32_t)f->L.units.size();
     counts[1] = (int32_t)f->L.materials.size();
     counts[2] = (int32_t)f->L.lights.size();
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_file_counts");
 }
 
-dr_status dr_scene_file_geometry(const dr_scene_file *f, float *xyz, float *nrm, int32_t *mat_id) {
+dr_status dr_scene_file_geometry(const dr_scene_file *f, float *xyz, float *nrm, int32_t *mat_id) try {
     if (!f) return fail(DR_E_ARG, "dr_scene_file_geometry: file is NULL");
     for (size_t i = 0; i < f->L.units.size(); i++) {
         const Unit &u = f->L.units[i];
@@ -1015,21 +1020,27 @@ dr_status dr_scene_file_geometry(const dr_scene_file *f, float *xyz, float *nrm,
         if (mat_id) mat_id[i] = u.mat;
     }
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_file_geometry");
 }
 
-dr_status dr_scene_file_materials(const dr_scene_file *f, dr_material *mats) {
+dr_status dr_scene_file_materials(const dr_scene_file *f, dr_material *mats) try {
     if (!f || !mats) return fail(DR_E_ARG, "dr_scene_file_materials: NULL argument");
     if (!f->L.materials.empty()) std::memcpy(mats, f->L.materials.data(), sizeof(dr_material) * f->L.materials.size());
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_file_materials");
 }
 
-dr_status dr_scene_file_lights(const dr_scene_file *f, dr_light *lights) {
+dr_status dr_scene_file_lights(const dr_scene_file *f, dr_light *lights) try {
     if (!f || !lights) return fail(DR_E_ARG, "dr_scene_file_lights: NULL argument");
     if (!f->L.lights.empty()) std::memcpy(lights, f->L.lights.data(), sizeof(dr_light) * f->L.lights.size());
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_file_lights");
 }
 
-dr_status dr_scene_file_camera(const dr_scene_file *f, dr_camera *c) {
+dr_status dr_scene_file_camera(const dr_scene_file *f, dr_camera *c) try {
     if (!f || !c) return fail(DR_E_ARG, "dr_scene_file_camera: NULL argument");
     const Loader &L = f->L;
     std::memset(c, 0, sizeof(*c));
@@ -1055,9 +1066,11 @@ dr_status dr_scene_file_camera(const dr_scene_file *f, dr_camera *c) {
     }
     c->origin_rows = 1;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_file_camera");
 }
 
-dr_status dr_scene_file_render_params(const dr_scene_file *f, dr_render_params *p) {
+dr_status dr_scene_file_render_params(const dr_scene_file *f, dr_render_params *p) try {
     if (!f || !p) return fail(DR_E_ARG, "dr_scene_file_render_params: NULL argument");
     std::memset(p, 0, sizeof(*p));
     p->mode = DR_MODE_REFERENCE;
@@ -1068,12 +1081,14 @@ dr_status dr_scene_file_render_params(const dr_scene_file *f, dr_render_params *
     p->boxing = f->L.boxing;
     p->iteration = 1;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_file_render_params");
 }
 
 int32_t dr_scene_file_textures(const dr_scene_file *f) { return f ? (int32_t)f->L.textures.size() : 0; }
 
 dr_status dr_scene_file_texture(const dr_scene_file *f, int32_t i, int32_t *width, int32_t *height, int32_t *filtering,
-                                float *rgba) {
+                                float *rgba) try {
     if (!f || i < 0 || i >= (int32_t)f->L.textures.size()) return fail(DR_E_ARG, "dr_scene_file_texture: bad texture");
     const Tex &t = f->L.textures[(size_t)i];
     if (width) *width = t.w;
@@ -1081,15 +1096,19 @@ dr_status dr_scene_file_texture(const dr_scene_file *f, int32_t i, int32_t *widt
     if (filtering) *filtering = t.filter;
     if (rgba) std::memcpy(rgba, t.rgba.data(), sizeof(float) * t.rgba.size());
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_file_texture");
 }
 
-dr_status dr_scene_file_texcoords(const dr_scene_file *f, float *uv) {
+dr_status dr_scene_file_texcoords(const dr_scene_file *f, float *uv) try {
     if (!f || !uv) return fail(DR_E_ARG, "dr_scene_file_texcoords: NULL argument");
     for (size_t i = 0; i < f->L.units.size(); i++) std::memcpy(uv + 6 * i, f->L.units[i].f.uv, sizeof(float) * 6);
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_scene_file_texcoords");
 }
 
-dr_status dr_scene_file_create_scene(const dr_scene_file *f, const dr_build_params *bp, dr_scene **out) {
+dr_status dr_scene_file_create_scene(const dr_scene_file *f, const dr_build_params *bp, dr_scene **out) try {
     if (!f || !out) return fail(DR_E_ARG, "dr_scene_file_create_scene: NULL argument");
     const Loader &L = f->L;
     const size_t n = L.units.size();
@@ -1108,6 +1127,8 @@ dr_status dr_scene_file_create_scene(const dr_scene_file *f, const dr_build_para
         *out = nullptr;
     }
     return st;
+} catch (...) {
+    return dr_internal_exception("dr_scene_file_create_scene");
 }
 
 void dr_scene_file_destroy(dr_scene_file *f) { delete f; }

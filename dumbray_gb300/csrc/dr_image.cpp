@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/dr_api.h"
+#include "dr_guard.h"
 
 void dr_internal_set_error(const char *msg);
 
@@ -104,7 +105,7 @@ bool write_file(const char *path, const void *data, size_t n) {
 
 extern "C" {
 
-dr_status dr_image_from_blocks(const float *fb, int32_t width, int32_t height, float *rgba) {
+dr_status dr_image_from_blocks(const float *fb, int32_t width, int32_t height, float *rgba) try {
     if (!fb || !rgba || width <= 0 || height <= 0) return fail(DR_E_ARG, "dr_image_from_blocks: bad argument");
     const int bw = (width + DR_BLOCK_W - 1) / DR_BLOCK_W;
     for (int y = 0; y < height; y++) {
@@ -115,16 +116,20 @@ dr_status dr_image_from_blocks(const float *fb, int32_t width, int32_t height, f
         }
     }
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_image_from_blocks");
 }
 
-dr_status dr_image_to_rgba8(const float *rgba, int32_t width, int32_t height, uint8_t *out) {
+dr_status dr_image_to_rgba8(const float *rgba, int32_t width, int32_t height, uint8_t *out) try {
     if (!rgba || !out || width <= 0 || height <= 0) return fail(DR_E_ARG, "dr_image_to_rgba8: bad argument");
     const size_t n = 4 * (size_t)width * height;
     for (size_t i = 0; i < n; i++) out[i] = channel_byte(rgba[i]);
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_image_to_rgba8");
 }
 
-dr_status dr_image_write_png(const float *rgba, int32_t width, int32_t height, const char *path) {
+dr_status dr_image_write_png(const float *rgba, int32_t width, int32_t height, const char *path) try {
     if (!rgba || !path || width <= 0 || height <= 0) return fail(DR_E_ARG, "dr_image_write_png: bad argument");
     std::vector<uint8_t> raw((size_t)height * (1 + 4 * (size_t)width));
     for (int y = 0; y < height; y++) {
@@ -142,9 +147,11 @@ dr_status dr_image_write_png(const float *rgba, int32_t width, int32_t height, c
     put_chunk(png, "IEND", {});
     if (!write_file(path, png.data(), png.size())) return fail(DR_E_ARG, std::string("dr_image_write_png: cannot write ") + path);
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_image_write_png");
 }
 
-dr_status dr_image_write_pfm(const float *rgba, int32_t width, int32_t height, const char *path) {
+dr_status dr_image_write_pfm(const float *rgba, int32_t width, int32_t height, const char *path) try {
     if (!rgba || !path || width <= 0 || height <= 0) return fail(DR_E_ARG, "dr_image_write_pfm: bad argument");
     // PFM: "PF", width height, negative scale = little-endian; RGB float rows from the bottom up.
     std::string head = "PF\n" + std::to_string(width) + " " + std::to_string(height) + "\n-1.0\n";
@@ -159,6 +166,8 @@ dr_status dr_image_write_pfm(const float *rgba, int32_t width, int32_t height, c
     // float bytes are written in host order; both the build hosts (x86-64, aarch64) are little-endian
     if (!write_file(path, out.data(), out.size())) return fail(DR_E_ARG, std::string("dr_image_write_pfm: cannot write ") + path);
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_image_write_pfm");
 }
 
 }  // extern "C"

@@ -30,6 +30,7 @@
 #include "../../include/dr_api.h"
 #include "dr_internal.h"
 #include "dr_kernels.h"
+#include "dr_guard.h"
 
 namespace {
 
@@ -84,7 +85,7 @@ cudaError_t scratch_address(unsigned char **out) {
 }  // namespace
 
 extern "C" dr_status dr_render_blocks_noalloc(const dr_scene *sc, const dr_camera *cam, float *fb, int32_t start_block,
-                                              int32_t end_block, const dr_render_params *p, void *stream_ptr) {
+                                              int32_t end_block, const dr_render_params *p, void *stream_ptr) try {
     if (!sc || !cam || !fb || !p) return nfail(DR_E_ARG, "dr_render_blocks_noalloc: NULL argument");
     if (p->mode != DR_MODE_REFERENCE && p->mode != DR_MODE_PHYSICAL) return nfail(DR_E_ARG, "dr_render_blocks_noalloc: bad mode");
     if (p->width <= 0 || p->height <= 0) return nfail(DR_E_ARG, "dr_render_blocks_noalloc: bad resolution");
@@ -187,4 +188,6 @@ extern "C" dr_status dr_render_blocks_noalloc(const dr_scene *sc, const dr_camer
     e = drk::launch_resolve(W, n_slots, stream, &launches, nullptr);
     if (e != cudaSuccess) return nfail(DR_E_CUDA, std::string("dr_render_blocks_noalloc: resolve: ") + cudaGetErrorString(e));
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_render_blocks_noalloc");
 }

@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "../../include/dr_api.h"
+#include "dr_guard.h"
 
 void dr_internal_set_error(const char *msg);
 
@@ -146,7 +147,7 @@ V3 read_vec(Reader &r, float sx) {
 
 extern "C" {
 
-dr_status dr_obj_read(const char *path, dr_mesh_file **out) {
+dr_status dr_obj_read(const char *path, dr_mesh_file **out) try {
     if (!out) return fail(DR_E_ARG, "dr_obj_read: out is NULL");
     *out = nullptr;
     if (!path) return fail(DR_E_ARG, "dr_obj_read: path is NULL");
@@ -267,6 +268,8 @@ dr_status dr_obj_read(const char *path, dr_mesh_file **out) {
     }
     *out = M;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_obj_read");
 }
 
 int32_t dr_mesh_file_objects(const dr_mesh_file *m) { return m ? (int32_t)m->objects.size() : 0; }
@@ -281,13 +284,15 @@ int32_t dr_mesh_file_object_triangles(const dr_mesh_file *m, int32_t i) {
     return (int32_t)(m->objects[i].xyz.size() / 9);
 }
 
-dr_status dr_mesh_file_object_data(const dr_mesh_file *m, int32_t i, float *xyz, float *nrm, float *uv) {
+dr_status dr_mesh_file_object_data(const dr_mesh_file *m, int32_t i, float *xyz, float *nrm, float *uv) try {
     if (!m || i < 0 || i >= (int32_t)m->objects.size()) return fail(DR_E_ARG, "dr_mesh_file_object_data: bad object");
     const auto &o = m->objects[i];
     if (xyz) std::memcpy(xyz, o.xyz.data(), o.xyz.size() * sizeof(float));
     if (nrm) std::memcpy(nrm, o.nrm.data(), o.nrm.size() * sizeof(float));
     if (uv) std::memcpy(uv, o.uv.data(), o.uv.size() * sizeof(float));
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_mesh_file_object_data");
 }
 
 void dr_mesh_file_destroy(dr_mesh_file *m) { delete m; }

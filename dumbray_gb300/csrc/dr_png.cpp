@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/dr_api.h"
+#include "dr_guard.h"
 
 void dr_internal_set_error(const char *msg);
 
@@ -364,7 +365,7 @@ dr_status fail(dr_status s, const std::string &m) {
 
 extern "C" {
 
-dr_status dr_png_read(const char *path, int32_t *width, int32_t *height, uint8_t *rgba8) {
+dr_status dr_png_read(const char *path, int32_t *width, int32_t *height, uint8_t *rgba8) try {
     if (!path || !width || !height) return fail(DR_E_ARG, "dr_png_read: NULL argument");
     std::vector<uint8_t> file;
     if (!read_all(path, file)) return fail(DR_E_ARG, std::string("dr_png_read: cannot open ") + path);
@@ -380,6 +381,8 @@ dr_status dr_png_read(const char *path, int32_t *width, int32_t *height, uint8_t
     *height = (int32_t)png.h;
     if (rgba8) std::memcpy(rgba8, png.rgba.data(), png.rgba.size());
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_png_read");
 }
 
 }  // extern "C"

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "../../include/dr_api.h"
+#include "dr_guard.h"
 
 void dr_internal_set_error(const char *msg);
 
@@ -187,7 +188,7 @@ void worker_loop(dr_progressive *P) {
 extern "C" {
 
 dr_status dr_progressive_create(const dr_scene *scene, const dr_camera *camera, const dr_render_params *params,
-                                int32_t double_buffered, dr_progressive **out) {
+                                int32_t double_buffered, dr_progressive **out) try {
     if (!out) return fail(DR_E_ARG, "dr_progressive_create: out is NULL");
     *out = nullptr;
     if (!scene || !camera || !params) return fail(DR_E_ARG, "dr_progressive_create: NULL argument");
@@ -210,9 +211,11 @@ dr_status dr_progressive_create(const dr_scene *scene, const dr_camera *camera, 
     }
     *out = P;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_progressive_create");
 }
 
-dr_status dr_progressive_set_target(dr_progressive *P, int32_t iterations) {
+dr_status dr_progressive_set_target(dr_progressive *P, int32_t iterations) try {
     if (!P) return fail(DR_E_ARG, "dr_progressive_set_target: NULL");
     {
         std::lock_guard<std::mutex> lk(P->m);
@@ -220,9 +223,11 @@ dr_status dr_progressive_set_target(dr_progressive *P, int32_t iterations) {
     }
     P->cv.notify_all();
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_progressive_set_target");
 }
 
-dr_status dr_progressive_set_view(dr_progressive *P, const dr_camera *camera, const dr_render_params *params) {
+dr_status dr_progressive_set_view(dr_progressive *P, const dr_camera *camera, const dr_render_params *params) try {
     if (!P) return fail(DR_E_ARG, "dr_progressive_set_view: NULL");
     if (params && (params->width <= 0 || params->height <= 0)) return fail(DR_E_ARG, "dr_progressive_set_view: bad resolution");
     {
@@ -233,10 +238,12 @@ dr_status dr_progressive_set_view(dr_progressive *P, const dr_camera *camera, co
     }
     P->cv.notify_all();
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_progressive_set_view");
 }
 
 dr_status dr_progressive_set_callbacks(dr_progressive *P, dr_progress_callback on_iteration,
-                                       dr_progress_callback on_complete, dr_progress_callback on_error, void *arg) {
+                                       dr_progress_callback on_complete, dr_progress_callback on_error, void *arg) try {
     if (!P) return fail(DR_E_ARG, "dr_progressive_set_callbacks: NULL");
     std::lock_guard<std::mutex> lk(P->m);
     P->on_iteration = on_iteration;
@@ -244,9 +251,11 @@ dr_status dr_progressive_set_callbacks(dr_progressive *P, dr_progress_callback o
     P->on_error = on_error;
     P->cb_arg = arg;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_progressive_set_callbacks");
 }
 
-dr_status dr_progressive_start(dr_progressive *P) {
+dr_status dr_progressive_start(dr_progressive *P) try {
     if (!P) return fail(DR_E_ARG, "dr_progressive_start: NULL");
     std::lock_guard<std::mutex> lk(P->m);
     if (P->running) return DR_OK;
@@ -254,9 +263,11 @@ dr_status dr_progressive_start(dr_progressive *P) {
     P->running = true;
     P->worker = std::thread(worker_loop, P);
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_progressive_start");
 }
 
-dr_status dr_progressive_stop(dr_progressive *P) {
+dr_status dr_progressive_stop(dr_progressive *P) try {
     if (!P) return fail(DR_E_ARG, "dr_progressive_stop: NULL");
     {
         std::lock_guard<std::mutex> lk(P->m);
@@ -268,15 +279,19 @@ dr_status dr_progressive_stop(dr_progressive *P) {
     std::lock_guard<std::mutex> lk(P->m);
     P->running = false;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_progressive_stop");
 }
 
-dr_status dr_progressive_wait(dr_progressive *P, int32_t count, int32_t timeout_ms) {
+dr_status dr_progressive_wait(dr_progressive *P, int32_t count, int32_t timeout_ms) try {
     if (!P) return fail(DR_E_ARG, "dr_progressive_wait: NULL");
     std::unique_lock<std::mutex> lk(P->m);
     const bool ok = P->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms < 0 ? 0 : timeout_ms),
                                    [&] { return !P->dirty && P->done >= count; });
     if (!ok) return fail(DR_E_TIMEOUT, "dr_progressive_wait: timed out" + (P->error.empty() ? std::string() : " (" + P->error + ")"));
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_progressive_wait");
 }
 
 int32_t dr_progressive_completed(dr_progressive *P) {
@@ -285,7 +300,7 @@ int32_t dr_progressive_completed(dr_progressive *P) {
     return P->done;
 }
 
-dr_status dr_progressive_read(dr_progressive *P, float *rgba, int32_t width, int32_t height, int32_t *iteration) {
+dr_status dr_progressive_read(dr_progressive *P, float *rgba, int32_t width, int32_t height, int32_t *iteration) try {
     if (!P || !rgba) return fail(DR_E_ARG, "dr_progressive_read: NULL argument");
     std::lock_guard<std::mutex> lk(P->m);
     if (P->front.empty()) return fail(DR_E_STATE, "dr_progressive_read: no image completed yet");
@@ -294,9 +309,11 @@ dr_status dr_progressive_read(dr_progressive *P, float *rgba, int32_t width, int
     std::memcpy(rgba, P->front.data(), P->front.size() * sizeof(float));
     if (iteration) *iteration = P->front_iteration;
     return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_progressive_read");
 }
 
-dr_status dr_progressive_save_png(dr_progressive *P, const char *path) {
+dr_status dr_progressive_save_png(dr_progressive *P, const char *path) try {
     if (!P || !path) return fail(DR_E_ARG, "dr_progressive_save_png: NULL argument");
     std::vector<float> img;
     int w, h;
@@ -308,6 +325,8 @@ dr_status dr_progressive_save_png(dr_progressive *P, const char *path) {
         h = P->front_h;
     }
     return dr_image_write_png(img.data(), w, h, path);
+} catch (...) {
+    return dr_internal_exception("dr_progressive_save_png");
 }
 
 double dr_progressive_render_seconds(dr_progressive *P) {

@@ -8,7 +8,8 @@
  * implemented by DumbRenderer (__source__/DataStructures/Renderers/DumbRenderer/DumbRenderer.cu:52-113),
  * together with the function packs that path calls: Octree cast, Shader, Lense, Light and the
  * block-based frame buffer.  Every entry point is extern "C", takes plain pointers and sizes, and
- * returns a dr_status; there is no CPU fallback.  Device pointers are CUDA device memory owned by
+ * returns a dr_status; there is no CPU fallback.  No C++ exception leaves the library: a host
+ * allocation failure inside a call returns DR_E_NOMEM, any other exception DR_E_STATE.  Device pointers are CUDA device memory owned by
  * the caller unless stated otherwise; `stream` is a cudaStream_t passed as void*.
  *
  * Threading: a dr_scene is immutable after creation and may be shared by any number of threads.

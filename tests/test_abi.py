@@ -85,3 +85,16 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
         dr.Scene(np.zeros((1, 3, 3), np.float32), materials=[dr.lambert()])
     with pytest.raises(RuntimeError, match="missing"):
         dr.Renderer()
+
+
+def test_exceptions_do_not_cross_the_c_abi():
+    """Host allocation failures inside an entry point come back as status codes (no std::terminate):
+    dr_image_write_png sizes its row buffer from width x height before it reads a pixel."""
+    L = dr.lib()
+    px = np.zeros(16, np.float32)
+    fn = L.dr_image_write_png
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_char_p]
+    assert fn(px.ctypes.data, 1 << 30, 1 << 30, b"never-written.png") == dr.DR_E_NOMEM
+    assert L.dr_last_error() == b"dr_image_write_png: out of host memory"
+    assert fn(px.ctypes.data, 0x7FFFFFFF, 0x7FFFFFFF, b"never-written.png") == dr.DR_E_STATE
+    assert L.dr_last_error().startswith(b"dr_image_write_png: ")
