@@ -105,3 +105,16 @@ def test_physical_tree_covers_every_triangle_with_fewer_refs(level, max_ratio):
     expl = dr.build_octree_host(tris, box_epsilon=dr.tight_box_epsilon(tris))
     for x, y in zip(phys[1:], expl[1:]):
         assert np.array_equal(np.asarray(x).view(np.int32), np.asarray(y).view(np.int32))
+
+
+@pytest.mark.timeout(120)
+@pytest.mark.parametrize("bad", [np.nan, np.inf, -np.inf, 3e38])
+def test_builder_terminates_on_non_finite_vertices(bad):
+    """Vertices the caller did not sanitise (NaN, infinities, coordinates near FLT_MAX) still give a
+    tree in bounded time, and every finite triangle stays referenced by a leaf."""
+    tris = np.random.default_rng(0).uniform(-1, 1, size=(200, 3, 3)).astype(np.float32)
+    tris[5, 1, 2] = bad
+    tris[17, 0, 0] = bad
+    st, box, child, leaf, refs = dr.build_octree_host(tris)
+    finite = np.isfinite(tris).all(axis=(1, 2)) & (np.abs(tris) < 1e30).all(axis=(1, 2))
+    assert set(np.flatnonzero(finite)) <= set(refs.tolist())
