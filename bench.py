@@ -34,9 +34,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Mpaths/s 1080p 64spp on 1 GB300: plain vs batched, fwd vs fwd+adjoint, at RMSE"
-# DRAM bytes (read + write) per extension ray of k_trace, from one ncu capture of every k_trace launch
-# of a 960x544, 4 spp frame of the same scene, camera and octree (0.933 GB over 3,946,242 rays); the
-# `traffic` of an average full-size launch is this times its ray count (profiles/k_trace_full_path_trace_1080p.md).
+# DRAM bytes (read + write) per extension ray of k_trace: ncu dram__bytes_read.sum + dram__bytes_write.sum
+# summed over every k_trace launch of one 960x544, 4 spp frame of the same scene, camera and octree
+# (0.933 GB over 3,946,242 rays); the `traffic` of an average full-size launch is this times its ray count.
 TRACE_DRAM_BYTES_PER_RAY = 236.4
 UNIT = "Mpaths/s"
 
@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable (adjoint) leg")
     ap.add_argument("--no-raycast", action="store_true", help="skip the ray-cast microbenchmark leg")
     ap.add_argument("--no-twin", action="store_true", help="skip the reference-mode twin leg")
+    ap.add_argument("--no-c1", action="store_true", help="skip the 256x256 plain path-trace leg")
     ap.add_argument("--lanes", type=int, default=0, help="concurrent wave pipelines per renderer (0 = library default)")
     ap.add_argument("--split", type=int, default=12,
                     help="octree leaf split threshold of the path-trace scene (12: best of 8/12/16/24 on this "
@@ -217,6 +218,19 @@ def cpu_baseline_ours(S, cam, W, H, depth, seed, spp=(8, 8)):
     return dict(value=paths / dt / 1e6, unit=UNIT, cores=threads, kind="port",
                 sample=f"FP64 oracle, centre patch of 8x12 blocks of {W}x{H} ({px:,} px) x {spp[0] * spp[1]} spp, "
                        f"depth {depth}, {dt:.1f} s"), (ranges, fb, p, osc)
+
+
+def fp64_error(g, o):
+    """Relative RMSE (RMSE over the compared pixels / the oracle's mean), relative difference of the
+    means, and that difference in units of its Monte Carlo standard error (per-pixel differences)."""
+    g = np.asarray(g, np.float64)[..., :3]
+    o = np.asarray(o, np.float64)[..., :3]
+    m = max(float(o.mean()), 1e-12)
+    diff = (g - o).reshape(-1, 3).mean(1)
+    se = max(float(diff.std(ddof=1) / np.sqrt(len(diff))), 1e-15)
+    return {"rmse_rel": round(float(np.sqrt(np.mean((g - o) ** 2)) / m), 6),
+            "mean_rel_diff": round(float((g.mean() - o.mean()) / m), 7),
+            "mean_diff_in_se": round(float(diff.mean() / se), 3)}
 
 
 def run_ours(a):
@@ -411,11 +425,39 @@ def run_ours(a):
             "rmse_rel": float(np.sqrt(np.mean((g2 - o2) ** 2)) / max(o2.mean(), 1e-9)),
             "mean_rel_diff": float((g2.mean() - o2.mean()) / max(o2.mean(), 1e-9)),
             "sample": "centre row of 12 blocks (1,536 px), 16 iterations x 64 spp = 1,024 spp, same seeds"}
+        # the fisheye and spherical lens variants of the same frame, on the same samples
+        lens_acc = {}
+        for lens in ("fisheye", "spherical"):
+            c2 = make_camera(dr, lens)
+            ofb3 = np.zeros((nb * 128, 4), np.float32)
+            gfb3 = dr.new_frame_buffer(W, H, dev)
+            for s0, s1 in ranges:
+                osc.render_blocks(c2, p, fb=ofb3, start=s0, end=s1, threads=threads)
+                rend.render_blocks(scene, c2, gfb3, s0, s1, p, stream)
+            ofb4 = np.zeros((nb * 128, 4), np.float32)
+            gfb4 = dr.new_frame_buffer(W, H, dev)
+            for it in range(1, 17):
+                pit = dr.render_params(W, H, dr.MODE_PHYSICAL, samples=(8, 8), max_bounces=a.depth, iteration=it, seed=4321)
+                for s0, s1 in crng:
+                    osc.render_blocks(c2, pit, fb=ofb4, start=s0, end=s1, threads=threads)
+                    rend.render_blocks(scene, c2, gfb4, s0, s1, pit, stream)
+            torch.cuda.synchronize()
+            g3, g4 = gfb3.cpu().numpy(), gfb4.cpu().numpy()
+            lens_acc[lens] = {
+                "patch_64spp": fp64_error(np.concatenate([g3[s0 * 128:s1 * 128] for s0, s1 in ranges]),
+                                          np.concatenate([ofb3[s0 * 128:s1 * 128] for s0, s1 in ranges])),
+                "converged_1024spp": fp64_error(np.concatenate([g4[s0 * 128:s1 * 128] for s0, s1 in crng]),
+                                                np.concatenate([ofb4[s0 * 128:s1 * 128] for s0, s1 in crng]))}
+        lens_acc["sample"] = ("as for the pinhole: centre patch 12,288 px x 64 spp and centre row of 12 blocks x "
+                              "1,024 spp, same seeds on both sides")
+        out["lens_variants_accuracy_vs_fp64_oracle"] = lens_acc
     del rend
     if rank == 0 and world == 1 and not a.no_raycast:
         out["raycast"] = run_raycast(dr, torch, dev, a, peak, peak_src)
+    if rank == 0 and world == 1 and not a.no_c1:
+        out["c1_plain"] = run_c1(dr, torch, dev, a)
     if rank == 0 and world == 1 and not a.no_twin:
-        out["reference_mode_twin"] = run_reference_twin_gpu(dr, torch, dev, a, S)
+        out["reference_mode_twin"] = run_reference_twin_gpu(dr, torch, dev, a, S, peak, peak_src)
     if rank == 0 and world == 1 and not a.no_batched:
         out["batched"] = run_batched(dr, torch, dev, a)
     if rank == 0 and world == 1 and not a.no_adjoint:
@@ -424,6 +466,79 @@ def run_ours(a):
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_c1(dr, torch, dev, a):
+    """The CPU-runnable plain path trace (2x2x2 room with a red wall, icosphere level 5 of radius 0.6,
+    0.5x0.5 emissive quad of radiance 10; pinhole 60 degrees; 256x256, 16 spp, depth 4, seed 0,
+    reference leaf size 8): GPU Mpaths/s (physical mode), its error against the FP64 oracle on the
+    whole image at the same samples, and the reference-expressible twin (the quad as a spherical
+    light of the same power) rendered in reference mode on the GPU and by the reference
+    DumbRenderer on host cores."""
+    from dumbray_gb300 import scenes
+    sys.path.insert(0, str(ROOT / "tests"))
+    import _oracle as O
+    c = scenes.box_and_icosphere(5)
+    mats = [dr.lambert((0.7, 0.7, 0.7)), dr.lambert((0.7, 0.1, 0.1)), dr.lambert((0.0, 0.0, 0.0), emission=(10.0, 10.0, 10.0))]
+    W = H = 256
+    nb = dr.block_count(W, H)
+    cam = dr.camera(dr.LENS_PINHOLE, position=(0.0, 0.0, -0.99), angle=60.0)
+    sc = dr.Scene(c["tris"], mat_id=c["mat_id"], materials=mats)
+    rend = dr.Renderer(1 << 22)
+    fb = dr.new_frame_buffer(W, H, dev)
+
+    def params(it):
+        return dr.render_params(W, H, dr.MODE_PHYSICAL, samples=(4, 4), max_bounces=4, iteration=it, seed=0)
+
+    for i in range(3):
+        rend.render_blocks(sc, cam, fb, 0, nb, params(2 + i))
+    K = 20
+    ms = _events_ms(torch, lambda i: rend.render_blocks(sc, cam, fb, 0, nb, params(2 + i)), K) / K
+    rend.render_blocks(sc, cam, fb, 0, nb, params(1))
+    torch.cuda.synchronize()
+    g = fb.cpu().numpy()
+    threads = os.cpu_count() or 1
+    osc = O.OracleScene(c["tris"], mat_id=c["mat_id"], materials=mats, threads=threads)
+    t0 = time.time()
+    o = osc.render_blocks(cam, params(1), threads=threads)
+    osec = time.time() - t0
+    paths = W * H * 16
+    out = {"workload": f"room + icosphere L5 + emissive quad ({len(c['tris']):,} tris), 256x256, 16 spp, depth 4, pinhole, "
+                       "physical mode",
+           "mpaths_s": round(paths / (ms / 1e3) / 1e6, 2), "ms_per_frame": round(ms, 3),
+           "accuracy_vs_fp64_oracle": dict(fp64_error(g, o), sample="whole image, 16 spp, same seeds"),
+           "fp64_oracle_mpaths_s": round(paths / osec / 1e6, 4), "fp64_oracle_cores": threads}
+    rend.close()
+    sc.close()
+    # reference-expressible twin: reference mode on the GPU vs the reference DumbRenderer on host cores
+    gold = ROOT / "tests" / "golden"
+    sys.path.insert(0, str(gold))
+    from make_golden import c1_twin
+    tris, mat, tmats, lights, tcam = c1_twin()
+    tsc = dr.Scene(tris, mat_id=mat, materials=tmats, lights=lights)
+    trend = dr.Renderer(1 << 22)
+    tfb = dr.new_frame_buffer(W, H, dev)
+
+    def tparams(it):
+        return dr.render_params(W, H, dr.MODE_REFERENCE, samples=(4, 4), max_bounces=4, iteration=it, seed=0)
+
+    for i in range(3):
+        trend.render_blocks(tsc, tcam, tfb, 0, nb, tparams(1 + i))
+    tms = _events_ms(torch, lambda i: trend.render_blocks(tsc, tcam, tfb, 0, nb, tparams(4 + i)), K) / K
+    trend.close()
+    tsc.close()
+    twin = {"workload": "reference-expressible twin (the quad as a spherical light of equal power at y = 0.8), "
+                        "reference mode, 256x256, 16 spp, depth 4",
+            "gpu_mpaths_s": round(paths / (tms / 1e3) / 1e6, 2),
+            "parity": "tests/test_configs_gpu.py: per pixel vs the oracle, statistically vs the reference DumbRenderer"}
+    ref = time_reference_renderer(tris, mat, tmats, lights, tcam, 4, steps=3, warmup=1, sw=W, sh=H)
+    if ref is not None:
+        sec, rbuild, rthreads, rpaths = ref
+        twin["reference_cpu_mpaths_s"] = round(rpaths / sec / 1e6, 4)
+        twin["reference_cpu_cores"] = rthreads
+        twin["vs_reference_cpu"] = round(twin["gpu_mpaths_s"] / twin["reference_cpu_mpaths_s"], 1)
+    out["reference_mode_twin"] = twin
+    return out
 
 
 def _batch_scene(dr, job, split=0):
@@ -444,39 +559,126 @@ def _events_ms(torch, fn, steps):
     return e0.elapsed_time(e1)
 
 
-def run_reference_twin_gpu(dr, torch, dev, a, S):
-    """The workload of the reference arm (the reference-expressible twin of the path-trace scene:
-    DumbBased / SimpleStochastic materials, 4 spherical lights, SimpleStochasticLense 60 degrees from
-    (0, 0.6, -3.4), depth a.depth) rendered in reference mode (DumbRenderer's estimator) on the
-    reference's octree, as a full 1920x1080 frame at 1 spp per step; same unit as the reference
-    arm, which times a 240x136 sample of that frame on the host cores."""
+def time_reference_renderer(tris, mat, mats, lights, cam, depth, steps, warmup, sw=240, sh=136):
+    """The reference DumbRenderer (compiled from the reference sources into oracle/_ref) on all host
+    threads: mean seconds per sw x sh x 1 spp render after `warmup` untimed ones, plus the octree
+    build time and the thread count.  None when the reference library is absent."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import _oracle as O
+    if not O.reference_available():
+        return None
+    L = O.reference()
+    threads = os.cpu_count() or 1
+    t_ = np.ascontiguousarray(tris, np.float32)
+    m_ = np.ascontiguousarray(mat, np.int32)
+    mrec = np.ascontiguousarray(np.stack([O.ref_material_record(m) for m in mats]))
+    lrec = np.ascontiguousarray(np.stack([O.ref_light_record(l) for l in lights]))
+    crec = O.ref_camera_record(cam)
+    t0 = time.time()
+    h = L.dref_scene_create(t_.ctypes.data, None, m_.ctypes.data, len(t_), mrec.ctypes.data, len(mrec),
+                            lrec.ctypes.data, len(lrec), crec.ctypes.data)
+    build_s = time.time() - t0
+    img = np.zeros((sh, sw, 4), np.float32)
+    try:
+        for _ in range(warmup):
+            L.dref_render(h, sw, sh, 1, 1, depth, 1, 1, threads, img.ctypes.data)
+        secs = [L.dref_render(h, sw, sh, 1, 1, depth, 1, 1, threads, img.ctypes.data) for _ in range(steps)]
+    finally:
+        L.dref_scene_destroy(h)
+    return float(np.mean(secs)), build_s, threads, sw * sh
+
+
+def run_reference_twin_gpu(dr, torch, dev, a, S, peak, peak_src):
+    """The drop-in path at the headline size: the reference-expressible twin of the path-trace scene
+    (DumbBased / SimpleStochastic materials, 4 spherical lights, SimpleStochasticLense 60 degrees from
+    (0, 0.6, -3.4)) rendered in reference mode (DumbRenderer's estimator) on the reference's octree,
+    1920x1080, 64 spp (8x8 sub-pixels), depth a.depth, i.e. the workload the reference arm times on
+    host cores.  value: CUDA events over the timed frames, scene resident; e2e: the same through the
+    public API with the frame buffer copied host->device and device->host every frame (pinned);
+    roofline: the photon casts (k_shadow_ref passes + k_photon_chain, the dominant kernel class),
+    algorithmic bytes = casts x (40 + 32 C_box + 36 C_tri) from the counting pass, over their busy
+    time; cpu_baseline: the reference DumbRenderer itself on a 240x136 x 1 spp sample of the frame."""
     tris, mat, mats, lights = reference_twin(S, dr)
+    t0 = time.time()
     sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights, device_build=True)
+    build_s = time.time() - t0
     cam = dr.camera(dr.LENS_SIMPLE_STOCHASTIC, position=(0.0, 0.6, -3.4), angle=60.0)
     W, H = 1920, 1080
+    spp = 64
     nb = dr.block_count(W, H)
     fb = dr.new_frame_buffer(W, H, dev)
     rend = dr.Renderer(a.wave, a.lanes)
+    stream = torch.cuda.current_stream()
 
-    def step(i):
-        rend.render_blocks(sc, cam, fb, 0, nb, dr.render_params(W, H, dr.MODE_REFERENCE, samples=(1, 1),
-                                                                 max_bounces=a.depth, iteration=1 + i, seed=77))
+    def params(i):
+        return dr.render_params(W, H, dr.MODE_REFERENCE, samples=(8, 8), max_bounces=a.depth, iteration=1 + i, seed=77)
 
-    for i in range(3):
-        step(i)
-    K = max(3, a.steps)
-    ms = _events_ms(torch, lambda i: step(3 + i), K) / K
-    rend.set_profiling(True)
-    step(3 + K)
+    rend.render_blocks(sc, cam, fb, 0, nb, params(0), stream)
+    K = max(2, min(3, a.steps))
     torch.cuda.synchronize()
+    rend.set_profiling(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(K):
+        rend.render_blocks(sc, cam, fb, 0, nb, params(1 + i), stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / K
     kt = rend.kernel_times()
+    kbusy = rend.kernel_busy()
     rend.set_profiling(False)
+    host_fb = torch.zeros(fb.shape, dtype=torch.float32).pin_memory()
+    host_out = torch.zeros(fb.shape, dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for i in range(K):
+        fb.copy_(host_fb, non_blocking=True)
+        rend.render_blocks(sc, cam, fb, 0, nb, params(1 + K + i), stream)
+        host_out.copy_(fb, non_blocking=True)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = f0.elapsed_time(f1) / K
+    rend.set_counting(True)
+    rend.render_blocks(sc, cam, fb, 0, nb, params(0), stream)
+    cnt = rend.counters()
+    rend.set_counting(False)
     rend.close()
     sc.close()
-    return {"kernel_ms_per_frame": {k: round(v[0], 2) for k, v in kt.items()},
-            "workload": f"reference-expressible twin ({len(tris):,} tris, {len(lights)} spherical lights), reference mode, "
-                        f"{W}x{H} x 1 spp, depth {a.depth}, reference octree",
-            "ms_per_frame": round(ms, 3), "mpaths_s": round(W * H / (ms / 1e3) / 1e6, 2)}
+    paths = W * H * spp
+    value = paths / (ms / 1e3) / 1e6
+    e2e = paths / (ms_e2e / 1e3) / 1e6
+    casts = cnt["shadow_casts"]
+    c_box = cnt["shadow_box"] / max(1, casts)
+    c_tri = cnt["shadow_tri"] / max(1, casts)
+    bpr = 40.0 + 32.0 * c_box + 36.0 * c_tri
+    shadow_ms = kbusy["shadow"] / K
+    achieved = casts * bpr / (shadow_ms / 1e3) / 1e9 if shadow_ms > 0 else 0.0
+    out = {"workload": f"reference-expressible twin ({len(tris):,} tris, {len(lights)} spherical lights), reference mode "
+                       f"(DumbRenderer's estimator), {W}x{H} x {spp} spp, depth {a.depth}, reference octree",
+           "mpaths_s": round(value, 3), "ms_per_frame": round(ms, 2), "frames": K,
+           "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(fb.numel() * 4),
+                   "d2h_bytes_per_step": int(fb.numel() * 4)},
+           "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(achieved / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
+                        "kernel": "k_shadow_ref + k_photon_chain (photon casts)", "casts_per_frame": int(casts),
+                        "c_box": round(c_box, 2), "c_tri": round(c_tri, 2), "bytes_per_cast": round(bpr, 1),
+                        "busy_ms_per_frame": round(shadow_ms, 2),
+                        "basis": "photon-cast busy time (union of launch intervals over lanes) per frame"},
+           "extension_rays_per_frame": int(cnt["trace_rays"]),
+           "kernel_busy_ms_per_frame": {k: round(v / K, 2) for k, v in kbusy.items()},
+           "kernel_launch_ms_sum_per_frame": {k: round(v[0] / K, 2) for k, v in kt.items()},
+           "scene_build_s": round(build_s, 2)}
+    ref = time_reference_renderer(tris, mat, mats, lights, cam, a.depth, steps=3, warmup=1)
+    if ref is not None:
+        sec, rbuild, threads, rpaths = ref
+        rv = rpaths / sec / 1e6
+        out["cpu_baseline"] = {"value": round(rv, 5), "unit": UNIT, "cores": threads, "kind": "reference",
+                               "sample": f"reference DumbRenderer (CPU threads) compiled from the reference sources; "
+                                         f"240x136 px x 1 spp per step ({rpaths:,} paths), 3 steps, octree build "
+                                         f"{rbuild:.1f} s excluded"}
+        out["vs_reference_cpu"] = {"device": round(value / rv, 1), "e2e": round(e2e / rv, 1)}
+    return out
 
 
 def run_raycast(dr, torch, dev, a, peak, peak_src):
@@ -543,6 +745,23 @@ def run_raycast(dr, torch, dev, a, peak, peak_src):
             del ot, dt, tri0, nb0, nt0
         out[tree] = res
         sc.close()
+    # parity on a subset: 65,536 incoherent rays and every 32nd primary, reference tree, culling on,
+    # against the oracle (the reference's Octree::cast restated; pinned to the reference's own casts)
+    sys.path.insert(0, str(ROOT / "tests"))
+    import _oracle as O
+    osc = O.OracleScene(mesh, threads=os.cpu_count() or 1)
+    so = np.concatenate([sets["incoherent_8M"][0][:65536], sets["primary_1080p"][0][::32]])
+    sd = np.concatenate([sets["incoherent_8M"][1][:65536], sets["primary_1080p"][1][::32]])
+    sc = dr.Scene(mesh, materials=[dr.lambert()])
+    gi, gt = dr.cast(sc, torch.from_numpy(so).to(dev), torch.from_numpy(sd).to(dev))
+    gi, gt = gi.cpu().numpy(), gt.cpu().numpy()
+    oi, ot, _, _ = osc.cast(so, sd, cull=True, threads=os.cpu_count() or 1)
+    hit = oi >= 0
+    out["parity_vs_oracle"] = {"rays": int(len(so)), "index_mismatches": int((gi != oi).sum()),
+                               "t_bit_mismatches": int((gt[hit].view(np.int32) != ot[hit].view(np.int32)).sum()),
+                               "tree": "reference", "cull": True}
+    sc.close()
+    del osc
     out["physical_vs_reference_tree_hit_mismatch"] = {
         k: float(np.mean(hits["reference_tree"][k] != hits["physical_tree"][k])) for k in sets}
     return out
@@ -619,6 +838,31 @@ def run_batched(dr, torch, dev, a):
     batch_launches = brend.launches() - l0
     batch_means = np.array([fb[:, :3].double().mean().item() for fb in fbs])
     rel = np.abs(batch_means - plain_means) / np.maximum(np.abs(plain_means), 1e-9)
+    # FP64 oracle error of a sample of jobs: the 4 cheapest for the oracle (paths x depth plus tree
+    # build), one per resolution, rendered by the batch at iteration 1 and by the oracle alike
+    sys.path.insert(0, str(ROOT / "tests"))
+    import _oracle as O
+    threads = os.cpu_count() or 1
+    batch.set_iteration(1)
+    batch.render(brend, use_graph=True)
+    torch.cuda.synchronize()
+    cost = [j["width"] * j["height"] * j["spp"] + 4 * n for j, n in zip(jobs, n_tris)]
+    picked, seen = [], set()
+    for i in np.argsort(cost):
+        if jobs[i]["width"] not in seen:
+            picked.append(int(i))
+            seen.add(jobs[i]["width"])
+        if len(picked) == 4:
+            break
+    acc = {}
+    for i in picked:
+        j = jobs[i]
+        osc = O.OracleScene(j["tris"], mat_id=j["mat_id"], materials=[dr.lambert(), dr.mirror(), dr.glossy()], threads=threads)
+        osc.set_triangle_params(j["albedo"], j["emission"], j["roughness"])
+        ofb = osc.render_blocks(cams[i], params(j, 1), threads=threads)
+        acc[f"job{i}"] = dict(fp64_error(fbs[i].cpu().numpy(), ofb), triangles=int(n_tris[i]),
+                              resolution=int(j["width"]), spp=int(j["spp"]))
+        del osc
     v_plain = paths * K / (plain_ms / 1e3) / 1e6
     v_batch = paths * K / (batch_ms / 1e3) / 1e6
     res = sorted({(j["width"], j["spp"]) for j in jobs})
@@ -636,6 +880,8 @@ def run_batched(dr, torch, dev, a):
                      "leaf_probe_ms": {str(k): v for k, v in split_table.items()},
                      "wave": best_wave, "wave_probe_ms": {str(k): v for k, v in wave_table.items()}},
         "job_mean_max_rel_diff_batched_vs_plain": float(rel.max()),
+        "accuracy_vs_fp64_oracle": dict(acc, sample="4 jobs (the cheapest for the oracle of each resolution), "
+                                                    "whole image, iteration 1 at the job's spp, same seeds"),
         "host_s": {"generate": round(gen_s, 1), "build": round(build_s, 1), "autotune": round(tune_s, 1)},
         "resolution_spp_mix": [list(r) for r in res],
     }
@@ -718,6 +964,24 @@ def run_differentiable(dr, torch, dev, a):
         emi[k, ch] = x
         fd = (lp - lm) / 2e-2
         errs.append(("emission", int(k), ch, float(ge_h[k, ch]), fd, abs(ge_h[k, ch] - fd) / max(abs(fd), 1e-12)))
+    # forward image against the FP64 oracle: 4 rows x 16 blocks at the image centre (8,192 px), 16 spp
+    sys.path.insert(0, str(ROOT / "tests"))
+    import _oracle as O
+    threads = os.cpu_count() or 1
+    osc = O.OracleScene(S["tris"], mat_id=S["mat_id"], materials=[dr.lambert()], threads=threads)
+    osc.set_triangle_params(S["albedo"], S["emission"], S["roughness"])
+    bw = nb // 32
+    ranges = [((14 + r) * bw + 16, (14 + r) * bw + 32) for r in range(4)]
+    ofb = np.zeros((nb * 128, 4), np.float32)
+    for s0, s1 in ranges:
+        osc.render_blocks(cam, p, fb=ofb, start=s0, end=s1, threads=threads)
+    rend.render_blocks(sc, cam, img, 0, nb, p)
+    torch.cuda.synchronize()
+    gimg = img.cpu().numpy()
+    fwd_acc = dict(fp64_error(np.concatenate([gimg[s0 * 128:s1 * 128] for s0, s1 in ranges]),
+                              np.concatenate([ofb[s0 * 128:s1 * 128] for s0, s1 in ranges])),
+                   sample="4 rows x 16 blocks at the centre (8,192 px), 16 spp, same seeds")
+    del osc
     rend.close()
     sc.close()
     worst = max(errs, key=lambda e: e[5])
@@ -727,6 +991,7 @@ def run_differentiable(dr, torch, dev, a):
         "fwd_ms": round(fwd_ms, 3), "fwd_adj_ms": round(fa_ms, 3), "ratio": round(fa_ms / fwd_ms, 3),
         "fwd_mpaths_s": round(paths / (fwd_ms / 1e3) / 1e6, 3),
         "fwd_adj_mpaths_s": round(paths / (fa_ms / 1e3) / 1e6, 3),
+        "forward_accuracy_vs_fp64_oracle": fwd_acc,
         "fd_check": {"method": "central differences, common random numbers, parameters written in place; "
                                "h = 1e-3 (albedo), 1e-2 (emission 10)",
                      "components": len(errs), "max_rel_err": float(max(e[5] for e in errs)),
@@ -769,23 +1034,10 @@ def run_reference(a):
     # bounded sample of the 1080p frame: a 240x136 image (1/64 of the pixels) at 1 spp per step
     sw, sh = 240, 136
     paths = sw * sh
-    if O.reference_available():
-        L = O.reference()
-        import ctypes
-        t_ = np.ascontiguousarray(tris, np.float32)
-        m_ = np.ascontiguousarray(mat, np.int32)
-        mrec = np.ascontiguousarray(np.stack([O.ref_material_record(m) for m in mats]))
-        lrec = np.ascontiguousarray(np.stack([O.ref_light_record(l) for l in lights]))
-        crec = O.ref_camera_record(cam)
-        t0 = time.time()
-        h = L.dref_scene_create(t_.ctypes.data, None, m_.ctypes.data, len(t_), mrec.ctypes.data, len(mrec),
-                                lrec.ctypes.data, len(lrec), crec.ctypes.data)
-        build_s = time.time() - t0
-        img = np.zeros((sh, sw, 4), np.float32)
-        for _ in range(a.warmup):
-            L.dref_render(h, sw, sh, 1, 1, a.depth, 1, 1, threads, img.ctypes.data)
-        secs = [L.dref_render(h, sw, sh, 1, 1, a.depth, 1, 1, threads, img.ctypes.data) for _ in range(a.steps)]
-        L.dref_scene_destroy(h)
+    ref = time_reference_renderer(tris, mat, mats, lights, cam, a.depth, a.steps, a.warmup, sw, sh)
+    if ref is not None:
+        sec, build_s, threads, _ = ref
+        secs = [sec]
         kind = "reference"
         what = "reference DumbRenderer (CPU threads) compiled from the reference sources"
     else:

@@ -772,7 +772,8 @@ def image_to_blockmajor(img: np.ndarray) -> np.ndarray:
 def render_blocks_noalloc(scene: Scene, cam: DrCamera, fb, start_block: int, end_block: int, params: DrRenderParams,
                           stream=None):
     """dr_render_blocks_noalloc: the same render as Renderer.render_blocks for callers that cannot
-    allocate device memory while rendering (e.g. inside a CUDA stream capture); uses the library's
+    allocate device memory while rendering (a foreign memory pool, a thread that must not synchronise
+    the device through cudaMalloc); uses the library's
     fixed 16 MiB device scratch array, at most 2048 blocks per call, calls on different streams race."""
     L = lib()
     fn = L.dr_render_blocks_noalloc

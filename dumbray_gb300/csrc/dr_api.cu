@@ -759,9 +759,12 @@ dr_status dr_renderer_counters(dr_renderer *r, int64_t *counts) try {
     return dr_internal_exception("dr_renderer_counters");
 }
 
-// Validates one render job and fills its Item (everything but the slot / path offsets).
-static dr_status make_item(const dr_scene *sc, const dr_camera *cam, float *fb, int32_t start_block, int32_t end_block,
-                           const dr_render_params *p, const char *who, drk::Item &I) {
+}  // extern "C"
+
+// Validates one render job and fills its Item (everything but the slot / path offsets).  Shared by
+// dr_render_blocks, the batch builder and dr_render_blocks_noalloc (declared in dr_internal.h).
+dr_status dr_internal_make_item(const dr_scene *sc, const dr_camera *cam, float *fb, int32_t start_block,
+                                int32_t end_block, const dr_render_params *p, const char *who, drk::Item &I) {
     if (!sc || !cam || !fb || !p) return fail(DR_E_ARG, std::string(who) + ": NULL argument");
     if (sc->max_texture > sc->n_textures)
         return fail(DR_E_ARG, std::string(who) + ": the scene's materials use textures it does not have (dr_scene_set_textures)");
@@ -814,6 +817,8 @@ static dr_status make_item(const dr_scene *sc, const dr_camera *cam, float *fb, 
     I.blend = (p->iteration <= 1) ? 1.0f : (1.0f / (float)p->iteration);
     return DR_OK;
 }
+
+extern "C" {
 
 static dr_status ensure_accum(dr_renderer *r, size_t slots) {
     if (r->accum_slots >= slots) return DR_OK;
@@ -940,7 +945,7 @@ dr_status dr_render_blocks(dr_renderer *r, const dr_scene *sc, const dr_camera *
     if (!r) return fail(DR_E_ARG, "dr_render_blocks: NULL argument");
     drk::WaveDesc W;
     std::memset(&W, 0, sizeof(W));
-    dr_status st = make_item(sc, cam, fb, start_block, end_block, p, "dr_render_blocks", W.inl);
+    dr_status st = dr_internal_make_item(sc, cam, fb, start_block, end_block, p, "dr_render_blocks", W.inl);
     if (st != DR_OK) return st;
     if (start_block == end_block) return DR_OK;
     cudaStream_t stream = (cudaStream_t)stream_ptr;
@@ -967,7 +972,7 @@ dr_status dr_render_adjoint(dr_renderer *r, const dr_scene *sc, const dr_camera 
     if (!r || !dl_dfb || !grad_albedo || !grad_emission) return fail(DR_E_ARG, "dr_render_adjoint: NULL argument");
     drk::WaveDesc W;
     std::memset(&W, 0, sizeof(W));
-    dr_status st = make_item(sc, cam, const_cast<float *>(dl_dfb), start_block, end_block, p, "dr_render_adjoint", W.inl);
+    dr_status st = dr_internal_make_item(sc, cam, const_cast<float *>(dl_dfb), start_block, end_block, p, "dr_render_adjoint", W.inl);
     if (st != DR_OK) return st;
     if (p->mode != DR_MODE_PHYSICAL) return fail(DR_E_ARG, "dr_render_adjoint: only the physical mode is differentiable");
     if (p->max_bounces + 1 > drd::kAdjDepth) return fail(DR_E_ARG, "dr_render_adjoint: too many bounces");
@@ -1111,7 +1116,7 @@ dr_status dr_batch_create(const dr_batch_item *items, int32_t n, dr_batch **out)
     long long slot = 0;
     for (int i = 0; i < n; i++) {
         const dr_batch_item &it = items[i];
-        dr_status st = make_item(it.scene, &it.camera, it.fb, it.start_block, it.end_block, &it.params, "dr_batch_create", b->items[i]);
+        dr_status st = dr_internal_make_item(it.scene, &it.camera, it.fb, it.start_block, it.end_block, &it.params, "dr_batch_create", b->items[i]);
         if (st != DR_OK) {
             delete b;
             return st;

@@ -1,9 +1,9 @@
 // dr_noalloc.cu - dr_render_blocks_noalloc: the block renderer for callers that cannot allocate
 // device memory while they render.
 //
-// Who needs it: a host that renders from inside a CUDA stream capture (cudaMalloc is not allowed
-// there), a real-time or plugin host whose device memory is owned by someone else's pool, or a
-// caller on a latency-critical thread where cudaMalloc / cudaFree would synchronise the device.
+// Who needs it: a real-time or plugin host whose device memory is owned by someone else's pool or
+// fixed budget, or a caller on a latency-critical thread where cudaMalloc / cudaFree would
+// synchronise the device.
 // dr_render_blocks keeps its wavefront queues in a dr_renderer that cudaMallocs them (and grows
 // its accumulator on demand); this entry point instead uses one fixed scratch region that lives
 // in the library image as a file-scope __device__ array, so a call allocates nothing.
@@ -86,24 +86,16 @@ cudaError_t scratch_address(unsigned char **out) {
 
 extern "C" dr_status dr_render_blocks_noalloc(const dr_scene *sc, const dr_camera *cam, float *fb, int32_t start_block,
                                               int32_t end_block, const dr_render_params *p, void *stream_ptr) try {
-    if (!sc || !cam || !fb || !p) return nfail(DR_E_ARG, "dr_render_blocks_noalloc: NULL argument");
-    if (p->mode != DR_MODE_REFERENCE && p->mode != DR_MODE_PHYSICAL) return nfail(DR_E_ARG, "dr_render_blocks_noalloc: bad mode");
-    if (p->width <= 0 || p->height <= 0) return nfail(DR_E_ARG, "dr_render_blocks_noalloc: bad resolution");
-    const int nblocks = dr_block_count(p->width, p->height);
-    if (start_block < 0 || end_block > nblocks || start_block > end_block)
-        return nfail(DR_E_ARG, "dr_render_blocks_noalloc: bad block range");
+    drk::WaveDesc W;
+    std::memset(&W, 0, sizeof(W));
+    drk::Item &I = W.inl;
+    dr_status st = dr_internal_make_item(sc, cam, fb, start_block, end_block, p, "dr_render_blocks_noalloc", I);
+    if (st != DR_OK) return st;
     if (end_block - start_block > DR_NOALLOC_MAX_BLOCKS)
         return nfail(DR_E_CAPACITY, "dr_render_blocks_noalloc: " + std::to_string(end_block - start_block) +
                                         " blocks requested, at most " + std::to_string(DR_NOALLOC_MAX_BLOCKS) +
                                         " per call (split the range)");
-    if (p->max_bounces < 0 || p->max_bounces > 64) return nfail(DR_E_ARG, "dr_render_blocks_noalloc: max_bounces must be in [0, 64]");
-    if (p->boxing < 0 || p->boxing > 3) return nfail(DR_E_ARG, "dr_render_blocks_noalloc: bad boxing mode");
-    if (cam->lens < 0 || cam->lens > DR_LENS_SPHERICAL) return nfail(DR_E_ARG, "dr_render_blocks_noalloc: bad lens");
-    if ((p->mode == DR_MODE_REFERENCE) != (cam->lens <= DR_LENS_SPHERICAL_SEGMENT))
-        return nfail(DR_E_ARG, "dr_render_blocks_noalloc: lens does not belong to the render mode");
     if (drk::ctrl_bytes() > kCtrl) return nfail(DR_E_CAPACITY, "dr_render_blocks_noalloc: control block too large");
-    if (!dr_internal_scene_textures_ok(sc))
-        return nfail(DR_E_ARG, "dr_render_blocks_noalloc: the scene's materials use textures it does not have");
     if (start_block == end_block) return DR_OK;
     const drd::Scene *S = dr_internal_scene_device(sc);
     cudaStream_t stream = (cudaStream_t)stream_ptr;
@@ -112,9 +104,8 @@ extern "C" dr_status dr_render_blocks_noalloc(const dr_scene *sc, const dr_camer
     cudaError_t e = scratch_address(&base);
     if (e != cudaSuccess) return nfail(DR_E_CUDA, std::string("dr_render_blocks_noalloc: scratch set-up: ") + cudaGetErrorString(e));
 
-    const int fx = std::max(1, p->samples_x), fy = std::max(1, p->samples_y);
-    const int spp = fx * fy;
-    const int n_slots = (end_block - start_block) * DR_BLOCK_W * DR_BLOCK_H;
+    const int spp = I.spp;
+    const int n_slots = I.n_slots;
     const int per_path_shadow = (p->mode == DR_MODE_REFERENCE) ? std::max(1, S->shadow_photons) : 1;
     long long wave = std::min<long long>(kWavePaths, (long long)kShadowRecords / per_path_shadow);
     wave = std::max<long long>(32, (wave / 32) * 32);
@@ -123,44 +114,6 @@ extern "C" dr_status dr_render_blocks_noalloc(const dr_scene *sc, const dr_camer
     e = cudaMemsetAsync(accum, 0, sizeof(float4) * (size_t)n_slots, stream);
     if (e != cudaSuccess) return nfail(DR_E_CUDA, std::string("dr_render_blocks_noalloc: clear: ") + cudaGetErrorString(e));
 
-    drk::WaveDesc W;
-    std::memset(&W, 0, sizeof(W));
-    drk::Item &I = W.inl;
-    I.S = *S;
-    I.camera = *cam;
-    {
-        float angle = cam->angle[0];
-        if (angle < 1.0f) angle = 1.0f;
-        else if (angle > 179.0f) angle = 179.0f;
-        float radian = (angle / (2 * 57.29577951308233f));
-        I.cam_x = 0.5f / std::tan(radian);
-    }
-    I.mode = p->mode;
-    I.width = p->width;
-    I.height = p->height;
-    I.fsaa_x = fx;
-    I.fsaa_y = fy;
-    I.spp = spp;
-    I.max_bounces = p->max_bounces;
-    I.clip = p->cull_backfaces;
-    {
-        float w = (float)p->width, h = (float)p->height;
-        float ps;
-        if (p->boxing == DR_BOXING_HEIGHT) ps = 1.0f / h;
-        else if (p->boxing == DR_BOXING_WIDTH) ps = 1.0f / w;
-        else if (p->boxing == DR_BOXING_MIN) ps = 1.0f / ((h <= w) ? h : w);
-        else ps = 1.0f / ((h >= w) ? h : w);
-        I.pixel_size = ps;
-        I.pdx = ps / (float)fx;
-        I.pdy = ps / (float)fy;
-    }
-    I.seed = p->seed;
-    I.sample_base = (uint32_t)((p->iteration < 1 ? 0 : p->iteration - 1) * spp);
-    I.start_block = start_block;
-    I.n_slots = n_slots;
-    I.fb = fb;
-    I.inv_spp = 1.0f / (float)spp;
-    I.blend = (p->iteration <= 1) ? 1.0f : (1.0f / (float)p->iteration);
     W.items = nullptr;
     W.n_items = 1;
     W.mode = p->mode;

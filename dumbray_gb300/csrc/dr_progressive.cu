@@ -19,6 +19,7 @@
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
+#include <exception>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -127,10 +128,30 @@ bool render_once(dr_progressive *P, const dr_camera &cam, dr_render_params p, in
     return true;
 }
 
-void worker_loop(dr_progressive *P) {
-    cudaSetDevice(P->device);
-    std::vector<float> img;
-    for (;;) {
+// Records an exception that escaped one iteration of the worker (host allocation failure while
+// staging or publishing an image, for instance) as the render error and fires the error callback;
+// the worker then carries on, as it does after a failed render.
+void report_worker_exception(dr_progressive *P, const char *what) noexcept {
+    dr_progress_callback cb = nullptr;
+    void *arg = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(P->m);
+        try {
+            P->error = std::string("progressive worker: ") + what;
+        } catch (...) {
+            P->error.clear();
+        }
+        cb = P->on_error;
+        arg = P->cb_arg;
+    }
+    P->cv.notify_all();
+    if (cb) cb(arg);
+    std::this_thread::sleep_for(std::chrono::milliseconds(8));
+}
+
+// One iteration of the worker: waits for work, renders, publishes.  false: the worker must stop.
+bool worker_iteration(dr_progressive *P, std::vector<float> &img) {
+    {
         dr_camera cam;
         dr_render_params p;
         int next;
@@ -138,7 +159,7 @@ void worker_loop(dr_progressive *P) {
         {
             std::unique_lock<std::mutex> lk(P->m);
             for (;;) {
-                if (P->stop) return;
+                if (P->stop) return false;
                 if (P->dirty) {
                     P->done = 0;
                     P->dirty = false;
@@ -180,6 +201,21 @@ void worker_loop(dr_progressive *P) {
         if (cb_it) cb_it(arg);
         if (cb_done) cb_done(arg);
         if (!ok) std::this_thread::sleep_for(std::chrono::milliseconds(8));
+    }
+    return true;
+}
+
+void worker_loop(dr_progressive *P) {
+    cudaSetDevice(P->device);
+    std::vector<float> img;
+    for (;;) {
+        try {
+            if (!worker_iteration(P, img)) return;
+        } catch (const std::exception &ex) {
+            report_worker_exception(P, ex.what());
+        } catch (...) {
+            report_worker_exception(P, "unknown exception");
+        }
     }
 }
 

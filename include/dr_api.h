@@ -373,9 +373,9 @@ int64_t dr_batch_paths(const dr_batch *batch);
 void dr_batch_destroy(dr_batch *batch);
 
 /* Allocation-free variant of dr_render_blocks.  It has no counterpart in the reference: it exists
- * for callers that cannot allocate device memory while they render (a host rendering inside a CUDA
- * stream capture, a plugin host whose device memory belongs to another pool, a latency-critical
- * thread that must not let cudaMalloc/cudaFree synchronise the device).  Same arguments, results
+ * for callers that cannot allocate device memory while they render (a plugin host whose device
+ * memory belongs to another allocator's pool or fixed budget, a latency-critical render thread that
+ * must not let cudaMalloc/cudaFree synchronise the device).  Same arguments, results
  * and blending as dr_render_blocks, but no dr_renderer: the scratch is one file-scope device array
  * of DR_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until process exit.
  * At most DR_NOALLOC_MAX_BLOCKS blocks per call (more returns DR_E_CAPACITY).  All calls share the

@@ -689,6 +689,10 @@ struct Scene {
     std::vector<int> emissive;                   // emissive triangle ids
     std::vector<double> emissive_cdf;            // by power (luminance-free: r+g+b) x area
     double emissive_total = 0.0;
+    // dro_scene_freeze_sampling: per-triangle power used for light selection and its pdfs, fixed at
+    // the time of the call (the device library's sampling tables stay fixed when parameters are
+    // written in place); empty = follow the current emission
+    std::vector<double> frozen_power;
 };
 
 // ---- textures (Texture.impl.cuh:81-95; ColoredTexture, DumbStructs.cuh:88-131) ------------------
@@ -1235,6 +1239,10 @@ double tri_area(const Scene &S, int i) {
 double emit_power(const Scene &S, int i) {
     return (S.emission[3 * i] + S.emission[3 * i + 1] + S.emission[3 * i + 2]) * tri_area(S, i);
 }
+// Power that light selection (the NEE table and the light pdf of MIS) uses for triangle i.
+double sample_power(const Scene &S, int i) {
+    return S.frozen_power.empty() ? emit_power(S, i) : S.frozen_power[i];
+}
 
 // Occlusion between p and q (segment strictly between the end points), float cast, no culling.
 bool occluded(const Scene &S, D3 p, D3 q, int ignore_a, int ignore_b) {
@@ -1280,7 +1288,7 @@ void phys_path(const Scene &S, const Cam &cam, int W, int H, int px, int py, int
             if (cosl > 0) {
                 double w = 1.0;
                 if (!prev_delta && S.emissive_total > 0) {
-                    double pl = emit_power(S, hit) / S.emissive_total / tri_area(S, hit);
+                    double pl = sample_power(S, hit) / S.emissive_total / tri_area(S, hit);
                     double pls = pl * ((double)t * (double)t * ddot(d, d)) / cosl;
                     w = mis2(prev_pdf, pls);
                 }
@@ -1310,7 +1318,7 @@ void phys_path(const Scene &S, const Cam &cam, int W, int H, int px, int py, int
             double cosl = -ddot(lout, wi);
             double cosi = ddot(ng, wi);
             if (cosl > 0 && cosi > 0 && !occluded(S, hp, lp, hit, li)) {
-                double pl = emit_power(S, li) / S.emissive_total / tri_area(S, li);
+                double pl = sample_power(S, li) / S.emissive_total / tri_area(S, li);
                 double pls = pl * dist2 / cosl;
                 double f[3], pb;
                 if (mt == DR_MAT_GLOSSY) {
@@ -1429,12 +1437,23 @@ void dro_scene_set_triangle_params(void *h, const float *albedo, const float *em
     if (rough) std::memcpy(S->rough.data(), rough, 4 * n);
 }
 
+// freeze != 0: light selection keeps the current per-triangle emission power from now on, whatever
+// later parameter updates write (finite differences with common random numbers then differentiate
+// a fixed estimator); freeze == 0: it follows the current emission again.
+void dro_scene_freeze_sampling(void *h, int freeze) {
+    Scene *S = (Scene *)h;
+    S->frozen_power.clear();
+    if (!freeze) return;
+    S->frozen_power.resize(S->tree.tri.size());
+    for (int i = 0; i < (int)S->tree.tri.size(); i++) S->frozen_power[i] = emit_power(*S, i);
+}
+
 static void build_emissive(Scene *S) {
     S->emissive.clear();
     S->emissive_cdf.clear();
     S->emissive_total = 0.0;
     for (int i = 0; i < (int)S->tree.tri.size(); i++) {
-        double p = emit_power(*S, i);
+        double p = sample_power(*S, i);
         if (p > 0) { S->emissive.push_back(i); S->emissive_total += p; S->emissive_cdf.push_back(S->emissive_total); }
     }
 }

@@ -28,6 +28,7 @@ def oracle():
         L.dro_scene_create.restype = vp
         L.dro_scene_create.argtypes = [vp, vp, vp, ci, vp, ci, vp, ci, ci, ci, ci]
         L.dro_scene_set_triangle_params.argtypes = [vp, vp, vp, vp]
+        L.dro_scene_freeze_sampling.argtypes = [vp, ci]
         L.dro_scene_set_textures.argtypes = [vp, vp, ci, vp]
         L.dro_scene_destroy.argtypes = [vp]
         L.dro_node_count.restype = ctypes.c_longlong
@@ -116,6 +117,11 @@ class OracleScene:
         arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float32) for a in (albedo, emission, roughness)]
         oracle().dro_scene_set_triangle_params(self.h, *[None if a is None else a.ctypes.data for a in arrs])
         self._keep = arrs
+
+    def freeze_sampling(self, freeze=True):
+        """Light selection keeps the current per-triangle emission power (as the device library's
+        sampling tables do when parameters are written in place), or follows it again."""
+        oracle().dro_scene_freeze_sampling(self.h, 1 if freeze else 0)
 
     def set_textures(self, textures, uv=None):
         """As dumbray_gb300.Scene.set_textures."""

@@ -6,6 +6,14 @@
                    off; reference node count.
   cast_c1.npz      the 20,492-triangle box + icosphere level 5 geometry; 16,384 incoherent rays,
                    culling on.
+  cast_c2_l8.npz   the ray-cast microbenchmark mesh itself (icosphere level 8, 1,310,720 triangles,
+                   radially displaced by 3-octave value noise, amplitude 0.1, seed 1; stored as its
+                   SHA-256, regenerated by the tests): 8,192 of the benchmark's incoherent rays (origins
+                   uniform in [-1.1, 1.1]^3, seed 0) and 8,100 of its 1920x1080 pinhole primaries (every
+                   256th); reference Octree::cast index and t, culling on and off; reference node count.
+  render_c1_twin.npz  the reference-expressible twin of the 256x256 box + icosphere scene (c1_twin):
+                   four reference DumbRenderer runs of 64 iterations at 256x256, depth 4, stored as
+                   float16 RGB (quantisation far below the Monte Carlo noise).
   render_*.npz     reference DumbRenderer CPU renders (four independent runs of 512 progressive
                    iterations each) of small reference-expressible scenes, 32x32: a room and a sphere
                    of each reference shader (DumbBased diffuse / metal, SimpleStochastic, Fresnel,
@@ -62,6 +70,69 @@ def cast_fixtures():
     o, d = scenes.incoherent_rays(16384, -0.95, 0.95, seed=9)
     idx, t, nodes = O.ref_cast(tris, o, d, cull=True)
     np.savez_compressed(OUT / "cast_c1.npz", tris=tris, o=o, d=d, idx_cull1=idx, t_cull1=t, nodes=np.int64(nodes))
+
+
+def mesh_sha256(tris) -> str:
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(tris, np.float32).tobytes()).hexdigest()
+
+
+def c2_rays():
+    """The C2 subset: the first 8,192 of 8,192 incoherent rays drawn like the benchmark's (seed 0)
+    and every 256th of the 1920x1080 primaries (60 degrees from (0, 0.3, -3) toward the origin)."""
+    oi, di = scenes.incoherent_rays(8192, -1.1, 1.1, seed=0)
+    op, dp = scenes.primary_rays(1920, 1080, 60.0, (0.0, 0.3, -3.0), (0.0, 0.0, 0.0))
+    return np.concatenate([oi, op[::256]]), np.concatenate([di, dp[::256]])
+
+
+def cast_c2_fixture():
+    tris = scenes.displaced_icosphere(8, 0.1, 1)
+    o, d = c2_rays()
+    out = dict(o=o, d=d, mesh_sha256=np.array(mesh_sha256(tris)), n_tris=np.int64(len(tris)))
+    for cull in (1, 0):
+        idx, t, nodes = O.ref_cast(tris, o, d, cull=bool(cull))
+        out[f"idx_cull{cull}"] = idx
+        out[f"t_cull{cull}"] = t
+        out["nodes"] = np.int64(nodes)
+    np.savez_compressed(OUT / "cast_c2_l8.npz", **out)
+    print("cast_c2_l8: nodes", int(out["nodes"]), "hit fraction", float((out["idx_cull1"] >= 0).mean()))
+
+
+C1_SIZE, C1_DEPTH = 256, 4
+
+
+def c1_twin():
+    """Reference-expressible twin of the plain path-trace scene (2x2x2 room, icosphere level 5 of
+    radius 0.6, 0.5x0.5 emissive quad of radiance 10 below the ceiling): the room and the sphere keep
+    their geometry with DumbBasedShader diffuse (metal 0) albedo 0.7 and the red wall 0.7/0.1/0.1;
+    the quad becomes a SphericalLightEmitter of the same power (radiance x area x pi over 4 pi per
+    channel, radius 0.05).  The emitter sits at y = 0.8, midway between the sphere's top (0.6) and
+    the ceiling (1.0), instead of on the ceiling: a point emitter touching a wall makes the
+    reference's 1/d^2 photons heavy-tailed, and four reference runs cannot then estimate the
+    standard error.  Lens: SimpleStochasticLense 60 degrees from (0, 0, -0.99).
+    Returns (tris, mat, mats, lights, cam)."""
+    c = scenes.box_and_icosphere(5)
+    n_geo = c["n_room"] + c["n_sphere"]
+    tris, mat = c["tris"][:n_geo], c["mat_id"][:n_geo].copy()
+    mats = [dr.dumb_based(diffuse=(0.7, 0.7, 0.7), metal=0.0), dr.dumb_based(diffuse=(0.7, 0.1, 0.1), metal=0.0)]
+    power = 10.0 * 0.25 * np.pi
+    lights = [dr.spherical_light((power / (4.0 * np.pi),) * 3, (0.0, 0.8, 0.0), 0.05)]
+    cam = dr.camera(dr.LENS_SIMPLE_STOCHASTIC, position=(0.0, 0.0, -0.99), angle=60.0)
+    return tris, mat, mats, lights, cam
+
+
+def render_c1_twin_fixture(iterations=64, runs=4):
+    tris, mat, mats, lights, cam = c1_twin()
+    out, secs = [], 0.0
+    for _ in range(runs):
+        img, t = O.ref_render(tris, mat, mats, lights, cam, C1_SIZE, C1_SIZE, max_bounces=C1_DEPTH,
+                              iterations=iterations)
+        out.append(img[..., :3].astype(np.float16))
+        secs += t
+    runs_arr = np.stack(out)
+    np.savez_compressed(OUT / "render_c1_twin.npz", runs=runs_arr, iterations=np.int64(iterations),
+                        size=np.int64(C1_SIZE), bounces=np.int64(C1_DEPTH), seconds=np.float64(secs))
+    print("c1 twin: reference seconds", secs, "mean", runs_arr.astype(np.float64).mean())
 
 
 def render_scene(kind: str):
@@ -383,11 +454,17 @@ if __name__ == "__main__":
     only = sys.argv[1:]
     if not only or "cast" in only:
         cast_fixtures()
+    if not only or "cast_c2" in only:
+        cast_c2_fixture()
+    if not only or "render_c1_twin" in only:
+        render_c1_twin_fixture()
     if not only or "render" in only:
         render_fixtures()
     if not only or "textures" in only:
         texture_fixtures()
     for k in only:
+        if k == "render_c1_twin":
+            continue
         if k.startswith("render_tex_"):
             texture_fixtures(kinds=(k[len("render_"):],))
         elif k.startswith("render_"):

@@ -94,78 +94,118 @@ def test_adjoint_matches_central_differences_with_common_random_numbers(cuda):
             assert abs(ge_h[k, ch] - fd) <= 1e-2 * abs(fd) + 1e-6, (k, ch, ge_h[k, ch], fd)
 
 
+def _fd_report(what, rows):
+    for name, k, ch, adj, fd in rows:
+        print(f"{what}: {name}[{k},{ch}] adjoint {adj:+.6e} fd {fd:+.6e} rel {abs(adj - fd) / max(abs(fd), 1e-12):.2e}")
+
+
 def test_adjoint_matches_fp64_oracle_finite_differences(cuda):
     """Reference gradient: central differences of the FP64 CPU oracle's loss (same estimator, same
-    random numbers, double precision), albedo of the 4 largest-gradient triangles."""
+    random numbers, double precision, light-selection table held fixed as on the device) for the 8
+    largest albedo components and every channel of the two emitter triangles, within 1e-2 relative.  64 spp: paths whose float and double versions
+    diverge (a hit decided differently near an edge) add noise that falls as 1/sqrt(paths)."""
     sc, cam, p, tris, mat, mats, albedo, emission, rough, target_alb = _setup(cuda)
+    p = dr.render_params(W, H, dr.MODE_PHYSICAL, samples=(8, 8), max_bounces=DEPTH, seed=3)
     n = len(tris)
-    osc = O.OracleScene(tris, mat_id=mat, materials=mats)
+    osc = O.OracleScene(tris, mat_id=mat, materials=mats, threads=16)
     osc.set_triangle_params(target_alb, emission, rough)
-    t_or = osc.render_blocks(cam, p).astype(np.float64)
+    t_or = osc.render_blocks(cam, p, threads=16).astype(np.float64)
     osc.set_triangle_params(albedo, emission, rough)
-    img_or = osc.render_blocks(cam, p).astype(np.float64)
+    # the device's light-selection table stays as built at scene creation while parameters are
+    # written in place; the oracle keeps its own fixed from here, so both differentiate one estimator
+    osc.freeze_sampling()
+    img_or = osc.render_blocks(cam, p, threads=16).astype(np.float64)
     img = _render(sc, cam, p, cuda)
-    # the adjoint weights come from the GPU image; the oracle's own loss uses its own image
+    # the adjoint weights come from the oracle's image: both sides differentiate the same loss
     dl = torch.zeros_like(img)
     dl[:, :3] = torch.from_numpy(2.0 * (img_or[:, :3] - t_or[:, :3])).float().to(cuda)
     ga = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
     ge = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
-    dr.Renderer(1 << 14).render_adjoint(sc, cam, dl, 0, dr.block_count(W, H), p, ga, ge)
+    dr.Renderer(1 << 16).render_adjoint(sc, cam, dl, 0, dr.block_count(W, H), p, ga, ge)
     torch.cuda.synchronize()
-    ga_h = ga.cpu().numpy()
-    for f in np.argsort(-np.abs(ga_h).ravel())[:4]:
+    ga_h, ge_h = ga.cpu().numpy(), ge.cpu().numpy()
+
+    def oracle_loss(alb, emi):
+        osc.set_triangle_params(alb, emi, rough)
+        im = osc.render_blocks(cam, p, threads=16).astype(np.float64)
+        return float(((im[:, :3] - t_or[:, :3]) ** 2).sum())
+
+    rows = []
+    for f in np.argsort(-np.abs(ga_h).ravel())[:8]:
         k, ch = divmod(int(f), 3)
-        hstep = 1e-3
         vals = []
         for sgn in (1, -1):
             a2 = albedo.copy()
-            a2[k, ch] += sgn * hstep
-            osc.set_triangle_params(a2, emission, rough)
-            im = osc.render_blocks(cam, p).astype(np.float64)
-            vals.append(float(((im[:, :3] - t_or[:, :3]) ** 2).sum()))
-        fd = (vals[0] - vals[1]) / (2 * hstep)
-        assert abs(ga_h[k, ch] - fd) <= 2e-2 * abs(fd) + 1e-6, (k, ch, ga_h[k, ch], fd)
+            a2[k, ch] += sgn * 1e-3
+            vals.append(oracle_loss(a2, emission))
+        rows.append(("albedo", k, ch, float(ga_h[k, ch]), (vals[0] - vals[1]) / 2e-3))
+    for k in range(n - 2, n):
+        for ch in range(3):
+            vals = []
+            for sgn in (1, -1):
+                e2 = emission.copy()
+                e2[k, ch] += sgn * 1e-2
+                vals.append(oracle_loss(albedo, e2))
+            rows.append(("emission", k, ch, float(ge_h[k, ch]), (vals[0] - vals[1]) / 2e-2))
+    _fd_report("32x32 vs FP64 FD", rows)
+    for name, k, ch, adj, fd in rows:
+        assert abs(adj - fd) <= 1e-2 * abs(fd) + 1e-6, (name, k, ch, adj, fd)
 
 
 def test_c5_workload_gradient_vs_fp64_oracle_fd(cuda):
     """The differentiable workload itself (icosphere L7 + box room, 327,692 triangles, per-triangle albedo
-    U[0.1, 0.9], emission 10 on 64 triangles, 512x512, 16 spp, depth 5) on a 16-block range at the image
-    centre: adjoint gradients of the L2 loss against central differences (h = 1e-3) of the FP64 oracle's
-    loss for the 4 largest albedo components, within 2e-2 relative."""
+    U[0.1, 0.9], emission 10 on 64 triangles, 512x512, 16 spp, depth 5) on a 64-block range at the image
+    centre (8,192 pixels): adjoint gradients of the L2 loss against central differences (h = 1e-3) of
+    the FP64 oracle's loss for the 8 largest albedo components, within 1e-2 relative."""
     S = scenes.differentiable_scene(7)
     tris, n = S["tris"], len(S["tris"])
     mats = [dr.lambert()]
     sc = dr.Scene(tris, mat_id=S["mat_id"], materials=mats, box_epsilon=dr.PHYSICAL_TREE)
     sc.set_triangle_params(S["albedo"], S["emission"], S["roughness"])
-    osc = O.OracleScene(tris, mat_id=S["mat_id"], materials=mats)
+    osc = O.OracleScene(tris, mat_id=S["mat_id"], materials=mats, threads=16)
     cam = dr.camera(dr.LENS_PINHOLE, position=(0.0, 0.0, -0.99), angle=60.0)
     p = dr.render_params(512, 512, dr.MODE_PHYSICAL, samples=(4, 4), max_bounces=5, seed=7)
-    s0 = 16 * 64 + 24
-    s1 = s0 + 16
-    rows = slice(s0 * 128, s1 * 128)
+    bw = dr.block_count(512, 512) // 32            # blocks per block row (64)
+    ranges = [((14 + r) * bw + 16, (14 + r) * bw + 32) for r in range(4)]     # 4 rows x 16 blocks
+
+    def oracle_image():
+        fb = np.zeros((dr.block_count(512, 512) * 128, 4), np.float32)
+        for s0, s1 in ranges:
+            osc.render_blocks(cam, p, fb=fb, start=s0, end=s1, threads=16)
+        return fb.astype(np.float64)
+
+    mask = np.zeros(dr.block_count(512, 512) * 128, bool)
+    for s0, s1 in ranges:
+        mask[s0 * 128:s1 * 128] = True
     osc.set_triangle_params(S["albedo_target"], S["emission"], S["roughness"])
-    t_or = osc.render_blocks(cam, p, start=s0, end=s1).astype(np.float64)
+    t_or = oracle_image()
     osc.set_triangle_params(S["albedo"], S["emission"], S["roughness"])
-    i_or = osc.render_blocks(cam, p, start=s0, end=s1).astype(np.float64)
-    dl = torch.zeros((dr.block_count(512, 512) * 128, 4), dtype=torch.float32, device=cuda)
-    dl[rows, :3] = torch.from_numpy(2.0 * (i_or[rows, :3] - t_or[rows, :3])).float().to(cuda)
+    i_or = oracle_image()
+    dl_h = np.zeros((len(mask), 4), np.float32)
+    dl_h[mask, :3] = 2.0 * (i_or[mask, :3] - t_or[mask, :3])
+    dl = torch.from_numpy(dl_h).to(cuda)
     ga = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
     ge = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
-    dr.Renderer(1 << 16).render_adjoint(sc, cam, dl, s0, s1, p, ga, ge)
+    rend = dr.Renderer(1 << 18)
+    for s0, s1 in ranges:
+        rend.render_adjoint(sc, cam, dl, s0, s1, p, ga, ge)
     torch.cuda.synchronize()
     ga_h = ga.cpu().numpy()
     assert float(np.abs(ga_h).sum()) > 0 and float(ge.abs().sum()) > 0
-    for f in np.argsort(-np.abs(ga_h).ravel())[:4]:
+    rows = []
+    for f in np.argsort(-np.abs(ga_h).ravel())[:8]:
         k, ch = divmod(int(f), 3)
         vals = []
         for sgn in (1, -1):
             a2 = S["albedo"].copy()
             a2[k, ch] += sgn * 1e-3
             osc.set_triangle_params(a2, S["emission"], S["roughness"])
-            im = osc.render_blocks(cam, p, start=s0, end=s1).astype(np.float64)
-            vals.append(float(((im[rows, :3] - t_or[rows, :3]) ** 2).sum()))
-        fd = (vals[0] - vals[1]) / 2e-3
-        assert abs(ga_h[k, ch] - fd) <= 2e-2 * abs(fd) + 1e-6, (k, ch, ga_h[k, ch], fd)
+            im = oracle_image()
+            vals.append(float(((im[mask, :3] - t_or[mask, :3]) ** 2).sum()))
+        rows.append(("albedo", k, ch, float(ga_h[k, ch]), (vals[0] - vals[1]) / 2e-3))
+    _fd_report("C5 workload vs FP64 FD", rows)
+    for name, k, ch, adj, fd in rows:
+        assert abs(adj - fd) <= 1e-2 * abs(fd) + 1e-6, (name, k, ch, adj, fd)
 
 
 def test_autograd_harness(cuda):

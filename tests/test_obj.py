@@ -109,7 +109,8 @@ def test_reference_failures_and_quirks(tmp_path, text):
 
 
 def test_reference_example_mesh_if_present():
-    p = Path("/root/reference/example_scenes/0/files/cargo.obj")
+    # the reference's example mesh, copied next to the compiled reference by oracle/build_ref.sh
+    p = Path(__file__).resolve().parents[1] / "oracle" / "_ref" / "example_scenes" / "0" / "files" / "cargo.obj"
     if not p.exists():
         pytest.skip("reference example scene not present")
     ours = _same(p)

@@ -24,6 +24,28 @@ def test_oracle_cast_matches_reference_golden(fixture, culls):
         assert np.array_equal(t[hit].view(np.int32), ref_t[hit].view(np.int32))  # bit-exact t
 
 
+def test_oracle_cast_matches_reference_golden_level8():
+    """The ray-cast microbenchmark mesh itself (level-8 displaced icosphere, 1,310,720 triangles) on the
+    reference's octree: node count and the reference's hits (index and t bit-exact) on the golden
+    subset of the benchmark's rays, culling on and off."""
+    sys_path_golden()
+    from make_golden import c2_rays, mesh_sha256
+    from dumbray_gb300 import scenes
+    g = np.load(GOLD / "cast_c2_l8.npz")
+    tris = scenes.displaced_icosphere(8, 0.1, 1)
+    assert mesh_sha256(tris) == str(g["mesh_sha256"])
+    o, d = c2_rays()
+    assert np.array_equal(o, g["o"]) and np.array_equal(d, g["d"])
+    osc = O.OracleScene(tris)
+    assert osc.node_count() == int(g["nodes"])
+    for cull in (1, 0):
+        idx, t, _, _ = osc.cast(o, d, cull=bool(cull))
+        ref_idx, ref_t = g[f"idx_cull{cull}"], g[f"t_cull{cull}"]
+        assert np.array_equal(idx, ref_idx)
+        hit = ref_idx >= 0
+        assert np.array_equal(t[hit].view(np.int32), ref_t[hit].view(np.int32))
+
+
 @pytest.mark.skipif(not O.reference_available(), reason="reference library not built here")
 def test_oracle_cast_matches_live_reference():
     from dumbray_gb300 import scenes

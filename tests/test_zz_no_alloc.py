@@ -1,8 +1,8 @@
 """dr_render_blocks_noalloc against dr_render_blocks.
 
 The allocation-free entry point serves callers that cannot allocate device memory while they
-render (inside a CUDA stream capture, under another owner's memory pool, or on a thread where
-cudaMalloc's implicit device synchronisation is not acceptable).  It must produce the same frame
+render (under another owner's memory pool or fixed budget, or on a thread where cudaMalloc's
+implicit device synchronisation is not acceptable).  It must produce the same frame
 buffer as the regular entry point - same paths, same blending - on consecutive calls, which share
 (and must correctly re-clear) its fixed scratch array.  Tolerance: the same per-pixel comparison
 as the other render tests (accumulation order of float atomics may differ).
@@ -28,31 +28,40 @@ def _compare(gpu, ref, tol_rel=2e-3, max_bad_frac=0.02):
     assert bad.mean() <= max_bad_frac, f"{bad.mean():.4f} of channels differ"
 
 
-def _scene(mode):
+def _scene(kind):
+    """(scene, camera, mode) of each covered case: reference semantics with a sphere light and a soft
+    directional light (SimpleStochastic lens), the same room through the spherical-segment lens, a
+    spotlight room (16-photon disc emitter with shadows), and the physical mode."""
     room = scenes.box((2, 2, 2), inward=True)
     sph = scenes.icosphere(3, 0.5)
     tris = np.concatenate([room, sph])
     mat = np.zeros(len(tris), np.int32)
     mat[len(room):] = 1
-    if mode == dr.MODE_REFERENCE:
+    if kind != "physical":
         mats = [dr.dumb_based(diffuse=(0.7, 0.7, 0.7), metal=0.0), dr.simple_stochastic((0.9, 0.8, 0.7), 0.3, 0.7, 8.0)]
         lights = [dr.spherical_light((1.5, 1.5, 1.5), (0.0, 0.8, 0.0), 0.1),
                   dr.soft_directional_light((0.4, 0.4, 0.6), (0.2, -1.0, 0.1), 3.0, 0.05)]
         cam = dr.camera(dr.LENS_SIMPLE_STOCHASTIC, position=(0.0, 0.0, -0.95), angle=60.0)
-        return dr.Scene(tris, mat_id=mat, materials=mats, lights=lights), cam
+        if kind == "segment_lens":
+            cam = dr.camera(dr.LENS_SPHERICAL_SEGMENT, position=(0.0, 0.0, -0.95), angle=(70.0, 50.0),
+                            focal_distance=2.0, softness=0.01, filter=(1.0, 0.9, 0.8))
+        elif kind == "spotlight":
+            lights = [dr.spotlight((1.0, 0.95, 0.9), 150.0, (0.3, 0.7, -0.4), (-0.2, -1.0, 0.3), 20.0, 50.0, 2.0, 0.15,
+                                   emit_from_sphere=False, cast_shadows=True, samples=16)]
+        return dr.Scene(tris, mat_id=mat, materials=mats, lights=lights), cam, dr.MODE_REFERENCE
     c = scenes.box_and_icosphere(3)
     mats = [dr.lambert((0.7, 0.7, 0.7)), dr.glossy((0.8, 0.6, 0.4), 0.2),
             dr.lambert((0.0, 0.0, 0.0), emission=(10.0, 10.0, 10.0))]
     cam = dr.camera(dr.LENS_PINHOLE, position=(0.0, 0.0, -0.99), angle=60.0)
-    return dr.Scene(c["tris"], mat_id=c["mat_id"], materials=mats), cam
+    return dr.Scene(c["tris"], mat_id=c["mat_id"], materials=mats), cam, dr.MODE_PHYSICAL
 
 
-@pytest.mark.parametrize("mode", [dr.MODE_REFERENCE, dr.MODE_PHYSICAL])
-def test_noalloc_matches_render_blocks_on_consecutive_calls(mode):
+@pytest.mark.parametrize("kind", ["reference", "segment_lens", "spotlight", "physical"])
+def test_noalloc_matches_render_blocks_on_consecutive_calls(kind):
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     dev = torch.device("cuda:0")
-    scene, cam = _scene(mode)
+    scene, cam, mode = _scene(kind)
     W, H = 72, 40
     nb = dr.block_count(W, H)
     fb_ref = dr.new_frame_buffer(W, H, dev)
@@ -74,7 +83,7 @@ def test_noalloc_rejects_ranges_beyond_its_scratch():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     dev = torch.device("cuda:0")
-    scene, cam = _scene(dr.MODE_REFERENCE)
+    scene, cam, _ = _scene("reference")
     W, H = 1024, 512   # 4096 blocks > DR_NOALLOC_MAX_BLOCKS
     fb = dr.new_frame_buffer(W, H, dev)
     p = dr.render_params(W, H, dr.MODE_REFERENCE)
