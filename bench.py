@@ -64,6 +64,12 @@ def parse():
     ap.add_argument("--no-raycast", action="store_true", help="skip the ray-cast microbenchmark leg")
     ap.add_argument("--no-twin", action="store_true", help="skip the reference-mode twin leg")
     ap.add_argument("--no-c1", action="store_true", help="skip the 256x256 plain path-trace leg")
+    ap.add_argument("--twin-only", action="store_true",
+                    help="profiling case: run only the reference-mode twin leg (at --twin-size / --twin-spp) and print it")
+    ap.add_argument("--twin-size", default="1920x1080", help="reference-mode twin resolution WxH")
+    ap.add_argument("--twin-spp", type=int, default=64, help="reference-mode twin samples per pixel (a square)")
+    ap.add_argument("--twin-tree", default="reference", choices=["reference", "physical"],
+                    help="octree padding of the reference-mode twin scene")
     ap.add_argument("--lanes", type=int, default=0, help="concurrent wave pipelines per renderer (0 = library default)")
     ap.add_argument("--split", type=int, default=12,
                     help="octree leaf split threshold of the path-trace scene (12: best of 8/12/16/24 on this "
@@ -600,18 +606,20 @@ def run_reference_twin_gpu(dr, torch, dev, a, S, peak, peak_src):
     time; cpu_baseline: the reference DumbRenderer itself on a 240x136 x 1 spp sample of the frame."""
     tris, mat, mats, lights = reference_twin(S, dr)
     t0 = time.time()
-    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights, device_build=True)
+    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights, device_build=True,
+                  box_epsilon=dr.PHYSICAL_TREE if a.twin_tree == "physical" else 0.0)
     build_s = time.time() - t0
     cam = dr.camera(dr.LENS_SIMPLE_STOCHASTIC, position=(0.0, 0.6, -3.4), angle=60.0)
-    W, H = 1920, 1080
-    spp = 64
+    W, H = (int(v) for v in a.twin_size.split("x"))
+    sx, sy = samples_xy(a.twin_spp)
+    spp = sx * sy
     nb = dr.block_count(W, H)
     fb = dr.new_frame_buffer(W, H, dev)
     rend = dr.Renderer(a.wave, a.lanes)
     stream = torch.cuda.current_stream()
 
     def params(i):
-        return dr.render_params(W, H, dr.MODE_REFERENCE, samples=(8, 8), max_bounces=a.depth, iteration=1 + i, seed=77)
+        return dr.render_params(W, H, dr.MODE_REFERENCE, samples=(sx, sy), max_bounces=a.depth, iteration=1 + i, seed=77)
 
     rend.render_blocks(sc, cam, fb, 0, nb, params(0), stream)
     K = max(2, min(3, a.steps))
@@ -655,7 +663,7 @@ def run_reference_twin_gpu(dr, torch, dev, a, S, peak, peak_src):
     shadow_ms = kbusy["shadow"] / K
     achieved = casts * bpr / (shadow_ms / 1e3) / 1e9 if shadow_ms > 0 else 0.0
     out = {"workload": f"reference-expressible twin ({len(tris):,} tris, {len(lights)} spherical lights), reference mode "
-                       f"(DumbRenderer's estimator), {W}x{H} x {spp} spp, depth {a.depth}, reference octree",
+                       f"(DumbRenderer's estimator), {W}x{H} x {spp} spp, depth {a.depth}, {a.twin_tree} octree",
            "mpaths_s": round(value, 3), "ms_per_frame": round(ms, 2), "frames": K,
            "e2e": {"value": round(e2e, 3), "unit": UNIT, "h2d_bytes_per_step": int(fb.numel() * 4),
                    "d2h_bytes_per_step": int(fb.numel() * 4)},
@@ -669,7 +677,7 @@ def run_reference_twin_gpu(dr, torch, dev, a, S, peak, peak_src):
            "kernel_busy_ms_per_frame": {k: round(v / K, 2) for k, v in kbusy.items()},
            "kernel_launch_ms_sum_per_frame": {k: round(v[0] / K, 2) for k, v in kt.items()},
            "scene_build_s": round(build_s, 2)}
-    ref = time_reference_renderer(tris, mat, mats, lights, cam, a.depth, steps=3, warmup=1)
+    ref = None if a.twin_only else time_reference_renderer(tris, mat, mats, lights, cam, a.depth, steps=3, warmup=1)
     if ref is not None:
         sec, rbuild, threads, rpaths = ref
         rv = rpaths / sec / 1e6
@@ -1071,6 +1079,15 @@ def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.twin_only:
+        import torch
+        import dumbray_gb300 as dr
+        from dumbray_gb300 import scenes
+        torch.cuda.set_device(0)
+        peak, peak_src = measured_peak()
+        out = run_reference_twin_gpu(dr, torch, torch.device("cuda", 0), a, scenes.full_scene(level=a.level, seed=1),
+                                     peak, peak_src)
+        print(json.dumps(out), flush=True)
     else:
         run_ours(a)
 

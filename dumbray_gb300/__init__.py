@@ -85,7 +85,8 @@ class DrLight(ctypes.Structure):
 class DrCamera(ctypes.Structure):
     _fields_ = [("lens", ctypes.c_int32), ("angle", ctypes.c_float * 2), ("focal_distance", ctypes.c_float),
                 ("softness", ctypes.c_float), ("filter", _F3), ("position", _F3), ("right", _F3), ("up", _F3),
-                ("forward", _F3), ("origin_rows", ctypes.c_int32), ("row_x", _F3), ("row_y", _F3), ("row_z", _F3)]
+                ("forward", _F3), ("origin_rows", ctypes.c_int32), ("row_x", _F3), ("row_y", _F3), ("row_z", _F3),
+                ("lens_x", ctypes.c_float)]
 
 
 class DrRenderParams(ctypes.Structure):

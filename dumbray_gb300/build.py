@@ -1,9 +1,15 @@
 """In-tree build of the native library ``dumbray_gb300/_build/libdumbray_gb300.so``.
 
 nvcc compiles the CUDA translation units for sm_103a only; the host octree builder is plain C++.
-Translation units compile in parallel; no cmake, no torch extension machinery.  FP contraction is
-disabled everywhere (device: ``-fmad=false``; host: ``-ffp-contract=off``) so the octree build and
-cast round exactly like DumbRay's host code on both x86-64 and aarch64.
+Translation units compile in parallel; no cmake, no torch extension machinery.
+
+FP contraction: host code is compiled with ``-ffp-contract=off`` (the host octree build rounds like
+DumbRay's host code on x86-64 and aarch64, where gcc would otherwise fuse multiply-adds).  On the
+device only the GPU octree builder (``octree_gpu.cu``, sharing its plain-operator geometry with the
+host builder through ``octree_geom.h``) is compiled with ``-fmad=false``, so its tree stays
+bit-identical to the host build.  The cast predicate and the traversal are written with explicitly
+rounded intrinsics (``__fadd_rn`` / ``__fmul_rn`` / ``__fdiv_rn`` / ``__fsqrt_rn``), which the compiler
+never contracts, so the render and adjoint kernels may fuse multiply-adds elsewhere.
 """
 from __future__ import annotations
 
@@ -19,6 +25,7 @@ CSRC = HERE / "csrc"
 OUT = HERE / "_build"
 LIB = OUT / "libdumbray_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NO_FMAD = {"octree_gpu.cu"}   # translation units whose bit-exactness rests on plain operators
 
 
 def _nvcc() -> str:
@@ -53,12 +60,13 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     OUT.mkdir(parents=True, exist_ok=True)
     nvcc = _nvcc()
     inc = ["-I", str(HERE.parent / "include")]
-    cu_flags = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
+    cu_flags = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
                 "-Xptxas", "-v"] + ARCH + inc
     jobs = []
     for src in sorted(CSRC.glob("*.cu")):
         obj = OUT / (src.stem + ".o")
-        jobs.append([nvcc, "-c", str(src), "-o", str(obj)] + cu_flags)
+        fmad = ["-fmad=false"] if src.name in NO_FMAD else ["-fmad=true"]
+        jobs.append([nvcc, "-c", str(src), "-o", str(obj)] + cu_flags + fmad)
     for src in sorted(CSRC.glob("*.cpp")):
         obj = OUT / (src.stem + ".o")
         jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-pthread", "-c", str(src), "-o", str(obj)] + inc)

@@ -787,7 +787,7 @@ dr_status dr_internal_make_item(const dr_scene *sc, const dr_camera *cam, float 
         if (angle < 1.0f) angle = 1.0f;
         else if (angle > 179.0f) angle = 179.0f;
         float radian = (angle / (2 * 57.29577951308233f));
-        I.cam_x = 0.5f / std::tan(radian);
+        I.cam_x = (cam->lens_x > 0.0f) ? cam->lens_x : 0.5f / std::tan(radian);
     }
     I.mode = p->mode;
     I.width = p->width;

@@ -164,7 +164,12 @@ typedef struct {
  * directions keep the right / up / forward combination (Transform::direction, Transform.impl.h:166).
  * The two differ for a rotated camera (the rows are the transpose of the direction basis, times the
  * scale); only the spherical-segment lens has origins off the camera position.  Zero-initialised
- * cameras keep the basis mapping. */
+ * cameras keep the basis mapping.
+ * lens_x > 0: the focal factor of DR_LENS_DEFAULT_PERSPECTIVE / DR_LENS_SIMPLE_STOCHASTIC used as
+ * given (the `x` a reference lens stores, DefaultPerspectiveLense.impl.cuh:5-9,
+ * SimpleStochasticLense.impl.cuh:4-9), so a host that holds constructed reference lenses passes
+ * them on exactly; 0 (zero-initialised): 0.5 / tan(angle[0] / 2), angle clamped to [1, 179]
+ * degrees, as the lens constructors compute it. */
 #define DR_LENS_DEFAULT_PERSPECTIVE 0
 #define DR_LENS_SIMPLE_STOCHASTIC 1
 #define DR_LENS_SPHERICAL_SEGMENT 2
@@ -186,6 +191,7 @@ typedef struct {
     float row_x[3];
     float row_y[3];
     float row_z[3];
+    float lens_x;
 } dr_camera;
 
 /* ---- render parameters ---------------------------------------------------------------------

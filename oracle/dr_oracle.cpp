@@ -1543,7 +1543,7 @@ void dro_render_blocks(void *h, const dr_camera *camera, const dr_render_params 
         if (angle < 1) angle = 1;
         else if (angle > 179) angle = 179;
         float radian = (angle / (2 * RADIAN_F));
-        cam.x = 0.5f / std::tan(radian);
+        cam.x = (camera->lens_x > 0.0f) ? camera->lens_x : 0.5f / std::tan(radian);
     }
     int W = p->width, H = p->height;
     int bw = (W + DR_BLOCK_W - 1) / DR_BLOCK_W;

@@ -12,6 +12,7 @@
 //   SphericalLightEmitter / SimpleSoftDirectionalLight / SimpleDirectionalLight / Spotlight   __source__/DataStructures/Objects/Scene/Lights/*
 //   DefaultPerspectiveLense / SimpleStochasticLense / Lenses::SphericalSegmentLense  __source__/DataStructures/Objects/Components/Lenses/*
 #include "DataStructures/Renderers/DumbRenderer/DumbRenderer.cuh"
+#include "ref_driver.h"
 #include "DataStructures/Screen/FrameBuffer/BlockBasedFrameBuffer/BlockBasedFrameBuffer.cuh"
 #include "DataStructures/Objects/Components/Shaders/DumbBasedShader/DumbBasedShader.cuh"
 #include "DataStructures/Objects/Components/Shaders/SimpleStochasticShader/SimpleStochasticShader.cuh"
@@ -167,10 +168,6 @@ void dref_octree_cast(void *h, const float *o, const float *d, int n, int clip, 
 //   camera: [0]=lens (0 DefaultPerspectiveLense, 1 SimpleStochasticLense, 2 SphericalSegmentLense)
 //     [1] angle (deg) / [1..2] alpha for spherical, [3] focal distance, [4] softness, [5..7] filter,
 //     [8..10] position, [11..13] euler angles (deg)
-struct RefScene {
-	TriScene scene;
-	DumbRenderer::CameraManager camera;
-};
 
 // uv: per-corner texture coordinates float[n][3][2] or NULL (the fixed (0,0) (1,0) (0,1) corners).
 void *dref_scene_create_uv(const float *xyz, const float *nrm, const float *uv, const int *mat, int n,
