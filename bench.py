@@ -78,7 +78,7 @@ def parse():
                     help="build the path-trace scene with the reference's octree padding (1.28e-3) instead of the "
                          "physical-mode padding scaled to the coordinates")
     ap.add_argument("--batch-scenes", type=int, default=64)
-    ap.add_argument("--batch-steps", type=int, default=2, help="timed steps of each batched arm")
+    ap.add_argument("--batch-steps", type=int, default=5, help="timed steps of each batched arm")
     return ap.parse_args()
 
 
@@ -831,6 +831,7 @@ def run_batched(dr, torch, dev, a):
     items = [(tuned[i], cams[i], params(j, 1), fbs[i], 0, nbs[i]) for i, j in enumerate(jobs)]
     sub = dr.Batch(items[::4])
     best_wave, wave_table, brend = autotune.tune_wave(sub, lanes=a.lanes)
+    best_shape, shape_table = autotune.tune_block_shape(sub, brend)
     sub.close()
     tune_s = time.time() - t0
 
@@ -844,6 +845,7 @@ def run_batched(dr, torch, dev, a):
 
     batch_ms = _events_ms(torch, batch_step, K)
     batch_launches = brend.launches() - l0
+    classes = batch_classes(dr, torch, jobs, tuned, cams, fbs, nbs, params, brend, K)
     batch_means = np.array([fb[:, :3].double().mean().item() for fb in fbs])
     rel = np.abs(batch_means - plain_means) / np.maximum(np.abs(plain_means), 1e-9)
     # FP64 oracle error of a sample of jobs: the 4 cheapest for the oracle (paths x depth plus tree
@@ -886,8 +888,11 @@ def run_batched(dr, torch, dev, a):
         "autotune": {"leaf_split_by_class": {str(autotune.SIZE_CLASSES[k]) if k < len(autotune.SIZE_CLASSES)
                                              else "inf": v for k, v in sorted(best_split.items())},
                      "leaf_probe_ms": {str(k): v for k, v in split_table.items()},
-                     "wave": best_wave, "wave_probe_ms": {str(k): v for k, v in wave_table.items()}},
+                     "wave": best_wave, "wave_probe_ms": {str(k): v for k, v in wave_table.items()},
+                     "block_shape": ["256x3", "128x6"][best_shape],
+                     "block_shape_probe_ms": {["256x3", "128x6"][k]: v for k, v in shape_table.items()}},
         "job_mean_max_rel_diff_batched_vs_plain": float(rel.max()),
+        "by_size_class": classes,
         "accuracy_vs_fp64_oracle": dict(acc, sample="4 jobs (the cheapest for the oracle of each resolution), "
                                                     "whole image, iteration 1 at the job's spp, same seeds"),
         "host_s": {"generate": round(gen_s, 1), "build": round(build_s, 1), "autotune": round(tune_s, 1)},
@@ -897,6 +902,56 @@ def run_batched(dr, torch, dev, a):
     brend.close()
     for sc in tuned:
         sc.close()
+    return out
+
+
+BATCH_CLASSES = ((0, 1 << 20, "<=1M paths"), (1 << 20, 1 << 24, "1M-16M paths"), (1 << 24, 1 << 62, ">16M paths"))
+
+
+def batch_classes(dr, torch, jobs, scenes, cams, fbs, nbs, params, rend, K):
+    """Where the batch's time goes, by job size (paths per frame): for each class the jobs' share of
+    the paths, their scene-by-scene time (plain dr_render_blocks launches, the same renderer and
+    scenes as the batch) and the same jobs as a batch of their own, K timed iterations each; and the
+    bound this puts on the whole batch's speed-up (only the time a class loses to plain launches can
+    be recovered)."""
+    out = {}
+    t_plain_total = 0.0
+    t_batch_total = 0.0
+    for lo, hi, name in BATCH_CLASSES:
+        idx = [i for i, j in enumerate(jobs) if lo < j["width"] * j["height"] * j["spp"] <= hi]
+        if not idx:
+            continue
+        paths = sum(jobs[i]["width"] * jobs[i]["height"] * jobs[i]["spp"] for i in idx)
+
+        def plain_step(k):
+            for i in idx:
+                rend.render_blocks(scenes[i], cams[i], fbs[i], 0, nbs[i], params(jobs[i], 2 + k))
+
+        plain_step(0)
+        t_plain = _events_ms(torch, plain_step, K) / K
+        sub = dr.Batch([(scenes[i], cams[i], params(jobs[i], 1), fbs[i], 0, nbs[i]) for i in idx])
+        sub.render(rend, use_graph=True)
+
+        def sub_step(k):
+            sub.set_iteration(2 + k)
+            sub.render(rend, use_graph=True)
+
+        t_batch = _events_ms(torch, sub_step, K) / K
+        sub.close()
+        t_plain_total += t_plain
+        t_batch_total += t_batch
+        out[name] = {"jobs": len(idx), "paths": int(paths), "plain_ms": round(t_plain, 2), "batched_ms": round(t_batch, 2),
+                     "plain_mpaths_s": round(paths / (t_plain / 1e3) / 1e6, 2),
+                     "batched_mpaths_s": round(paths / (t_batch / 1e3) / 1e6, 2),
+                     "speedup": round(t_plain / t_batch, 3)}
+    for v in out.values():
+        v["share_of_plain_time"] = round(v["plain_ms"] / max(t_plain_total, 1e-9), 4)
+    # upper bound of the whole batch's speed-up if every class ran at the fastest per-path rate any
+    # class reaches, batched or not
+    total_paths = sum(v["paths"] for v in out.values())
+    best_rate = max(max(v["plain_mpaths_s"], v["batched_mpaths_s"]) for v in out.values())
+    out["bound"] = {"plain_ms_sum": round(t_plain_total, 2), "class_batches_ms_sum": round(t_batch_total, 2),
+                    "speedup_if_every_class_ran_at_best_rate": round(t_plain_total / (total_paths / best_rate / 1e3), 3)}
     return out
 
 

@@ -168,6 +168,10 @@ def lib() -> ctypes.CDLL:
     L.dr_renderer_set_lanes.argtypes = [vp, i32]
     L.dr_renderer_lanes.restype = i32
     L.dr_renderer_lanes.argtypes = [vp]
+    L.dr_renderer_set_block_shape.restype = i32
+    L.dr_renderer_set_block_shape.argtypes = [vp, i32]
+    L.dr_renderer_block_shape.restype = i32
+    L.dr_renderer_block_shape.argtypes = [vp]
     L.dr_renderer_set_counting.restype = i32
     L.dr_renderer_set_counting.argtypes = [vp, i32]
     L.dr_renderer_counters.restype = i32
@@ -626,6 +630,14 @@ class Renderer:
     def set_lanes(self, lanes: int):
         """Concurrent wave pipelines of one render (dr_renderer_set_lanes)."""
         check(lib().dr_renderer_set_lanes(self._h, int(lanes)))
+
+    def set_block_shape(self, shape: int):
+        """Traversal block shape (dr_renderer_set_block_shape): 0 = 256 x 3, 1 = 128 x 6 per SM."""
+        check(lib().dr_renderer_set_block_shape(self._h, int(shape)))
+
+    @property
+    def block_shape(self) -> int:
+        return int(lib().dr_renderer_block_shape(self._h))
 
     @property
     def lanes(self) -> int:

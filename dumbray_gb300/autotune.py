@@ -7,7 +7,8 @@ Picks, by timing short renders on the GPU:
     a reference-mode scene keeps 8 because its casts must match the reference tree bit for bit.
     Larger leaves trade child-box tests for triangle tests, which the cooperative warp-wide leaf
     rounds run well, so the best value depends on the triangle density of the scene.
-  * the wave size (paths in flight per wave = queue capacity of the renderer) of a batch.
+  * the wave size (paths in flight per wave = queue capacity of the renderer) of a batch;
+  * the block shape of the traversal kernels (256 threads x 3 blocks or 128 x 6 per SM).
 
 Each probe is timed with CUDA events after one untimed render; the measured table is returned
 with the choice so callers can report it.
@@ -91,6 +92,18 @@ def tune_wave(batch, candidates=(1 << 20, 1 << 21, 1 << 22, 1 << 23, 1 << 24), u
         else:
             r.close()
     return best, table, best_r
+
+
+def tune_block_shape(batch, renderer, shapes=(0, 1), use_graph=True):
+    """Times one batch render with each traversal block shape on `renderer` (dr_renderer_set_block_shape);
+    leaves the renderer on the fastest and returns (best, {shape: ms})."""
+    table = {}
+    for sh in shapes:
+        renderer.set_block_shape(sh)
+        table[sh] = round(_time_ms(lambda: batch.render(renderer, use_graph=use_graph), reps=1), 2)
+    best = min(table, key=table.get)
+    renderer.set_block_shape(best)
+    return best, table
 
 
 def representatives(jobs, n_tris):

@@ -157,6 +157,7 @@ struct dr_renderer {
     // one render and adding into the same accumulator (one kernel's tail overlaps another
     // pipeline's work).  Extra lanes are allocated on first use.
     int lanes = 1;
+    int shape = 0;                  // traversal block shape (dr_renderer_set_block_shape)
     std::vector<WaveScratch> extra;
     cudaEvent_t fork = nullptr;
     // Identifies the current set of scratch buffers: a new value at creation and whenever a buffer a
@@ -718,6 +719,17 @@ dr_status dr_renderer_set_lanes(dr_renderer *r, int32_t lanes) try {
 
 int32_t dr_renderer_lanes(const dr_renderer *r) { return r ? r->lanes : 0; }
 
+dr_status dr_renderer_set_block_shape(dr_renderer *r, int32_t shape) try {
+    if (!r) return fail(DR_E_ARG, "dr_renderer_set_block_shape: renderer is NULL");
+    if (shape < 0 || shape > 1) return fail(DR_E_ARG, "dr_renderer_set_block_shape: shape must be 0 or 1");
+    r->shape = shape;
+    return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_renderer_set_block_shape");
+}
+
+int32_t dr_renderer_block_shape(const dr_renderer *r) { return r ? r->shape : -1; }
+
 dr_status dr_renderer_kernel_times(dr_renderer *r, double *ms, int64_t *launches) try {
     if (!r) return fail(DR_E_ARG, "dr_renderer_kernel_times: renderer is NULL");
     cudaError_t e = r->prof.harvest();
@@ -844,6 +856,7 @@ static void wave_buffers(dr_renderer *r, drk::WaveDesc &W) {
     W.accum = r->accum;
     W.ctrl = r->ctrl;
     W.prefix = r->prefix;
+    W.shape = r->shape;
 }
 
 // Wave size for `lanes` concurrent pipelines: at most `wave`, and small enough that a render of
@@ -1020,6 +1033,7 @@ struct dr_batch {
     unsigned long long graph_scratch = 0;   // scratch_id of the renderer the graph was captured with
     long long graph_wave = 0;
     int graph_lanes = 0;
+    int graph_shape = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     long long graph_launches = 0;
@@ -1211,7 +1225,8 @@ dr_status dr_batch_render(dr_renderer *r, dr_batch *b, int32_t use_graph, void *
         if (st == DR_OK) cudaEventRecord(b->done, stream);
         return st;
     }
-    if (b->exec == nullptr || b->graph_scratch != r->scratch_id || b->graph_wave != wave || b->graph_lanes != lanes) {
+    if (b->exec == nullptr || b->graph_scratch != r->scratch_id || b->graph_wave != wave || b->graph_lanes != lanes ||
+        b->graph_shape != r->shape) {
         // lane scratch is allocated before the capture (no allocation while capturing); the lanes'
         // streams join the capture through the fork event and leave it through their done events
         if (lanes > 1) {
@@ -1245,6 +1260,7 @@ dr_status dr_batch_render(dr_renderer *r, dr_batch *b, int32_t use_graph, void *
         b->graph_scratch = r->scratch_id;
         b->graph_wave = wave;
         b->graph_lanes = lanes;
+        b->graph_shape = r->shape;
         size_t nodes = 0;
         cudaGraphGetNodes(g, nullptr, &nodes);
         b->graph_launches = 0;

@@ -109,13 +109,14 @@ struct BatchSource {
     // single-scene source: never asked for a per-job scene (MULTI = false)
     __device__ __forceinline__ const Scene &scene(int) { return *scene0; }
     __device__ __forceinline__ bool clip(int) { return cull; }
-    __device__ __forceinline__ void store(int i, const Hit &h, int nb, int nt) {
+    __device__ __forceinline__ bool store(int i, const Hit &h, int nb, int nt) {
         hit_tri[i] = h.tri;
         hit_t[i] = h.tri >= 0 ? h.t : FLT_MAX;
         if (nbox) {
             nbox[i] = nb;
             ntri[i] = nt;
         }
+        return false;
     }
 };
 
@@ -131,20 +132,12 @@ __global__ void __launch_bounds__(128) k_cast(Scene S, const float *__restrict__
 
 // ---------------------------------------------------------------------------------------------
 // Wave control block (int slots, zeroed at the start of every wave).
-// Engine passes over reference photons per bounce; chains still going after them finish one photon
-// per lane (k_photon_chain).
-constexpr int kPhotonPasses = 4;
-
 struct Ctrl {
     int ray_count[kMaxBounceSlots];
     int shadow_count[kMaxBounceSlots];
     int fetch_trace[kMaxBounceSlots];
     int fetch_shade[kMaxBounceSlots];
     int fetch_shadow[kMaxBounceSlots];
-    // reference photons continuing through blockers: per bounce and engine pass, the list length
-    // (pass p reads list p, written by pass p - 1; list 0 is the shadow queue itself) and its fetch
-    int photon_count[kMaxBounceSlots][kPhotonPasses + 1];
-    int photon_fetch[kMaxBounceSlots][kPhotonPasses + 1];
     int fetch_camera;
     int error;
 };
@@ -337,11 +330,12 @@ struct TraceSource {
         const Item &I = job_of<MULTI>(*A, job);
         return I.mode == DR_MODE_REFERENCE && I.clip != 0;
     }
-    __device__ __forceinline__ void store(int i, const Hit &h, int b_, int t_) {
+    __device__ __forceinline__ bool store(int i, const Hit &h, int b_, int t_) {
         hits[i] = make_float2(__int_as_float(h.tri), h.t);
         rays++;
         nb += b_;
         nt += t_;
+        return false;
     }
 };
 
@@ -352,12 +346,14 @@ struct TraceSource {
 constexpr int kTraceThreads = 256;
 constexpr int kTraceBlocksPerSM = 3;
 
-template <bool COUNT, bool MULTI>
-__global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_trace(WaveArgs A, int b) {
+// Block shapes a renderer can select (dr_renderer_set_block_shape): 0 = 256 x 3, 1 = 128 x 6 per SM
+// (both cap registers at 80); the autotuner times them.
+template <bool COUNT, bool MULTI, int TT = kTraceThreads, int TB = kTraceBlocksPerSM>
+__global__ void __launch_bounds__(TT, TB) k_trace(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const int n = *((volatile int *)&C->ray_count[b]);
     uint32_t stack[kStack];
-    __shared__ WarpLeafSlots slots[kTraceThreads / 32];
+    __shared__ WarpLeafSlots slots[TT / 32];
     TraceSource<MULTI> src{&A, A.q[b & 1], A.hits, &C->fetch_trace[b], n, chunk_for(n), 0, 0, 0};
     trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5], A.inl.S.front_only ? 2 : 1);
     if (COUNT) count_add64(A.counters, src.rays, src.nb, src.nt);
@@ -470,15 +466,17 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
 
 // Reference light visibility (DumbRenderer.cu:361-428): cast from the light sample toward the
 // point; it counts if the first hit is the shaded triangle or lies within sqrt(8 eps) of the
-// point; otherwise the blocker's reflected colour decides whether the photon continues.
+// point; otherwise the blocker's reflected colour decides whether the photon continues (from just
+// past the blocker, with that colour, the blocker as the ignored object).
 //
-// Every cast of a photon runs on the persistent traversal engine (RefPhotonSource), in passes: pass
-// 0 over the shadow queue, pass p over the photons that pass p - 1 sent on through a blocker.  A
-// continuing photon has its own queue record rewritten in place (its lane has already loaded it):
-// origin just past the blocker, colour attenuated, blocker as the ignored object; its index goes to
-// the next pass's list.  Lists alternate between the hits buffer and the p3 plane of the ray queue
-// this bounce has consumed (both idle during this phase).  Photons still going after the last pass
-// finish in k_photon_chain, one per lane, as the reference's loop does.
+// Every cast of a photon, continuations included, runs on the persistent traversal engine in one
+// launch per bounce: a lane whose photon continues rewrites the photon's queue record in place and
+// starts the next cast at once (the engine's restart), so chains of any length keep their lane and
+// the launch ends when the last chain does, instead of one launch per continuation step.  At most
+// kPhotonCasts casts per photon (the oracle's bound, never reached by a photon that moves along
+// one line through finite geometry); the cast count travels in the record's s3.w.
+constexpr int kPhotonCasts = 64;
+
 __device__ __forceinline__ bool photon_arrives(const Hit &h, int target, f3 hp) {
     const f3 dd = xsub(h.p, hp);
     return h.tri == target || xdot(dd, dd) <= (8.0f * kEps);
@@ -488,116 +486,64 @@ __device__ __forceinline__ bool photon_arrives(const Hit &h, int target, f3 hp) 
 // registers do not weigh on the traversal it is reached from.
 __device__ __noinline__ c3 blocker_reflect(const Scene &S, int tri, f3 p, f3 ld) { return ref_reflect(S, tri, p, ld, ld, true, 0); }
 
-__device__ __forceinline__ int *photon_list(const WaveArgs &A, int b, int pass) {
-    return (pass & 1) ? reinterpret_cast<int *>(A.hits) : reinterpret_cast<int *>(A.q[b & 1].p3);
-}
-
 template <bool MULTI>
 struct RefPhotonSource {
     static constexpr float kOccludeBelow = 0.0f;
     const WaveArgs *A;
     ShadowQ sq;
-    int *fetch, *out_count, *out_list;
-    const int *in_list;   // nullptr: the shadow queue itself
+    int *fetch;
     int n, chunk;
     long long rays, nb, nt;
-    __device__ __forceinline__ int rec(int i) const { return in_list ? in_list[i] : i; }
     __device__ __forceinline__ bool next(int &b, int &e) { return fetch_chunk(fetch, n, chunk, b, e); }
     __device__ __forceinline__ void load(int i, f3 &o, f3 &d, int &ign, int &job) {
-        const int r = rec(i);
-        o = f3of(sq.s0[r]);
-        d = f3of(sq.s1[r]);
-        ign = __float_as_int(sq.s2[r].w);
-        job = __float_as_int(sq.s4[r].w);
+        o = f3of(sq.s0[i]);
+        d = f3of(sq.s1[i]);
+        ign = __float_as_int(sq.s2[i].w);
+        job = __float_as_int(sq.s4[i].w);
     }
     __device__ __forceinline__ const Scene &scene(int job) { return job_of<MULTI>(*A, job).S; }
     __device__ __forceinline__ bool clip(int job) { return job_of<MULTI>(*A, job).clip != 0; }
-    __device__ __forceinline__ void store(int i, const Hit &h, int b_, int t_) {
+    __device__ __forceinline__ bool store(int i, const Hit &h, int b_, int t_) {
         rays++;
         nb += b_;
         nt += t_;
-        if (h.tri < 0) return;
-        const int r = rec(i);
-        const float4 s0 = sq.s0[r], s1 = sq.s1[r], s2 = sq.s2[r], s3 = sq.s3[r], s4 = sq.s4[r];
+        if (h.tri < 0) return false;
+        const float4 s0 = sq.s0[i], s1 = sq.s1[i], s2 = sq.s2[i], s3 = sq.s3[i], s4 = sq.s4[i];
         const c3 lc = mkc(s3.x, s3.y, s3.z);
         if (photon_arrives(h, __float_as_int(s1.w), f3of(s2))) {
             accum_add(A->accum, __float_as_int(s0.w), mkc(s4.x * lc.r, s4.y * lc.g, s4.z * lc.b));
-            return;
+            return false;
         }
+        const int casts = __float_as_int(s3.w) + 1;
+        if (casts >= kPhotonCasts) return false;
         const Scene &S = job_of<MULTI>(*A, __float_as_int(s4.w)).S;
         const f3 ld = f3of(s1);
         const c3 tr = cmul(blocker_reflect(S, h.tri, h.p, ld), lc);
-        if ((tr.r + tr.g + tr.b) > kEps) {
-            const f3 lo = add3(h.p, mul3(norm3(ld), 64.0f * kEps));
-            sq.s0[r] = make_float4(lo.x, lo.y, lo.z, s0.w);
-            sq.s2[r] = make_float4(s2.x, s2.y, s2.z, __int_as_float(h.tri));
-            sq.s3[r] = make_float4(tr.r, tr.g, tr.b, s3.w);
-            out_list[atomicAdd(out_count, 1)] = r;
-        }
+        if (!((tr.r + tr.g + tr.b) > kEps)) return false;
+        const f3 lo = add3(h.p, mul3(norm3(ld), 64.0f * kEps));
+        sq.s0[i] = make_float4(lo.x, lo.y, lo.z, s0.w);
+        sq.s2[i] = make_float4(s2.x, s2.y, s2.z, __int_as_float(h.tri));
+        sq.s3[i] = make_float4(tr.r, tr.g, tr.b, __int_as_float(casts));
+        return true;
     }
 };
 
 // Reference photon casts: the transparency rule puts shading on the cast path, so this kernel gets
 // its own register budget (kShadowRefBlocksPerSM blocks of kTraceThreads per SM).  At 3 blocks (80
 // registers) it spills about 200 bytes; at 2 (up to 128 registers) none.  Reference-mode twin of the
-// path trace (Mpaths/s, two runs each): 3 blocks 50.5 / 51.0, 2 blocks 56.5 / 56.3.
+// path trace (Mpaths/s, two runs each, 1 spp): 3 blocks 50.5 / 51.0, 2 blocks 56.5 / 56.3.
 constexpr int kShadowRefBlocksPerSM = 2;
 
 template <bool COUNT, bool MULTI>
-__global__ void __launch_bounds__(kTraceThreads, kShadowRefBlocksPerSM) k_shadow_ref(WaveArgs A, int b, int pass) {
+__global__ void __launch_bounds__(kTraceThreads, kShadowRefBlocksPerSM) k_shadow_ref(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
-    const int n = pass == 0 ? *((volatile int *)&C->shadow_count[b]) : *((volatile int *)&C->photon_count[b][pass]);
+    const int n = *((volatile int *)&C->shadow_count[b]);
     if (n == 0) return;
     uint32_t stack[kStack];
     __shared__ WarpLeafSlots slots[kTraceThreads / 32];
-    RefPhotonSource<MULTI> src{&A, A.sq, pass == 0 ? &C->fetch_shadow[b] : &C->photon_fetch[b][pass],
-                               &C->photon_count[b][pass + 1], photon_list(A, b, pass + 1),
-                               pass == 0 ? nullptr : photon_list(A, b, pass), n, chunk_for(n), 0, 0, 0};
+    RefPhotonSource<MULTI> src{&A, A.sq, &C->fetch_shadow[b], n, chunk_for(n), 0, 0, 0};
     trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5]);
     if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
-}
-
-// Chains still going after the engine passes: one photon per lane, from its rewritten record.
-template <bool COUNT, bool MULTI>
-__global__ void __launch_bounds__(256) k_photon_chain(WaveArgs A, int b) {
-    Ctrl *C = A.ctrl;
-    const int n = *((volatile int *)&C->photon_count[b][kPhotonPasses]);
-    const int *chain = photon_list(A, b, kPhotonPasses);
-    for (;;) {
-        int base = warp_fetch(&C->photon_fetch[b][kPhotonPasses]);
-        if (base >= n) break;
-        int j = base + (int)lane_id();
-        int casts = 0, nb = 0, nt = 0;
-        if (j < n) {
-            const int i = chain[j];
-            float4 s0 = A.sq.s0[i], s1 = A.sq.s1[i], s2 = A.sq.s2[i], s3 = A.sq.s3[i], s4 = A.sq.s4[i];
-            const Item &I = job_of<MULTI>(A, __float_as_int(s4.w));
-            const Scene &S = I.S;
-            const bool clip = I.clip != 0;
-            f3 lo = f3of(s0), ld = f3of(s1), hp = f3of(s2);
-            int target = __float_as_int(s1.w);
-            int slot = __float_as_int(s0.w);
-            c3 lc = mkc(s3.x, s3.y, s3.z);
-            int restrict_obj = __float_as_int(s2.w);
-            for (int guard = kPhotonPasses; guard < 64; guard++) {   // casts 0 .. kPhotonPasses-1 were the passes'
-                Hit h;
-                casts++;
-                cast_closest<COUNT>(S, lo, ld, clip, restrict_obj, h, nb, nt);
-                if (h.tri < 0) break;
-                if (photon_arrives(h, target, hp)) {
-                    accum_add(A.accum, slot, mkc(s4.x * lc.r, s4.y * lc.g, s4.z * lc.b));
-                    break;
-                }
-                c3 tr = cmul(ref_reflect(S, h.tri, h.p, ld, ld, true, 0), lc);
-                if ((tr.r + tr.g + tr.b) > kEps) {
-                    lc = tr;
-                    lo = add3(h.p, mul3(norm3(ld), 64.0f * kEps));
-                    restrict_obj = h.tri;
-                } else break;
-            }
-        }
-        if (COUNT) count_add64(A.counters + 3, casts, nb, nt);
-    }
 }
 
 // Adjoint helpers: dL/dI of the pixel behind an accumulator slot, divided by spp (the pixel is the
@@ -823,7 +769,7 @@ struct ShadowPhysSource {
     }
     __device__ __forceinline__ const Scene &scene(int job) { return job_of<MULTI>(*A, job).S; }
     __device__ __forceinline__ bool clip(int) { return false; }
-    __device__ __forceinline__ void store(int i, const Hit &h, int b_, int t_) {
+    __device__ __forceinline__ bool store(int i, const Hit &h, int b_, int t_) {
         int light_tri = __float_as_int(sq.s1[i].w);
         bool vis = (h.tri < 0) || (h.tri == light_tri) || !(h.t < 0.999f);
         if (vis) {
@@ -849,18 +795,19 @@ struct ShadowPhysSource {
         rays++;
         nb += b_;
         nt += t_;
+        return false;
     }
 };
 
 // Physical visibility: closest hit from the shading point toward the sampled light point
 // (direction = light point - shading point, so the light is at t = 1), ignoring the shading
 // triangle; visible if nothing but the light triangle is hit before t = 0.999.
-template <bool COUNT, bool MULTI, bool ADJ>
-__global__ void __launch_bounds__(kTraceThreads, kTraceBlocksPerSM) k_shadow_phys(WaveArgs A, int b) {
+template <bool COUNT, bool MULTI, bool ADJ, int TT = kTraceThreads, int TB = kTraceBlocksPerSM>
+__global__ void __launch_bounds__(TT, TB) k_shadow_phys(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const int n = *((volatile int *)&C->shadow_count[b]);
     uint32_t stack[kStack];
-    __shared__ WarpLeafSlots slots[kTraceThreads / 32];
+    __shared__ WarpLeafSlots slots[TT / 32];
     ShadowPhysSource<MULTI, ADJ> src{&A, A.sq, A.accum, &C->fetch_shadow[b], n, chunk_for(n), 0, 0, 0};
     trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5], A.inl.S.front_only ? 2 : 1);
     if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
@@ -1065,18 +1012,18 @@ static void fill_args(const WaveDesc &W, WaveArgs &A, unsigned long long *counte
     A.prefix = W.prefix;
 }
 
-template <bool MULTI>
+template <bool MULTI, int TT, int TB>
 static void launch_wave_t(const WaveDesc &W, const WaveArgs &A, cudaStream_t stream, Profiler &P, bool count, long long &nl) {
     const int grid = sm_count() * 8;
     P.begin(KC_CAMERA, stream);
     k_camera<MULTI><<<grid, 256, 0, stream>>>(A);
     P.end(KC_CAMERA, stream);
     nl++;
-    const int tgrid = grid * (256 / kTraceThreads);   // same threads in flight as the 256-thread kernels
+    const int tgrid = grid * (256 / TT);   // same threads in flight as the 256-thread kernels
     for (int b = 0; b <= W.max_bounces; b++) {
         P.begin(KC_TRACE, stream);
-        if (count) k_trace<true, MULTI><<<tgrid, kTraceThreads, 0, stream>>>(A, b);
-        else k_trace<false, MULTI><<<tgrid, kTraceThreads, 0, stream>>>(A, b);
+        if (count) k_trace<true, MULTI, TT, TB><<<tgrid, TT, 0, stream>>>(A, b);
+        else k_trace<false, MULTI, TT, TB><<<tgrid, TT, 0, stream>>>(A, b);
         P.end(KC_TRACE, stream);
         P.begin(KC_SHADE, stream);
         if (W.mode == DR_MODE_REFERENCE) k_shade_ref<MULTI><<<grid, 256, 0, stream>>>(A, b);
@@ -1085,18 +1032,14 @@ static void launch_wave_t(const WaveDesc &W, const WaveArgs &A, cudaStream_t str
         P.end(KC_SHADE, stream);
         P.begin(KC_SHADOW, stream);
         if (W.mode == DR_MODE_REFERENCE) {
-            for (int pass = 0; pass < kPhotonPasses; pass++) {
-                if (count) k_shadow_ref<true, MULTI><<<tgrid, kTraceThreads, 0, stream>>>(A, b, pass);
-                else k_shadow_ref<false, MULTI><<<tgrid, kTraceThreads, 0, stream>>>(A, b, pass);
-            }
-            if (count) k_photon_chain<true, MULTI><<<grid, 256, 0, stream>>>(A, b);
-            else k_photon_chain<false, MULTI><<<grid, 256, 0, stream>>>(A, b);
-            nl += kPhotonPasses;
+            const int sgrid = sm_count() * kShadowRefBlocksPerSM;   // one persistent block per slot
+            if (count) k_shadow_ref<true, MULTI><<<sgrid, kTraceThreads, 0, stream>>>(A, b);
+            else k_shadow_ref<false, MULTI><<<sgrid, kTraceThreads, 0, stream>>>(A, b);
         } else if (W.adjoint) {
-            k_shadow_phys<false, MULTI, true><<<tgrid, kTraceThreads, 0, stream>>>(A, b);
+            k_shadow_phys<false, MULTI, true, TT, TB><<<tgrid, TT, 0, stream>>>(A, b);
         } else {
-            if (count) k_shadow_phys<true, MULTI, false><<<tgrid, kTraceThreads, 0, stream>>>(A, b);
-            else k_shadow_phys<false, MULTI, false><<<tgrid, kTraceThreads, 0, stream>>>(A, b);
+            if (count) k_shadow_phys<true, MULTI, false, TT, TB><<<tgrid, TT, 0, stream>>>(A, b);
+            else k_shadow_phys<false, MULTI, false, TT, TB><<<tgrid, TT, 0, stream>>>(A, b);
         }
         P.end(KC_SHADOW, stream);
         nl += 3;
@@ -1112,8 +1055,14 @@ cudaError_t launch_wave(const WaveDesc &W, cudaStream_t stream, long long *launc
     long long nl = 0;
     Profiler dummy;
     Profiler &P = prof ? *prof : dummy;
-    if (W.items) launch_wave_t<true>(W, A, stream, P, counters != nullptr, nl);
-    else launch_wave_t<false>(W, A, stream, P, counters != nullptr, nl);
+    const bool cnt = counters != nullptr;
+    if (W.shape == 1) {
+        if (W.items) launch_wave_t<true, 128, 6>(W, A, stream, P, cnt, nl);
+        else launch_wave_t<false, 128, 6>(W, A, stream, P, cnt, nl);
+    } else {
+        if (W.items) launch_wave_t<true, kTraceThreads, kTraceBlocksPerSM>(W, A, stream, P, cnt, nl);
+        else launch_wave_t<false, kTraceThreads, kTraceBlocksPerSM>(W, A, stream, P, cnt, nl);
+    }
     if (launches) *launches += nl;
     return cudaGetLastError();
 }

@@ -50,6 +50,7 @@ struct WaveDesc {
     void *ctrl;
     int *prefix;                 // adjoint: [wave capacity][kAdjDepth] triangle of each path vertex
     bool adjoint;
+    int shape;                   // traversal block shape: 0 = 256 threads x 3 blocks per SM, 1 = 128 x 6
 };
 
 // Kernel classes for per-class timing.

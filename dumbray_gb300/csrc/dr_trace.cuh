@@ -68,6 +68,16 @@ __device__ __forceinline__ int lane_start(const Scene &S, LaneRay &L) {
     return kTrav;
 }
 
+// A ray the source rewrote in place (a photon continuing past a blocker): the lane starts it at
+// once, without going back to the warp's chunk.
+template <bool COUNT, bool MULTI, class Source>
+__device__ __forceinline__ int restart(const Scene &S, Source &src, int i, LaneRay &L) {
+    int ign, job;
+    src.load(i, L.o, L.d, ign, job);
+    L.ignore = ign;
+    return lane_start<COUNT>(MULTI ? src.scene(job) : S, L);
+}
+
 // Per-warp shared scratch of the cooperative leaf rounds.
 struct WarpLeafSlots {
     unsigned long long key[32];
@@ -79,7 +89,8 @@ struct WarpLeafSlots {
 //   void load(int i, f3 &o, f3 &d, int &ignore, int &job)
 //   const Scene &scene(int job)               the scene of a job (MULTI only)
 //   bool clip(int job)                        backface culling of a job (MULTI = false: job 0 for all)
-//   void store(int i, const Hit &h, int nbox, int ntri)
+//   bool store(int i, const Hit &h, int nbox, int ntri)   true: ray i was rewritten (load() now
+//                                             gives its next cast) and the lane traces it at once
 //   static constexpr float kOccludeBelow      > 0: visibility-only rays (any hit nearer than this
 //                                             settles them); 0: closest hit
 // MULTI = false: every ray belongs to scene `S`.  MULTI = true: rays of different scenes share the
@@ -141,8 +152,7 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
                 Hit h;
                 h.tri = -1;
                 h.t = FLT_MAX;
-                src.store(cur_i, h, L.nb, L.nt);
-                mode = kIdle;
+                mode = src.store(cur_i, h, L.nb, L.nt) ? restart<COUNT, MULTI>(S, src, cur_i, L) : kIdle;
             } else {
                 int k = __ffs(m) - 1;
                 L.cur &= ~(1u << k);
@@ -260,8 +270,7 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
                 h.tri = L.bi;
                 h.t = L.best;
                 h.p = L.bp;
-                src.store(cur_i, h, L.nb, L.nt);
-                mode = kIdle;
+                mode = src.store(cur_i, h, L.nb, L.nt) ? restart<COUNT, MULTI>(S, src, cur_i, L) : kIdle;
             } else {
                 mode = kTrav;
             }

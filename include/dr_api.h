@@ -335,6 +335,14 @@ void dr_renderer_destroy(dr_renderer *r);
 dr_status dr_renderer_set_lanes(dr_renderer *r, int32_t lanes);
 int32_t dr_renderer_lanes(const dr_renderer *r);
 
+/* Block shape of the traversal kernels (no counterpart in the reference, which launches one
+ * thread per pixel): 0 = 256 threads x 3 blocks per SM (default), 1 = 128 threads x 6 blocks per SM.
+ * Both cap registers at 80 and keep the same threads in flight; they differ in how warps share an
+ * SM's blocks and leave the tail of a launch.  Results do not depend on the shape.  A batch graph
+ * captured with one shape is re-captured when the renderer's shape changes. */
+dr_status dr_renderer_set_block_shape(dr_renderer *r, int32_t shape);
+int32_t dr_renderer_block_shape(const dr_renderer *r);
+
 /* Replaces DumbRenderer::renderBlocksGPU (DumbRenderer.cu:87-113): renders blocks
  * [start_block, end_block) of a width x height image into the caller's device frame buffer
  * (BlockBasedFrameBuffer<8,16> layout, float4), setting (iteration <= 1) or blending (1/iteration)

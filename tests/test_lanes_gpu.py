@@ -54,7 +54,7 @@ def test_lanes_match_one_lane_physical(cuda, lanes):
 
 
 def test_lanes_match_one_lane_reference_mode(cuda):
-    """Reference mode: photon casts in passes over continuing photons, per lane."""
+    """Reference mode: photon casts (continuing through blockers in place), per lane."""
     tris, mat, mats, lights, cam = render_scene("spot")
     lights = lights + render_scene("diffuse")[3]
     sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights)
@@ -110,3 +110,34 @@ def test_busy_time_and_arguments(cuda):
     for bad in (0, 9, -1):
         with pytest.raises(dr.DumbRayError):
             r.set_lanes(bad)
+
+
+@pytest.mark.parametrize("mode", [dr.MODE_PHYSICAL, dr.MODE_REFERENCE])
+def test_block_shapes_render_the_same_image(cuda, mode):
+    """dr_renderer_set_block_shape changes how the traversal kernels are launched, not what they
+    compute: both shapes give the same image (up to float accumulation order), also through a
+    captured batch graph, which is re-captured when the shape changes."""
+    if mode == dr.MODE_PHYSICAL:
+        sc, cam = _physical()
+    else:
+        tris, mat, mats, lights, cam = render_scene("metal")
+        sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights)
+    p = dr.render_params(96, 64, mode, samples=(2, 2), max_bounces=4, seed=12)
+    r = dr.Renderer(4096, 2)
+    assert r.block_shape == 0
+    a = _render(r, sc, cam, p, cuda)
+    r.set_block_shape(1)
+    assert r.block_shape == 1
+    b = _render(r, sc, cam, p, cuda)
+    assert np.allclose(a, b, rtol=1e-4, atol=1e-6)
+    fb = dr.new_frame_buffer(96, 64, cuda)
+    batch = dr.Batch([(sc, cam, p, fb, 0, dr.block_count(96, 64))])
+    for shape in (0, 1, 0):
+        r.set_block_shape(shape)
+        fb.zero_()
+        batch.render(r, use_graph=True)
+        torch.cuda.synchronize()
+        assert np.allclose(fb.cpu().numpy(), a, rtol=1e-4, atol=1e-6)
+    with pytest.raises(dr.DumbRayError):
+        r.set_block_shape(2)
+    batch.close()

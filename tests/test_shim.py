@@ -1,5 +1,6 @@
 """The reference-side drop-in GB300Renderer (tests/shim/GB300Renderer.cu), compiled against the
-reference sources and linked with the reference host path and this library.
+reference sources into one shared object with the reference's own objects (as inside a DumbRay
+build) and linked with this library.
 
 CPU: it compiles, links with no undefined symbol, exports the harness entry points, and its set-up
 fails with NULL (no crash) where there is no GPU.
@@ -51,15 +52,17 @@ def shim():
         L.dshim_error.restype = ctypes.c_char_p
         L.dshim_error.argtypes = [vp]
         L.dshim_destroy.argtypes = [vp]
+        L.dref_scene_destroy.argtypes = [vp]
         _lib = L
     return _lib
 
 
 class RefScene:
-    """A reference TriScene + camera built through the reference's constructors (dref_scene_create_uv)."""
+    """A reference TriScene + camera built through the reference's constructors (dref_scene_create_uv of
+    the reference objects inside the shim's own shared object)."""
 
     def __init__(self, tris, mat, mats, lights, cam, uv=None, textures=()):
-        L = O.reference()
+        L = shim()
         self.t = np.ascontiguousarray(tris, np.float32)
         self.m = np.ascontiguousarray(mat, np.int32)
         self.mrec = np.ascontiguousarray(np.stack([O.ref_material_record(x) for x in mats]))
@@ -80,7 +83,7 @@ class RefScene:
 
     def close(self):
         if self.h:
-            O.reference().dref_scene_destroy(self.h)
+            shim().dref_scene_destroy(self.h)
             self.h = None
 
 
@@ -90,7 +93,7 @@ def test_shim_builds_links_and_exports():
     for name in ("dshim_create", "dshim_render", "dshim_read", "dshim_camera", "dshim_error", "dshim_destroy"):
         assert hasattr(L, name)
     out = subprocess.run(["nm", "-DC", str(LIB)], capture_output=True, text=True).stdout
-    assert "GB300Renderer::renderBlocksGPU" in out
+    assert "GB300Renderer::renderBlocksGPU" in out and "DumbRenderer::renderBlocksCPU" in out
 
 
 @needs_ref
