@@ -669,7 +669,7 @@ def run_reference_twin_gpu(dr, torch, dev, a, S, peak, peak_src):
                    "d2h_bytes_per_step": int(fb.numel() * 4)},
            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                         "frac": round(achieved / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
-                        "kernel": "k_shadow_ref + k_photon_chain (photon casts)", "casts_per_frame": int(casts),
+                        "kernel": "k_shadow_ref (photon casts, continuations included)", "casts_per_frame": int(casts),
                         "c_box": round(c_box, 2), "c_tri": round(c_tri, 2), "bytes_per_cast": round(bpr, 1),
                         "busy_ms_per_frame": round(shadow_ms, 2),
                         "basis": "photon-cast busy time (union of launch intervals over lanes) per frame"},

@@ -3,13 +3,16 @@
 nvcc compiles the CUDA translation units for sm_103a only; the host octree builder is plain C++.
 Translation units compile in parallel; no cmake, no torch extension machinery.
 
-FP contraction: host code is compiled with ``-ffp-contract=off`` (the host octree build rounds like
-DumbRay's host code on x86-64 and aarch64, where gcc would otherwise fuse multiply-adds).  On the
-device only the GPU octree builder (``octree_gpu.cu``, sharing its plain-operator geometry with the
-host builder through ``octree_geom.h``) is compiled with ``-fmad=false``, so its tree stays
-bit-identical to the host build.  The cast predicate and the traversal are written with explicitly
-rounded intrinsics (``__fadd_rn`` / ``__fmul_rn`` / ``__fdiv_rn`` / ``__fsqrt_rn``), which the compiler
-never contracts, so the render and adjoint kernels may fuse multiply-adds elsewhere.
+FP contraction is off everywhere: host code is compiled with ``-ffp-contract=off`` (the host octree
+build rounds like DumbRay's host code on x86-64 and aarch64, where gcc would otherwise fuse
+multiply-adds) and device code with ``-fmad=false``.  The GPU octree builder needs it for trees
+bit-identical to the host build; the cast predicate is written with explicitly rounded intrinsics,
+which are never contracted.  The render kernels would not need it: letting them fuse was measured on
+a GB300 and bought
+nothing on the 1080p path trace (327.4 / 327.5 Mpaths/s fused, 328.3 unfused) and about 2.5% on the
+reference-mode twin (158.3 vs 154.5), while it moved same-seed per-pixel agreement with the FP64
+oracle past 1% on one physical-mode lens case, so they stay unfused too.  ``NO_FMAD`` lists the
+translation units that are compiled unfused; every one is, today.
 """
 from __future__ import annotations
 
@@ -25,7 +28,7 @@ CSRC = HERE / "csrc"
 OUT = HERE / "_build"
 LIB = OUT / "libdumbray_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NO_FMAD = {"octree_gpu.cu"}   # translation units whose bit-exactness rests on plain operators
+NO_FMAD = {"octree_gpu.cu", "dr_kernels.cu", "dr_api.cu", "dr_noalloc.cu", "dr_progressive.cu"}
 
 
 def _nvcc() -> str:

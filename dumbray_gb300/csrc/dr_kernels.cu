@@ -508,20 +508,23 @@ struct RefPhotonSource {
         nb += b_;
         nt += t_;
         if (h.tri < 0) return false;
-        const float4 s0 = sq.s0[i], s1 = sq.s1[i], s2 = sq.s2[i], s3 = sq.s3[i], s4 = sq.s4[i];
-        const c3 lc = mkc(s3.x, s3.y, s3.z);
-        if (photon_arrives(h, __float_as_int(s1.w), f3of(s2))) {
-            accum_add(A->accum, __float_as_int(s0.w), mkc(s4.x * lc.r, s4.y * lc.g, s4.z * lc.b));
+        // record planes are read where each branch needs them, so few values stay live in the
+        // traversal loop this is inlined into
+        const float4 s2 = sq.s2[i];
+        if (photon_arrives(h, __float_as_int(sq.s1[i].w), f3of(s2))) {
+            const float4 s3 = sq.s3[i], s4 = sq.s4[i];
+            accum_add(A->accum, __float_as_int(sq.s0[i].w), mkc(s4.x * s3.x, s4.y * s3.y, s4.z * s3.z));
             return false;
         }
+        const float4 s3 = sq.s3[i];
         const int casts = __float_as_int(s3.w) + 1;
         if (casts >= kPhotonCasts) return false;
-        const Scene &S = job_of<MULTI>(*A, __float_as_int(s4.w)).S;
-        const f3 ld = f3of(s1);
-        const c3 tr = cmul(blocker_reflect(S, h.tri, h.p, ld), lc);
+        const Scene &S = job_of<MULTI>(*A, __float_as_int(sq.s4[i].w)).S;
+        const f3 ld = f3of(sq.s1[i]);
+        const c3 tr = cmul(blocker_reflect(S, h.tri, h.p, ld), mkc(s3.x, s3.y, s3.z));
         if (!((tr.r + tr.g + tr.b) > kEps)) return false;
         const f3 lo = add3(h.p, mul3(norm3(ld), 64.0f * kEps));
-        sq.s0[i] = make_float4(lo.x, lo.y, lo.z, s0.w);
+        sq.s0[i] = make_float4(lo.x, lo.y, lo.z, sq.s0[i].w);
         sq.s2[i] = make_float4(s2.x, s2.y, s2.z, __int_as_float(h.tri));
         sq.s3[i] = make_float4(tr.r, tr.g, tr.b, __int_as_float(casts));
         return true;

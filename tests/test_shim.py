@@ -177,7 +177,9 @@ def test_render_blocks_gpu_matches_direct_call(cuda, kind):
             x = np.float32(0.5) / np.tan(np.float32(cam.angle[0]) / np.float32(2 * 57.29577951308233))
             assert abs(c.lens_x - float(x)) <= 4 * np.spacing(np.float32(x))
         want = _direct(SCENES[kind], c, W, H, fsaa, bounces, seed, cuda)
-        _same(got, want)
+        # in-image pixels only: neither renderer writes the padding of the last block row, and the
+        # reference's host buffer (and so its device replica) starts uninitialised there
+        _same(dr.blockmajor_to_image(got, W, H).reshape(-1, 4), dr.blockmajor_to_image(want, W, H).reshape(-1, 4))
         assert float(got[:, :3].mean()) > 0
     finally:
         L.dshim_destroy(h)
