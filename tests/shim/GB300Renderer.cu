@@ -184,7 +184,7 @@ bool convert_light(const Light &src, dr_light &l, std::string &error) {
 		set3(l.color, s.color.r, s.color.g, s.color.b);
 		set3(l.direction, s.dir.x, s.dir.y, s.dir.z);
 		l.distance = s.dist;
-		l.softness = s.soft;
+		l.softness = (s.dist != 0.0f) ? s.soft / s.dist : 0.0f;   // the constructor stores distance x softness
 	} else if (holds<SimpleDirectionalLight>(src, Color(1.0f, 1.0f, 1.0f), Vector3(0.0f, -1.0f, 0.0f), 1.0f)) {
 		const SimpleDirectionalLight &s = *src.getObject<SimpleDirectionalLight>();
 		l.type = DR_LIGHT_DIRECTIONAL;
