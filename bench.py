@@ -288,6 +288,7 @@ def run_ours(a):
     torch.cuda.synchronize()
     clocks = sampler.stop()
     launches = rend.launches() - launches0
+    wave_rays, wave_shadows = rend.wave_counts(a.depth + 1)
     ktimes = rend.kernel_times()
     kbusy = rend.kernel_busy()
     rend.set_profiling(False)
@@ -376,6 +377,8 @@ def run_ours(a):
         "kernel_launch_ms_sum_per_step": {k: round(v[0] / a.steps, 2) for k, v in ktimes.items()},
         "first_frame_ms": None if first_ms is None else round(first_ms, 1),
         "rays_per_frame": {"extension": cnt["trace_rays"], "shadow": cnt["shadow_casts"]},
+        "last_wave_rays_per_bounce": {"extension": wave_rays, "shadow": wave_shadows,
+                                      "basis": "queue sizes of the last wave on the renderer's first lane"},
         "mrays_per_s": round((cnt["trace_rays"] + cnt["shadow_casts"]) * a.steps / (ms / 1e3) / 1e6, 1),
     }
     if clocks:

@@ -176,6 +176,8 @@ def lib() -> ctypes.CDLL:
     L.dr_renderer_set_counting.argtypes = [vp, i32]
     L.dr_renderer_counters.restype = i32
     L.dr_renderer_counters.argtypes = [vp, vp]
+    L.dr_renderer_wave_counts.restype = i32
+    L.dr_renderer_wave_counts.argtypes = [vp, vp, vp, i32]
     L.dr_render_adjoint.restype = i32
     L.dr_render_adjoint.argtypes = [vp, vp, vp, vp, i32, i32, vp, vp, vp, vp]
     L.dr_batch_create.restype = i32
@@ -651,6 +653,14 @@ class Renderer:
         check(lib().dr_renderer_counters(self._h, c.ctypes.data))
         return dict(trace_rays=int(c[0]), trace_box=int(c[1]), trace_tri=int(c[2]), shadow_casts=int(c[3]),
                     shadow_box=int(c[4]), shadow_tri=int(c[5]))
+
+    def wave_counts(self, n: int = 9):
+        """(rays per bounce, shadow records per bounce) of the last wave on the renderer's own scratch
+        (dr_renderer_wave_counts), bounces 0 .. n-1."""
+        rays = np.zeros(n, np.int32)
+        sh = np.zeros(n, np.int32)
+        check(lib().dr_renderer_wave_counts(self._h, rays.ctypes.data, sh.ctypes.data, int(n)))
+        return rays.tolist(), sh.tolist()
 
     def render_blocks(self, scene: Scene, cam: DrCamera, fb, start_block: int, end_block: int, params: DrRenderParams,
                       stream=None):

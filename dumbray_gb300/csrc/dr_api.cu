@@ -757,6 +757,19 @@ dr_status dr_renderer_set_counting(dr_renderer *r, int32_t enable) try {
     return dr_internal_exception("dr_renderer_set_counting");
 }
 
+dr_status dr_renderer_wave_counts(dr_renderer *r, int32_t *rays, int32_t *shadow_records, int32_t n) try {
+    if (!r || !rays || !shadow_records) return fail(DR_E_ARG, "dr_renderer_wave_counts: NULL argument");
+    if (n < 0 || n > drd::kMaxBounceSlots) return fail(DR_E_ARG, "dr_renderer_wave_counts: n must be in [0, 68]");
+    if (n == 0) return DR_OK;
+    if (!r->ctrl) return fail(DR_E_STATE, "dr_renderer_wave_counts: the renderer has not rendered");
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = drk::read_wave_counts(r->ctrl, rays, shadow_records, n);
+    if (e != cudaSuccess) return cuda_fail(e, "dr_renderer_wave_counts");
+    return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_renderer_wave_counts");
+}
+
 dr_status dr_renderer_counters(dr_renderer *r, int64_t *counts) try {
     if (!r || !counts) return fail(DR_E_ARG, "dr_renderer_counters: NULL argument");
     unsigned long long h[6] = {0, 0, 0, 0, 0, 0};

@@ -905,6 +905,13 @@ cudaError_t launch_cast(const Scene &S, const float *o, const float *d, const in
 
 size_t ctrl_bytes() { return sizeof(Ctrl); }
 
+cudaError_t read_wave_counts(const void *ctrl, int *rays, int *shadows, int n) {
+    const Ctrl *C = static_cast<const Ctrl *>(ctrl);
+    cudaError_t e = cudaMemcpy(rays, C->ray_count, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(shadows, C->shadow_count, sizeof(int) * (size_t)n, cudaMemcpyDeviceToHost);
+    return e;
+}
+
 Profiler::~Profiler() {
     reset();
     for (cudaEvent_t e : pool_) cudaEventDestroy(e);

@@ -86,6 +86,9 @@ class Profiler {
 };
 
 size_t ctrl_bytes();
+// Per-bounce queue counts of the wave last run on control block `ctrl`: rays[b] = extension rays
+// traced at bounce b, shadows[b] = shadow / photon records queued at bounce b (b < n <= kMaxBounceSlots).
+cudaError_t read_wave_counts(const void *ctrl, int *rays, int *shadows, int n);
 
 cudaError_t launch_cast(const drd::Scene &S, const float *o, const float *d, const int *ignore, int n, int clip, int *hit_tri,
                         float *hit_t, int *nbox, int *ntri, cudaStream_t stream, long long *launches);

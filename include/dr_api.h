@@ -437,6 +437,13 @@ dr_status dr_renderer_set_counting(dr_renderer *r, int32_t enable);
  * {extension rays, their box tests, their triangle tests, shadow casts, their box tests, their triangle tests}. */
 dr_status dr_renderer_counters(dr_renderer *r, int64_t *counts);
 
+/* Queue sizes of the last wave the renderer ran on its own scratch (its first lane), per bounce b < n
+ * (n <= 68; synchronises the device): rays[b] extension rays traced at bounce b (b = 0: camera rays),
+ * shadow_records[b] shadow rays (physical mode) or light photons (reference mode) queued at bounce b.
+ * With one lane and a wave at least as large as a render, these are the render's own counts - path
+ * survival per bounce, and the rays of each trace launch for profiling.  No reference counterpart. */
+dr_status dr_renderer_wave_counts(dr_renderer *r, int32_t *rays, int32_t *shadow_records, int32_t n);
+
 /* ---- images (host memory) ----------------------------------------------------------------
  * Replace Images::saveBufferPNG (__source__/Namespaces/Images/Images.cu:22-40) and the frame
  * buffer's getColor walk it does.  rgba is a row-major float[height][width][4] image. */

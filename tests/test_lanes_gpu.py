@@ -141,3 +141,22 @@ def test_block_shapes_render_the_same_image(cuda, mode):
     with pytest.raises(dr.DumbRayError):
         r.set_block_shape(2)
     batch.close()
+
+
+def test_wave_counts_sum_to_the_counted_rays(cuda):
+    """dr_renderer_wave_counts: with one lane and a wave that holds the whole render, the per-bounce
+    queue sizes of the last wave are the render's own, so the extension rays add up to what the
+    counting pass counts and bounce 0 holds one camera ray per path."""
+    sc, cam = _physical()
+    p = dr.render_params(96, 64, dr.MODE_PHYSICAL, samples=(2, 2), max_bounces=4, seed=3)
+    r = dr.Renderer(1 << 16, 1)
+    r.set_counting(True)
+    _render(r, sc, cam, p, cuda)
+    cnt = r.counters()
+    rays, shadows = r.wave_counts(6)
+    assert rays[0] == 96 * 64 * 4
+    assert sum(rays) == cnt["trace_rays"]
+    assert sum(shadows) == cnt["shadow_casts"]
+    assert rays[5] == 0 and all(a >= b for a, b in zip(rays, rays[1:]))
+    with pytest.raises(dr.DumbRayError):
+        r.wave_counts(69)
