@@ -35,9 +35,10 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Mpaths/s 1080p 64spp on 1 GB300: plain vs batched, fwd vs fwd+adjoint, at RMSE"
 # DRAM bytes (read + write) per extension ray of k_trace: ncu dram__bytes_read.sum + dram__bytes_write.sum
-# summed over every k_trace launch of one 960x544, 4 spp frame of the same scene, camera and octree
-# (0.933 GB over 3,946,242 rays); the `traffic` of an average full-size launch is this times its ray count.
-TRACE_DRAM_BYTES_PER_RAY = 236.4
+# of the bounce-1 launch of a 960x544, 4 spp frame of the same scene, camera and octree rendered as one
+# wave (348.0 MB over its 1,375,097 rays, caches flushed before the launch); the `traffic` of an average
+# full-size launch is this times its ray count.
+TRACE_DRAM_BYTES_PER_RAY = 253.1
 UNIT = "Mpaths/s"
 
 
@@ -64,6 +65,8 @@ def parse():
     ap.add_argument("--no-raycast", action="store_true", help="skip the ray-cast microbenchmark leg")
     ap.add_argument("--no-twin", action="store_true", help="skip the reference-mode twin leg")
     ap.add_argument("--no-c1", action="store_true", help="skip the 256x256 plain path-trace leg")
+    ap.add_argument("--raycast-only", action="store_true",
+                    help="profiling case: run only the ray-cast microbenchmark leg and print it")
     ap.add_argument("--twin-only", action="store_true",
                     help="profiling case: run only the reference-mode twin leg (at --twin-size / --twin-spp) and print it")
     ap.add_argument("--twin-size", default="1920x1080", help="reference-mode twin resolution WxH")
@@ -1137,6 +1140,12 @@ def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.raycast_only:
+        import torch
+        import dumbray_gb300 as dr
+        torch.cuda.set_device(0)
+        peak, peak_src = measured_peak()
+        print(json.dumps(run_raycast(dr, torch, torch.device("cuda", 0), a, peak, peak_src)), flush=True)
     elif a.twin_only:
         import torch
         import dumbray_gb300 as dr
