@@ -506,6 +506,17 @@ def run_c1(dr, torch, dev, a):
         rend.render_blocks(sc, cam, fb, 0, nb, params(2 + i))
     K = 20
     ms = _events_ms(torch, lambda i: rend.render_blocks(sc, cam, fb, 0, nb, params(2 + i)), K) / K
+    # the same frames as a one-job batch: the whole launch sequence replayed from one CUDA graph
+    # (dr_batch_render), the iteration rewritten in the job table between replays
+    batch = dr.Batch([(sc, cam, params(2), fb, 0, nb)])
+    batch.render(rend, use_graph=True)
+
+    def graph_step(i):
+        batch.set_iteration(3 + i)
+        batch.render(rend, use_graph=True)
+
+    graph_ms = _events_ms(torch, graph_step, K) / K
+    batch.close()
     rend.render_blocks(sc, cam, fb, 0, nb, params(1))
     torch.cuda.synchronize()
     g = fb.cpu().numpy()
@@ -518,6 +529,8 @@ def run_c1(dr, torch, dev, a):
     out = {"workload": f"room + icosphere L5 + emissive quad ({len(c['tris']):,} tris), 256x256, 16 spp, depth 4, pinhole, "
                        "physical mode",
            "mpaths_s": round(paths / (ms / 1e3) / 1e6, 2), "ms_per_frame": round(ms, 3),
+           "one_job_graph_mpaths_s": round(paths / (graph_ms / 1e3) / 1e6, 2),
+           "one_job_graph_ms_per_frame": round(graph_ms, 3),
            "accuracy_vs_fp64_oracle": dict(fp64_error(g, o), sample="whole image, 16 spp, same seeds"),
            "fp64_oracle_mpaths_s": round(paths / osec / 1e6, 4), "fp64_oracle_cores": threads}
     rend.close()
