@@ -238,7 +238,7 @@ GB300Renderer::GB300Renderer(
 	int samplesPerPixelY, int pixelsPerGPUThread, bool ignoreBackfaces)
 	: DumbRenderer(configuration, blockSettings, buffer, sceneManager, camera, boxingMode, maxBounces,
 		samplesPerPixelX, samplesPerPixelY, pixelsPerGPUThread, ignoreBackfaces),
-	scene(NULL), converted(NULL), seed(0) {}
+	scene(NULL), converted(NULL), seed(0), tightOctree(false) {}
 
 GB300Renderer::~GB300Renderer() {
 	killRenderThreads();   // no worker thread may still be inside renderBlocksGPU
@@ -256,6 +256,12 @@ std::string GB300Renderer::lastError() {
 void GB300Renderer::invalidateScene() {
 	std::lock_guard<std::mutex> guard(sceneLock);
 	converted = NULL;
+}
+
+void GB300Renderer::setTightOctree(bool tight) {
+	std::lock_guard<std::mutex> guard(sceneLock);
+	if (tight != tightOctree) converted = NULL;
+	tightOctree = tight;
 }
 
 void GB300Renderer::fail(const std::string &message) {
@@ -295,7 +301,8 @@ bool GB300Renderer::ensureScene(std::string &err) {
 		if (!convert_light(lights[i], lts[i], err)) return false;
 	dr_build_params bp;
 	std::memset(&bp, 0, sizeof(bp));
-	bp.device_build = 1;   // the reference's split rule and padding, built on this worker's GPU
+	bp.device_build = 1;   // the reference's split rule, built on this worker's GPU
+	bp.box_epsilon = tightOctree ? -1.0f : 0.0f;   // 0: the reference's padding; < 0: the physical-mode one
 	dr_scene *out = NULL;
 	if (dr_scene_create(xyz.data(), nrm.data(), mat.data(), n, mats.data(), (int32_t)mats.size(), lts.data(),
 	                    (int32_t)lts.size(), &bp, &out) != DR_OK) {

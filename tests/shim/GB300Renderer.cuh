@@ -54,6 +54,11 @@ public:
 	// Drops the converted scene so that the next render converts getScene() again (after the host
 	// changed the scene's geometry, materials, lights or textures).
 	void invalidateScene();
+	// Octree padding of the converted scene: false (default) the reference's 1.28e-3, so every cast
+	// equals Octree::cast bit for bit; true the library's physical-mode padding (2^-18 x the largest
+	// coordinate), which holds fewer duplicated triangles per leaf and renders faster, with the same
+	// closest hits up to float32 near-ties (two triangles a few ulps apart along the ray).
+	void setTightOctree(bool tight);
 
 protected:
 	bool renderBlocksGPU(const Info &info, FrameBuffer *host, FrameBuffer *device,
@@ -76,5 +81,6 @@ private:
 	const SceneType *converted;                  // the TriScene that `scene` was made from
 	std::vector<dr_renderer *> renderers;        // by Info::globalThreadId
 	uint32_t seed;
+	bool tightOctree;
 	std::string error;
 };

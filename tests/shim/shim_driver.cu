@@ -138,6 +138,9 @@ int dshim_read(void *h, int start, int end, float *out) {
 	return 1;
 }
 
+// GB300Renderer::setTightOctree.
+void dshim_set_tight_octree(void *h, int tight) { ((Frame *)h)->renderer->setTightOctree(tight != 0); }
+
 // The camera GB300Renderer hands the library (1 = ok).
 int dshim_camera(void *h, dr_camera *out) {
 	Frame *f = (Frame *)h;

@@ -86,6 +86,19 @@ def test_reference_lenses_and_boxing(cuda, lens, boxing):
     _compare(dr.blockmajor_to_image(fb, 33, 19), dr.blockmajor_to_image(osc.render_blocks(cam, p), 33, 19))
 
 
+@pytest.mark.parametrize("kind", ["diffuse", "metal", "ss", "spot"])
+def test_reference_mode_on_the_physical_mode_octree(cuda, kind):
+    """Reference semantics on the tighter physical-mode octree (a drop-in option): the closest hits are
+    the reference tree's up to float32 near-ties, so the frame equals the oracle's (which builds the
+    reference's tree) per pixel within the same tolerance."""
+    tris, mat, mats, lights, cam = _ref_scene(kind)
+    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights, box_epsilon=dr.PHYSICAL_TREE)
+    osc = O.OracleScene(tris, mat_id=mat, materials=mats, lights=lights)
+    p = dr.render_params(40, 28, dr.MODE_REFERENCE, samples=(2, 3), max_bounces=3, seed=5)
+    fb, _ = _gpu_render(sc, cam, p, cuda)
+    _compare(dr.blockmajor_to_image(fb, 40, 28), dr.blockmajor_to_image(osc.render_blocks(cam, p), 40, 28))
+
+
 @pytest.mark.parametrize("cull", [True, False])
 @pytest.mark.parametrize("bounces", [0, 1, 5])
 def test_reference_cull_and_bounce_limit(cuda, cull, bounces):

@@ -53,6 +53,7 @@ def shim():
         L.dshim_error.argtypes = [vp]
         L.dshim_destroy.argtypes = [vp]
         L.dref_scene_destroy.argtypes = [vp]
+        L.dshim_set_tight_octree.argtypes = [vp, ci]
         _lib = L
     return _lib
 
@@ -127,10 +128,10 @@ def _scenes():
 SCENES = _scenes()
 
 
-def _direct(sc_args, cam, W, H, fsaa, bounces, seed, cuda):
+def _direct(sc_args, cam, W, H, fsaa, bounces, seed, cuda, box_epsilon=0.0):
     import torch
     tris, mat, mats, lights, _, uv, textures = sc_args
-    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights)
+    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights, box_epsilon=box_epsilon)
     if textures:
         sc.set_textures(textures, uv)
     fb = dr.new_frame_buffer(W, H, cuda)
@@ -227,3 +228,31 @@ def test_two_worker_threads_on_disjoint_blocks(cuda):
     two = frame(2)
     _same(two, one)
     rs.close()
+
+
+@needs_ref
+@pytest.mark.gpu
+def test_tight_octree_option(cuda):
+    """setTightOctree(true): the converted scene takes the physical-mode padding; the frame equals
+    dr_render_blocks on a scene built with that padding."""
+    import torch
+    L = shim()
+    tris, mat, mats, lights, cam, uv, textures = SCENES["metal"]
+    rs = RefScene(tris, mat, mats, lights, cam)
+    W, H = 40, 36
+    h = L.dshim_create(rs.h, W, H, 2, 2, 3, 1, dr.BOXING_HEIGHT, 9)
+    assert h
+    try:
+        L.dshim_set_tight_octree(h, 1)
+        nb = dr.block_count(W, H)
+        s = torch.cuda.Stream()
+        assert L.dshim_render(h, 0, 0, nb, ctypes.c_void_p(s.cuda_stream)) == 1, L.dshim_error(h)
+        got = np.zeros((nb * 128, 4), np.float32)
+        assert L.dshim_read(h, 0, nb, got.ctypes.data) == 1
+        c = dr.DrCamera()
+        assert L.dshim_camera(h, ctypes.byref(c)) == 1
+        want = _direct(SCENES["metal"], c, W, H, (2, 2), 3, 9, cuda, box_epsilon=dr.PHYSICAL_TREE)
+        _same(dr.blockmajor_to_image(got, W, H).reshape(-1, 4), dr.blockmajor_to_image(want, W, H).reshape(-1, 4))
+    finally:
+        L.dshim_destroy(h)
+        rs.close()
