@@ -157,7 +157,8 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
                 int k = __ffs(m) - 1;
                 L.cur &= ~(1u << k);
                 int node = (int)(L.cur >> GS) * 8 + (L.order ^ k);
-                float4 lo = __ldg(S.nodes + 2 * (size_t)node), hi = __ldg(S.nodes + 2 * (size_t)node + 1);
+                float4 lo, hi;
+                ldg2(S.nodes + 2 * (size_t)node, lo, hi);
                 int w = __float_as_int(lo.w);
                 if (w < 0) {
                     L.r = ~w;
