@@ -11,6 +11,11 @@
                    SHA-256, regenerated by the tests): 8,192 of the benchmark's incoherent rays (origins
                    uniform in [-1.1, 1.1]^3, seed 0) and 8,100 of its 1920x1080 pinhole primaries (every
                    256th); reference Octree::cast index and t, culling on and off; reference node count.
+  render_c3_twin.npz  the reference-expressible twin of the full path-trace scene (bench.reference_twin:
+                   the level-8 displaced icosphere on a ground plane, DumbBased diffuse / metal and
+                   SimpleStochastic mirror materials by triangle hash, 4 spherical lights; the
+                   SimpleStochasticLense 60-degree view of the benchmark frame at 96x54, depth 8): four
+                   reference DumbRenderer runs of 256 iterations, float16 RGB.
   render_c1_twin.npz  the reference-expressible twin of the 256x256 box + icosphere scene (c1_twin):
                    four reference DumbRenderer runs of 64 iterations at 256x256, depth 4, stored as
                    float16 RGB (quantisation far below the Monte Carlo noise).
@@ -133,6 +138,33 @@ def render_c1_twin_fixture(iterations=64, runs=4):
     np.savez_compressed(OUT / "render_c1_twin.npz", runs=runs_arr, iterations=np.int64(iterations),
                         size=np.int64(C1_SIZE), bounces=np.int64(C1_DEPTH), seconds=np.float64(secs))
     print("c1 twin: reference seconds", secs, "mean", runs_arr.astype(np.float64).mean())
+
+
+C3_W, C3_H, C3_DEPTH = 96, 54, 8
+
+
+def c3_twin():
+    """(tris, mat, mats, lights, cam) of the full path-trace scene's reference-expressible twin, as the
+    benchmark's reference-mode leg and reference arm render it."""
+    import bench
+    S = scenes.full_scene(level=8, seed=1)
+    tris, mat, mats, lights = bench.reference_twin(S, dr)
+    cam = dr.camera(dr.LENS_SIMPLE_STOCHASTIC, position=(0.0, 0.6, -3.4), angle=60.0)
+    return tris, mat, mats, lights, cam
+
+
+def render_c3_twin_fixture(iterations=256, runs=4):
+    tris, mat, mats, lights, cam = c3_twin()
+    out, secs = [], 0.0
+    for _ in range(runs):
+        img, t = O.ref_render(tris, mat, mats, lights, cam, C3_W, C3_H, max_bounces=C3_DEPTH, iterations=iterations)
+        out.append(img[..., :3].astype(np.float16))
+        secs += t
+    runs_arr = np.stack(out)
+    np.savez_compressed(OUT / "render_c3_twin.npz", runs=runs_arr, iterations=np.int64(iterations),
+                        width=np.int64(C3_W), height=np.int64(C3_H), bounces=np.int64(C3_DEPTH),
+                        seconds=np.float64(secs))
+    print("c3 twin: reference seconds", secs, "mean", runs_arr.astype(np.float64).mean())
 
 
 def render_scene(kind: str):
@@ -458,12 +490,14 @@ if __name__ == "__main__":
         cast_c2_fixture()
     if not only or "render_c1_twin" in only:
         render_c1_twin_fixture()
+    if not only or "render_c3_twin" in only:
+        render_c3_twin_fixture()
     if not only or "render" in only:
         render_fixtures()
     if not only or "textures" in only:
         texture_fixtures()
     for k in only:
-        if k == "render_c1_twin":
+        if k in ("render_c1_twin", "render_c3_twin"):
             continue
         if k.startswith("render_tex_"):
             texture_fixtures(kinds=(k[len("render_"):],))

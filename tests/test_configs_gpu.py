@@ -11,7 +11,12 @@ which the test reports).
 C1 (plain path trace, 256x256, 16 spp, depth 4): the physical estimator against the FP64 oracle
 (same counter-based random numbers) at 64 spp (four blended iterations of 16 spp); the
 reference-expressible twin in reference mode against the oracle per pixel and against four
-reference DumbRenderer runs (tests/golden/render_c1_twin.npz) statistically."""
+reference DumbRenderer runs (tests/golden/render_c1_twin.npz) statistically.
+
+C3 (the full path-trace scene): its reference-expressible twin (the level-8 displaced icosphere on a
+ground plane, DumbBased diffuse / metal and SimpleStochastic mirror materials, 4 spherical lights,
+depth 8), the benchmark's view at 96x54, in reference mode against four reference DumbRenderer runs
+(tests/golden/render_c3_twin.npz) statistically."""
 from pathlib import Path
 import sys
 
@@ -25,7 +30,7 @@ import _oracle as O
 
 GOLD = Path(__file__).resolve().parent / "golden"
 sys.path.insert(0, str(GOLD))
-from make_golden import C1_DEPTH, C1_SIZE, c1_twin, c2_rays, mesh_sha256  # noqa: E402
+from make_golden import C1_DEPTH, C1_SIZE, C3_DEPTH, C3_H, C3_W, c1_twin, c2_rays, c3_twin, mesh_sha256  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -187,3 +192,26 @@ def test_c1_twin_matches_reference_renderer_statistically(cuda):
     r.close()
     ratio, dm_se = compare_runs(runs, g["runs"].astype(np.float32))
     print(f"C1 twin vs reference DumbRenderer: MSE / expected {ratio:.3f}, mean difference {dm_se:+.2f} SE")
+
+
+def test_c3_twin_matches_reference_renderer_statistically(cuda):
+    """8 GPU runs of 256 spp (16x16 sub-pixels) against four reference DumbRenderer runs of 256
+    iterations of the full path-trace scene's twin (1,310,722 triangles, depth 8): MSE of the run
+    means within 1.5x of the variance the runs predict, image means within 4 standard errors."""
+    from _stats import compare_runs
+    g = np.load(GOLD / "render_c3_twin.npz")
+    assert int(g["width"]) == C3_W and int(g["height"]) == C3_H and int(g["bounces"]) == C3_DEPTH
+    tris, mat, mats, lights, cam = c3_twin()
+    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights, device_build=True)
+    r = dr.Renderer(1 << 22)
+    runs = []
+    for seed in range(300, 308):
+        p = dr.render_params(C3_W, C3_H, dr.MODE_REFERENCE, samples=(16, 16), max_bounces=C3_DEPTH, seed=seed)
+        fb = dr.new_frame_buffer(C3_W, C3_H, cuda)
+        r.render_blocks(sc, cam, fb, 0, dr.block_count(C3_W, C3_H), p)
+        torch.cuda.synchronize()
+        runs.append(dr.blockmajor_to_image(fb, C3_W, C3_H)[..., :3])
+    r.close()
+    sc.close()
+    ratio, dm_se = compare_runs(runs, g["runs"].astype(np.float32))
+    print(f"C3 twin vs reference DumbRenderer: MSE / expected {ratio:.3f}, mean difference {dm_se:+.2f} SE")
