@@ -12,8 +12,8 @@
 //   k_resolve         accumulators -> BlockBasedFrameBuffer<8,16> set / blend (BlockBasedFrameBuffer.impl.cuh:149-156)
 //
 // Wavefront design: queues are structure-of-arrays of float4/int4 records in HBM; work is pulled by
-// persistent warps through one atomic per warp; outputs are compacted with a warp ballot and one
-// atomic per warp.  Queue counts live in a device control block, so a whole wave is a fixed launch
+// persistent warps (shading: blocks) through one atomic per warp (block); outputs are compacted with
+// ballots and one atomic per warp (block; extension rays grouped by direction octant).  Queue counts live in a device control block, so a whole wave is a fixed launch
 // sequence with no host synchronisation (and can be captured in a CUDA graph).  Every path record
 // carries the index of its render job, so the paths of many scenes can share a wave (batches).
 #include <algorithm>
@@ -39,6 +39,46 @@ __device__ __forceinline__ int warp_alloc(int *counter, bool want) {
     if ((int)lane_id() == leader) base = atomicAdd(counter, __popc(ballot));
     base = __shfl_sync(0xFFFFFFFFu, base, leader);
     return want ? base + __popc(ballot & ((1u << lane_id()) - 1u)) : -1;
+}
+
+// Block-wide steps of the shading kernels (kShadeThreads threads, every thread calls both
+// together): fetch the block's next kShadeThreads queue entries, then allocate the children's
+// slots in the next queue with the block's children grouped by direction octant.  The block's
+// paths are neighbouring pixels of one sample, so a warp of the next trace gets rays leaving
+// nearby points into one octant, which descend the octree along the same nodes.
+constexpr int kShadeThreads = 256;
+struct ShadeBlockShared {
+    int base, out;
+    int cnt[kShadeThreads / 32][8];  // [warp][octant]: counts, then exclusive offsets
+};
+__device__ __forceinline__ int block_fetch(int *counter, ShadeBlockShared &sh) {
+    if (threadIdx.x == 0) sh.base = atomicAdd(counter, kShadeThreads);
+    __syncthreads();
+    return sh.base;
+}
+__device__ __forceinline__ int block_alloc_by_octant(int *counter, bool want, f3 dir, ShadeBlockShared &sh) {
+    const int oct = (dir.x < 0.0f) | ((dir.y < 0.0f) << 1) | ((dir.z < 0.0f) << 2);
+    const int wid = (int)(threadIdx.x >> 5);
+    unsigned mine = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, want && oct == k);
+        if (want && oct == k) mine = m;
+        if (lane_id() == 0) sh.cnt[wid][k] = __popc(m);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int total = 0;
+        for (int k = 0; k < 8; k++)
+            for (int v = 0; v < kShadeThreads / 32; v++) {
+                const int c = sh.cnt[v][k];
+                sh.cnt[v][k] = total;
+                total += c;
+            }
+        sh.out = total ? atomicAdd(counter, total) : 0;
+    }
+    __syncthreads();
+    return want ? sh.out + sh.cnt[wid][oct] + __popc(mine & ((1u << lane_id()) - 1u)) : -1;
 }
 
 // Warp-level work fetch from a dynamic counter; returns the base index (warp-uniform).
@@ -362,15 +402,16 @@ __global__ void __launch_bounds__(TT, TB) k_trace(WaveArgs A, int b) {
 // Reference semantics: one layer of DumbRenderer's state machine, with the layer gather folded
 // into a forward throughput (getReflectedColor is linear in the photon colour).
 template <bool MULTI>
-__global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
+__global__ void __launch_bounds__(kShadeThreads) k_shade_ref(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const Queue Q = A.q[b & 1];
     const Queue N = A.q[(b + 1) & 1];
     const int n = *((volatile int *)&C->ray_count[b]);
+    __shared__ ShadeBlockShared bs;
     for (;;) {
-        int base = warp_fetch(&C->fetch_shade[b]);
+        const int base = block_fetch(&C->fetch_shade[b], bs);
         if (base >= n) break;
-        int i = base + (int)lane_id();
+        int i = base + (int)threadIdx.x;
         bool active = i < n;
         int tri = -1;
         float4 p0, p1, p2;
@@ -454,7 +495,7 @@ __global__ void __launch_bounds__(256) k_shade_ref(WaveArgs A, int b) {
                 }
             }
         }
-        int w = warp_alloc(&C->ray_count[b + 1], child);
+        int w = block_alloc_by_octant(&C->ray_count[b + 1], child, cd, bs);
         if (child) {
             N.p0[w] = make_float4(hp.x, hp.y, hp.z, p0.w);
             N.p1[w] = make_float4(cd.x, cd.y, cd.z, p1.w);
@@ -534,7 +575,8 @@ struct RefPhotonSource {
 // Reference photon casts: the transparency rule puts shading on the cast path, so this kernel gets
 // its own register budget (kShadowRefBlocksPerSM blocks of kTraceThreads per SM).  At 3 blocks (80
 // registers) it spills about 200 bytes; at 2 (up to 128 registers) none.  Reference-mode twin of the
-// path trace (Mpaths/s, two runs each, 1 spp): 3 blocks 50.5 / 51.0, 2 blocks 56.5 / 56.3.
+// path trace (1920x1080 x 64 spp, Mpaths/s): 3 blocks 146.5, 2 blocks 152.7; 192 x 3, 128 x 5 and
+// 160 x 4 threads per SM compile to 96 registers with about 150 bytes of spills.
 constexpr int kShadowRefBlocksPerSM = 2;
 
 template <bool COUNT, bool MULTI>
@@ -576,15 +618,16 @@ __device__ __forceinline__ void scatter_albedo(const Item &I, const int *pre, in
 // Physical path step.  ADJ: adjoint pass (no image; gradients of emission hits are scattered here,
 // vertex triangles are recorded for the NEE gradients scattered by k_shadow_phys).
 template <bool MULTI, bool ADJ>
-__global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
+__global__ void __launch_bounds__(kShadeThreads) k_shade_phys(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
     const Queue Q = A.q[b & 1];
     const Queue N = A.q[(b + 1) & 1];
     const int n = *((volatile int *)&C->ray_count[b]);
+    __shared__ ShadeBlockShared bs;
     for (;;) {
-        int base = warp_fetch(&C->fetch_shade[b]);
+        const int base = block_fetch(&C->fetch_shade[b], bs);
         if (base >= n) break;
-        int i = base + (int)lane_id();
+        int i = base + (int)threadIdx.x;
         bool active = i < n;
         int tri = -1;
         float4 p0, p1, p2;
@@ -743,7 +786,7 @@ __global__ void __launch_bounds__(256) k_shade_phys(WaveArgs A, int b) {
             if (ADJ) A.sq.s3[ws] = make_float4(__int_as_float(path), __int_as_float(b), 0.0f, 0.0f);
             A.sq.s4[ws] = make_float4(scontrib.r, scontrib.g, scontrib.b, __int_as_float(p3.w));
         }
-        int w = warp_alloc(&C->ray_count[b + 1], child);
+        int w = block_alloc_by_octant(&C->ray_count[b + 1], child, nd, bs);
         if (child) {
             N.p0[w] = make_float4(hp.x, hp.y, hp.z, p0.w);
             N.p1[w] = make_float4(nd.x, nd.y, nd.z, p1.w);
@@ -1036,9 +1079,9 @@ static void launch_wave_t(const WaveDesc &W, const WaveArgs &A, cudaStream_t str
         else k_trace<false, MULTI, TT, TB><<<tgrid, TT, 0, stream>>>(A, b);
         P.end(KC_TRACE, stream);
         P.begin(KC_SHADE, stream);
-        if (W.mode == DR_MODE_REFERENCE) k_shade_ref<MULTI><<<grid, 256, 0, stream>>>(A, b);
-        else if (W.adjoint) k_shade_phys<MULTI, true><<<grid, 256, 0, stream>>>(A, b);
-        else k_shade_phys<MULTI, false><<<grid, 256, 0, stream>>>(A, b);
+        if (W.mode == DR_MODE_REFERENCE) k_shade_ref<MULTI><<<grid, kShadeThreads, 0, stream>>>(A, b);
+        else if (W.adjoint) k_shade_phys<MULTI, true><<<grid, kShadeThreads, 0, stream>>>(A, b);
+        else k_shade_phys<MULTI, false><<<grid, kShadeThreads, 0, stream>>>(A, b);
         P.end(KC_SHADE, stream);
         P.begin(KC_SHADOW, stream);
         if (W.mode == DR_MODE_REFERENCE) {
