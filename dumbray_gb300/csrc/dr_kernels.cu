@@ -623,7 +623,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade_phys(WaveArgs A, int b)
     const Queue Q = A.q[b & 1];
     const Queue N = A.q[(b + 1) & 1];
     const int n = *((volatile int *)&C->ray_count[b]);
-    __shared__ ShadeBlockShared bs;
+    __shared__ ShadeBlockShared bs, bss;  // fetch + extension rays; shadow rays
     for (;;) {
         const int base = block_fetch(&C->fetch_shade[b], bs);
         if (base >= n) break;
@@ -778,7 +778,7 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade_phys(WaveArgs A, int b)
                 if (child) nd = norm3(nd);
             }
         }
-        int ws = warp_alloc(&C->shadow_count[b], emit_shadow);
+        int ws = block_alloc_by_octant(&C->shadow_count[b], emit_shadow, sdir, bss);
         if (emit_shadow) {
             A.sq.s0[ws] = make_float4(hp.x, hp.y, hp.z, __int_as_float(slot));
             A.sq.s1[ws] = make_float4(sdir.x, sdir.y, sdir.z, __int_as_float(light_tri));
