@@ -620,9 +620,11 @@ def run_reference_twin_gpu(dr, torch, dev, a, S, peak, peak_src):
     1920x1080, 64 spp (8x8 sub-pixels), depth a.depth, i.e. the workload the reference arm times on
     host cores.  value: CUDA events over the timed frames, scene resident; e2e: the same through the
     public API with the frame buffer copied host->device and device->host every frame (pinned);
-    roofline: the photon casts (k_shadow_ref passes + k_photon_chain, the dominant kernel class),
-    algorithmic bytes = casts x (40 + 32 C_box + 36 C_tri) from the counting pass, over their busy
-    time; cpu_baseline: the reference DumbRenderer itself on a 240x136 x 1 spp sample of the frame."""
+    roofline: the photon casts (k_shadow_ref first casts + k_photon_chain transparency chains, the
+    dominant kernel class), algorithmic bytes = casts x (40 + 32 C_box + 36 C_tri) from the counting pass, over
+    their busy time; last_wave_counts: extension rays and photon records per bounce of the counting
+    pass's last wave (the whole frame when it is one wave), so casts / records is the photons' mean
+    cast count; cpu_baseline: the reference DumbRenderer itself on a 240x136 x 1 spp sample."""
     tris, mat, mats, lights = reference_twin(S, dr)
     t0 = time.time()
     sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights, device_build=True,
@@ -669,6 +671,7 @@ def run_reference_twin_gpu(dr, torch, dev, a, S, peak, peak_src):
     rend.set_counting(True)
     rend.render_blocks(sc, cam, fb, 0, nb, params(0), stream)
     cnt = rend.counters()
+    wave_rays, wave_photons = rend.wave_counts(a.depth + 1)
     rend.set_counting(False)
     rend.close()
     sc.close()
@@ -688,11 +691,13 @@ def run_reference_twin_gpu(dr, torch, dev, a, S, peak, peak_src):
                    "d2h_bytes_per_step": int(fb.numel() * 4)},
            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                         "frac": round(achieved / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
-                        "kernel": "k_shadow_ref (photon casts, continuations included)", "casts_per_frame": int(casts),
+                        "kernel": "k_shadow_ref + k_photon_chain (photon casts, chains included)", "casts_per_frame": int(casts),
                         "c_box": round(c_box, 2), "c_tri": round(c_tri, 2), "bytes_per_cast": round(bpr, 1),
                         "busy_ms_per_frame": round(shadow_ms, 2),
                         "basis": "photon-cast busy time (union of launch intervals over lanes) per frame"},
            "extension_rays_per_frame": int(cnt["trace_rays"]),
+           "last_wave_counts": {"extension": wave_rays, "photon_records": wave_photons,
+                                "single_wave": paths <= a.wave},
            "kernel_busy_ms_per_frame": {k: round(v / K, 2) for k, v in kbusy.items()},
            "kernel_launch_ms_sum_per_frame": {k: round(v[0] / K, 2) for k, v in kt.items()},
            "scene_build_s": round(build_s, 2)}

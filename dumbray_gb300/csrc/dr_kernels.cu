@@ -140,11 +140,12 @@ struct BatchSource {
         e = min(b + kChunk, n);
         return b < n;
     }
-    __device__ __forceinline__ void load(int i, f3 &ro, f3 &rd, int &ign, int &job) {
+    __device__ __forceinline__ bool load(int i, f3 &ro, f3 &rd, int &ign, int &job) {
         ro = mkf3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
         rd = mkf3(d[3 * i], d[3 * i + 1], d[3 * i + 2]);
         ign = ignore ? ignore[i] : -1;
         job = 0;
+        return true;
     }
     // single-scene source: never asked for a per-job scene (MULTI = false)
     __device__ __forceinline__ const Scene &scene(int) { return *scene0; }
@@ -178,6 +179,8 @@ struct Ctrl {
     int fetch_trace[kMaxBounceSlots];
     int fetch_shade[kMaxBounceSlots];
     int fetch_shadow[kMaxBounceSlots];
+    int blocked_count[kMaxBounceSlots];   // reference photons stopped by a blocker at bounce b
+    int fetch_chain[kMaxBounceSlots];
     int fetch_camera;
     int error;
 };
@@ -357,13 +360,14 @@ struct TraceSource {
     int n, chunk;
     long long rays, nb, nt;
     __device__ __forceinline__ bool next(int &b, int &e) { return fetch_chunk(fetch, n, chunk, b, e); }
-    __device__ __forceinline__ void load(int i, f3 &o, f3 &d, int &ign, int &job) {
+    __device__ __forceinline__ bool load(int i, f3 &o, f3 &d, int &ign, int &job) {
         float4 p0 = Q.p0[i], p1 = Q.p1[i];
         int4 p3 = Q.p3[i];
         o = f3of(p0);
         d = f3of(p1);
         ign = p3.x;
         job = p3.w;
+        return true;
     }
     __device__ __forceinline__ const Scene &scene(int job) { return job_of<MULTI>(*A, job).S; }
     __device__ __forceinline__ bool clip(int job) {
@@ -510,12 +514,16 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade_ref(WaveArgs A, int b) 
 // point; otherwise the blocker's reflected colour decides whether the photon continues (from just
 // past the blocker, with that colour, the blocker as the ignored object).
 //
-// Every cast of a photon, continuations included, runs on the persistent traversal engine in one
-// launch per bounce: a lane whose photon continues rewrites the photon's queue record in place and
-// starts the next cast at once (the engine's restart), so chains of any length keep their lane and
-// the launch ends when the last chain does, instead of one launch per continuation step.  At most
-// kPhotonCasts casts per photon (the oracle's bound, never reached by a photon that moves along
-// one line through finite geometry); the cast count travels in the record's s3.w.
+// Two launches per bounce on the persistent traversal engine.  k_shadow_ref casts every photon once
+// and settles those that arrive or miss; a photon stopped by a blocker stays in its record as
+// blocked (the hit point in s0, the blocker in s2.w, its cast count negated in s3.w) and its index
+// joins the bounce's blocked list.  k_photon_chain takes the blocked photons: the blocker's colour
+// decides whether each continues, and a continuing photon starts its next cast at once in the same
+// lane (its record rewritten in place, the engine's restart), so a chain of any length keeps its
+// lane.  Under 1% of the photons of the path-trace twin are ever blocked, but compiled into the
+// cast kernel the blocker shading and the chain restart cost every cast; kept apart, the cast kernel
+// holds no shading code.  At most kPhotonCasts casts per photon (the oracle's bound, never reached
+// by a photon that moves along one line through finite geometry); the count travels in s3.w.
 constexpr int kPhotonCasts = 64;
 
 __device__ __forceinline__ bool photon_arrives(const Hit &h, int target, f3 hp) {
@@ -527,20 +535,51 @@ __device__ __forceinline__ bool photon_arrives(const Hit &h, int target, f3 hp) 
 // registers do not weigh on the traversal it is reached from.
 __device__ __noinline__ c3 blocker_reflect(const Scene &S, int tri, f3 p, f3 ld) { return ref_reflect(S, tri, p, ld, ld, true, 0); }
 
+// Blocked photon lists live in the bounce's spent extension queue: in reference mode nothing reads
+// q[b & 1] between k_shade_ref(b) and k_shade_ref(b + 1), and its p0 plane (4 ints per path) holds
+// the bounce's photons (at most 2 per path of the wave's capacity).
+__device__ __forceinline__ int *blocked_list(const WaveArgs &A, int b) { return reinterpret_cast<int *>(A.q[b & 1].p0); }
+
+// Photon j, stopped by blocker `tri` at `p` after `casts` casts: the blocker's reflected colour
+// decides whether it continues; if so its record becomes the next cast.  False: the photon ends.
+template <bool MULTI>
+__device__ __forceinline__ bool photon_pass(const WaveArgs &A, const ShadowQ &sq, int j, int tri, f3 p, int casts) {
+    const float4 s3 = sq.s3[j];
+    const Scene &S = job_of<MULTI>(A, __float_as_int(sq.s4[j].w)).S;
+    const f3 ld = f3of(sq.s1[j]);
+    const c3 tr = cmul(blocker_reflect(S, tri, p, ld), mkc(s3.x, s3.y, s3.z));
+    if (!((tr.r + tr.g + tr.b) > kEps)) return false;
+    const f3 lo = add3(p, mul3(norm3(ld), 64.0f * kEps));
+    sq.s0[j] = make_float4(lo.x, lo.y, lo.z, sq.s0[j].w);
+    const float4 s2 = sq.s2[j];
+    sq.s2[j] = make_float4(s2.x, s2.y, s2.z, __int_as_float(tri));
+    sq.s3[j] = make_float4(tr.r, tr.g, tr.b, __int_as_float(casts));
+    return true;
+}
+
+// An arriving photon adds its colour to its pixel's accumulator.
+__device__ __forceinline__ void photon_arrive(const WaveArgs &A, const ShadowQ &sq, int j) {
+    const float4 s3 = sq.s3[j], s4 = sq.s4[j];
+    accum_add(A.accum, __float_as_int(sq.s0[j].w), mkc(s4.x * s3.x, s4.y * s3.y, s4.z * s3.z));
+}
+
+// First cast of every photon of a bounce (k_shadow_ref).
 template <bool MULTI>
 struct RefPhotonSource {
     static constexpr float kOccludeBelow = 0.0f;
     const WaveArgs *A;
     ShadowQ sq;
     int *fetch;
+    int *blocked, *blocked_count;
     int n, chunk;
     long long rays, nb, nt;
     __device__ __forceinline__ bool next(int &b, int &e) { return fetch_chunk(fetch, n, chunk, b, e); }
-    __device__ __forceinline__ void load(int i, f3 &o, f3 &d, int &ign, int &job) {
+    __device__ __forceinline__ bool load(int i, f3 &o, f3 &d, int &ign, int &job) {
         o = f3of(sq.s0[i]);
         d = f3of(sq.s1[i]);
         ign = __float_as_int(sq.s2[i].w);
         job = __float_as_int(sq.s4[i].w);
+        return true;
     }
     __device__ __forceinline__ const Scene &scene(int job) { return job_of<MULTI>(*A, job).S; }
     __device__ __forceinline__ bool clip(int job) { return job_of<MULTI>(*A, job).clip != 0; }
@@ -549,35 +588,65 @@ struct RefPhotonSource {
         nb += b_;
         nt += t_;
         if (h.tri < 0) return false;
-        // record planes are read where each branch needs them, so few values stay live in the
-        // traversal loop this is inlined into
         const float4 s2 = sq.s2[i];
         if (photon_arrives(h, __float_as_int(sq.s1[i].w), f3of(s2))) {
-            const float4 s3 = sq.s3[i], s4 = sq.s4[i];
-            accum_add(A->accum, __float_as_int(sq.s0[i].w), mkc(s4.x * s3.x, s4.y * s3.y, s4.z * s3.z));
+            photon_arrive(*A, sq, i);
             return false;
         }
-        const float4 s3 = sq.s3[i];
-        const int casts = __float_as_int(s3.w) + 1;
+        const int casts = __float_as_int(sq.s3[i].w) + 1;
         if (casts >= kPhotonCasts) return false;
-        const Scene &S = job_of<MULTI>(*A, __float_as_int(sq.s4[i].w)).S;
-        const f3 ld = f3of(sq.s1[i]);
-        const c3 tr = cmul(blocker_reflect(S, h.tri, h.p, ld), mkc(s3.x, s3.y, s3.z));
-        if (!((tr.r + tr.g + tr.b) > kEps)) return false;
-        const f3 lo = add3(h.p, mul3(norm3(ld), 64.0f * kEps));
-        sq.s0[i] = make_float4(lo.x, lo.y, lo.z, sq.s0[i].w);
+        sq.s0[i] = make_float4(h.p.x, h.p.y, h.p.z, sq.s0[i].w);
         sq.s2[i] = make_float4(s2.x, s2.y, s2.z, __int_as_float(h.tri));
-        sq.s3[i] = make_float4(tr.r, tr.g, tr.b, __int_as_float(casts));
-        return true;
+        reinterpret_cast<float *>(sq.s3 + i)[3] = __int_as_float(-casts);
+        blocked[atomicAdd(blocked_count, 1)] = i;
+        return false;
     }
 };
 
-// Reference photon casts: the transparency rule puts shading on the cast path, so this kernel gets
-// its own register budget (kShadowRefBlocksPerSM blocks of kTraceThreads per SM).  At 3 blocks (80
-// registers) it spills about 200 bytes; at 2 (up to 128 registers) none.  Reference-mode twin of the
-// path trace (1920x1080 x 64 spp, Mpaths/s): 3 blocks 146.5, 2 blocks 152.7; 192 x 3, 128 x 5 and
-// 160 x 4 threads per SM compile to 96 registers with about 150 bytes of spills.
-constexpr int kShadowRefBlocksPerSM = 2;
+// The blocked photons of a bounce and their chains (k_photon_chain); entry i is photon blocked[i].
+template <bool MULTI>
+struct RefPhotonChainSource {
+    static constexpr float kOccludeBelow = 0.0f;
+    const WaveArgs *A;
+    ShadowQ sq;
+    const int *blocked;
+    int *fetch;
+    int n, chunk;
+    long long rays, nb, nt;
+    __device__ __forceinline__ bool next(int &b, int &e) { return fetch_chunk(fetch, n, chunk, b, e); }
+    __device__ __forceinline__ bool load(int i, f3 &o, f3 &d, int &ign, int &job) {
+        const int j = blocked[i];
+        const int w = __float_as_int(sq.s3[j].w);
+        if (w < 0 && !photon_pass<MULTI>(*A, sq, j, __float_as_int(sq.s2[j].w), f3of(sq.s0[j]), -w)) return false;
+        o = f3of(sq.s0[j]);
+        d = f3of(sq.s1[j]);
+        ign = __float_as_int(sq.s2[j].w);
+        job = __float_as_int(sq.s4[j].w);
+        return true;
+    }
+    __device__ __forceinline__ const Scene &scene(int job) { return job_of<MULTI>(*A, job).S; }
+    __device__ __forceinline__ bool clip(int job) { return job_of<MULTI>(*A, job).clip != 0; }
+    __device__ __forceinline__ bool store(int i, const Hit &h, int b_, int t_) {
+        rays++;
+        nb += b_;
+        nt += t_;
+        if (h.tri < 0) return false;
+        const int j = blocked[i];
+        if (photon_arrives(h, __float_as_int(sq.s1[j].w), f3of(sq.s2[j]))) {
+            photon_arrive(*A, sq, j);
+            return false;
+        }
+        const int casts = __float_as_int(sq.s3[j].w) + 1;
+        if (casts >= kPhotonCasts) return false;
+        return photon_pass<MULTI>(*A, sq, j, h.tri, h.p, casts);
+    }
+};
+
+// Blocks per SM of the photon kernels (kTraceThreads threads each): the first-cast kernel holds no
+// shading and takes the traversal's own budget; the chain kernel, with the blocker shading, gets up
+// to 128 registers.
+constexpr int kShadowRefBlocksPerSM = 3;
+constexpr int kPhotonChainBlocksPerSM = 2;
 
 template <bool COUNT, bool MULTI>
 __global__ void __launch_bounds__(kTraceThreads, kShadowRefBlocksPerSM) k_shadow_ref(WaveArgs A, int b) {
@@ -586,7 +655,19 @@ __global__ void __launch_bounds__(kTraceThreads, kShadowRefBlocksPerSM) k_shadow
     if (n == 0) return;
     uint32_t stack[kStack];
     __shared__ WarpLeafSlots slots[kTraceThreads / 32];
-    RefPhotonSource<MULTI> src{&A, A.sq, &C->fetch_shadow[b], n, chunk_for(n), 0, 0, 0};
+    RefPhotonSource<MULTI> src{&A, A.sq, &C->fetch_shadow[b], blocked_list(A, b), &C->blocked_count[b], n, chunk_for(n), 0, 0, 0};
+    trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5]);
+    if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
+}
+
+template <bool COUNT, bool MULTI>
+__global__ void __launch_bounds__(kTraceThreads, kPhotonChainBlocksPerSM) k_photon_chain(WaveArgs A, int b) {
+    Ctrl *C = A.ctrl;
+    const int n = *((volatile int *)&C->blocked_count[b]);
+    if (n == 0) return;
+    uint32_t stack[kStack];
+    __shared__ WarpLeafSlots slots[kTraceThreads / 32];
+    RefPhotonChainSource<MULTI> src{&A, A.sq, blocked_list(A, b), &C->fetch_chain[b], n, chunk_for(n), 0, 0, 0};
     trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5]);
     if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
 }
@@ -807,11 +888,12 @@ struct ShadowPhysSource {
     int n, chunk;
     long long rays, nb, nt;
     __device__ __forceinline__ bool next(int &b, int &e) { return fetch_chunk(fetch, n, chunk, b, e); }
-    __device__ __forceinline__ void load(int i, f3 &o, f3 &d, int &ign, int &job) {
+    __device__ __forceinline__ bool load(int i, f3 &o, f3 &d, int &ign, int &job) {
         o = f3of(sq.s0[i]);
         d = f3of(sq.s1[i]);
         ign = __float_as_int(sq.s2[i].w);
         job = __float_as_int(sq.s4[i].w);
+        return true;
     }
     __device__ __forceinline__ const Scene &scene(int job) { return job_of<MULTI>(*A, job).S; }
     __device__ __forceinline__ bool clip(int) { return false; }
@@ -1086,8 +1168,15 @@ static void launch_wave_t(const WaveDesc &W, const WaveArgs &A, cudaStream_t str
         P.begin(KC_SHADOW, stream);
         if (W.mode == DR_MODE_REFERENCE) {
             const int sgrid = sm_count() * kShadowRefBlocksPerSM;   // one persistent block per slot
-            if (count) k_shadow_ref<true, MULTI><<<sgrid, kTraceThreads, 0, stream>>>(A, b);
-            else k_shadow_ref<false, MULTI><<<sgrid, kTraceThreads, 0, stream>>>(A, b);
+            const int cgrid = sm_count() * kPhotonChainBlocksPerSM;
+            if (count) {
+                k_shadow_ref<true, MULTI><<<sgrid, kTraceThreads, 0, stream>>>(A, b);
+                k_photon_chain<true, MULTI><<<cgrid, kTraceThreads, 0, stream>>>(A, b);
+            } else {
+                k_shadow_ref<false, MULTI><<<sgrid, kTraceThreads, 0, stream>>>(A, b);
+                k_photon_chain<false, MULTI><<<cgrid, kTraceThreads, 0, stream>>>(A, b);
+            }
+            nl++;
         } else if (W.adjoint) {
             k_shadow_phys<false, MULTI, true, TT, TB><<<tgrid, TT, 0, stream>>>(A, b);
         } else {

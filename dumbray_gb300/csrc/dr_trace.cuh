@@ -68,12 +68,13 @@ __device__ __forceinline__ int lane_start(const Scene &S, LaneRay &L) {
     return kTrav;
 }
 
-// A ray the source rewrote in place (a photon continuing past a blocker): the lane starts it at
-// once, without going back to the warp's chunk.
+// Loads entry i of the source into the lane and starts its ray; kIdle when the source has nothing
+// to trace for it.  Also serves a ray the source rewrote in place (a photon continuing past a
+// blocker): the lane starts it at once, without going back to the warp's chunk.
 template <bool COUNT, bool MULTI, class Source>
 __device__ __forceinline__ int restart(const Scene &S, Source &src, int i, LaneRay &L) {
     int ign, job;
-    src.load(i, L.o, L.d, ign, job);
+    if (!src.load(i, L.o, L.d, ign, job)) return kIdle;
     L.ignore = ign;
     return lane_start<COUNT>(MULTI ? src.scene(job) : S, L);
 }
@@ -86,7 +87,7 @@ struct WarpLeafSlots {
 
 // Source interface:
 //   bool next(int &begin, int &end)           warp-uniform; false when no work is left
-//   void load(int i, f3 &o, f3 &d, int &ignore, int &job)
+//   bool load(int i, f3 &o, f3 &d, int &ignore, int &job)   false: entry i needs no cast (done)
 //   const Scene &scene(int job)               the scene of a job (MULTI only)
 //   bool clip(int job)                        backface culling of a job (MULTI = false: job 0 for all)
 //   bool store(int i, const Hit &h, int nbox, int ntri)   true: ray i was rewritten (load() now
@@ -129,10 +130,7 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
                 int rank = __popc(want & lt_mask);
                 if (mode == kIdle && rank < avail) {
                     cur_i = c_next + rank;
-                    int ign, job;
-                    src.load(cur_i, L.o, L.d, ign, job);
-                    L.ignore = ign;
-                    mode = lane_start<COUNT>(MULTI ? src.scene(job) : S, L);
+                    mode = restart<COUNT, MULTI>(S, src, cur_i, L);
                 }
                 c_next += min(avail, __popc(want));
             }
