@@ -118,7 +118,8 @@ struct WaveScratch {
             if (e == cudaSuccess) e = cudaMalloc((void **)&q3[k], sizeof(int4) * wave);
         }
         if (e == cudaSuccess) e = cudaMalloc((void **)&hits, sizeof(float2) * wave);
-        for (int j = 0; j < 5 && e == cudaSuccess; j++) e = cudaMalloc((void **)&s[j], sizeof(float4) * shadow);
+        for (int j = 0; j < 5 && e == cudaSuccess; j++)
+            e = cudaMalloc((void **)&s[j], sizeof(float4) * drd::shadow_plane_records((int)shadow));
         if (e == cudaSuccess) e = cudaMalloc(&ctrl, drk::ctrl_bytes());
         return e;
     }
@@ -673,7 +674,8 @@ dr_status dr_renderer_create(int32_t wave_paths, dr_renderer **out) try {
         if (e == cudaSuccess) e = cudaMalloc((void **)&r->q3[k], sizeof(int4) * W);
     }
     if (e == cudaSuccess) e = cudaMalloc((void **)&r->hits, sizeof(float2) * W);
-    for (int j = 0; j < 5 && e == cudaSuccess; j++) e = cudaMalloc((void **)&r->s[j], sizeof(float4) * (size_t)r->shadow_capacity);
+    for (int j = 0; j < 5 && e == cudaSuccess; j++)
+        e = cudaMalloc((void **)&r->s[j], sizeof(float4) * drd::shadow_plane_records(r->shadow_capacity));
     if (e == cudaSuccess) e = cudaMalloc(&r->ctrl, drk::ctrl_bytes());
     if (e != cudaSuccess) {
         delete r;
@@ -866,6 +868,7 @@ static void wave_buffers(dr_renderer *r, drk::WaveDesc &W) {
     }
     W.hits = r->hits;
     for (int j = 0; j < 5; j++) W.s[j] = r->s[j];
+    W.shadow_cap = r->shadow_capacity;
     W.accum = r->accum;
     W.ctrl = r->ctrl;
     W.prefix = r->prefix;

@@ -179,8 +179,10 @@ struct Ctrl {
     int fetch_trace[kMaxBounceSlots];
     int fetch_shade[kMaxBounceSlots];
     int fetch_shadow[kMaxBounceSlots];
-    int blocked_count[kMaxBounceSlots];   // reference photons stopped by a blocker at bounce b
-    int fetch_chain[kMaxBounceSlots];
+    int blocked_count[kMaxBounceSlots];   // reference photons stopped by a blocker at bounce b and
+    int fetch_chain[kMaxBounceSlots];     // left in place (the carry region was full)
+    int carry_count;                      // blocked reference photons moved to the carry region
+    int fetch_carry;
     int fetch_camera;
     int error;
 };
@@ -209,6 +211,8 @@ struct WaveArgs {
     Queue q[2];
     float2 *hits;
     ShadowQ sq;
+    ShadowQ cq;             // carry region of the shadow planes (blocked reference photons)
+    int carry_cap;
     float *accum;           // [total slots][4]
     Ctrl *ctrl;
     unsigned long long *counters;  // counting pass only
@@ -514,16 +518,21 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade_ref(WaveArgs A, int b) 
 // point; otherwise the blocker's reflected colour decides whether the photon continues (from just
 // past the blocker, with that colour, the blocker as the ignored object).
 //
-// Two launches per bounce on the persistent traversal engine.  k_shadow_ref casts every photon once
-// and settles those that arrive or miss; a photon stopped by a blocker stays in its record as
-// blocked (the hit point in s0, the blocker in s2.w, its cast count negated in s3.w) and its index
-// joins the bounce's blocked list.  k_photon_chain takes the blocked photons: the blocker's colour
-// decides whether each continues, and a continuing photon starts its next cast at once in the same
-// lane (its record rewritten in place, the engine's restart), so a chain of any length keeps its
-// lane.  Under 1% of the photons of the path-trace twin are ever blocked, but compiled into the
-// cast kernel the blocker shading and the chain restart cost every cast; kept apart, the cast kernel
-// holds no shading code.  At most kPhotonCasts casts per photon (the oracle's bound, never reached
-// by a photon that moves along one line through finite geometry); the count travels in s3.w.
+// The casts run on the persistent traversal engine.  k_shadow_ref casts every photon of a bounce
+// once and settles those that arrive or miss; a photon stopped by a blocker becomes a blocked record
+// (the hit point in s0, the blocker in s2.w, its cast count negated in s3.w) in the wave's carry
+// region.  k_photon_chain, once per wave after the last bounce, takes the blocked photons: the
+// blocker's colour decides whether each continues, and a continuing photon starts its next cast at
+// once in the same lane (its record rewritten in place, the engine's restart), so a chain of any
+// length keeps its lane.  Under 1% of the photons of the path-trace twin are ever blocked, but
+// compiled into the cast kernel the blocker shading and the chain restart cost every cast, and a
+// chain launch per bounce would end every bounce with its longest chain; so the cast kernel holds
+// no shading code and the chains wait for the wave's end.  When the carry region is full a blocked
+// photon stays in its bounce's record and joins the bounce's blocked list (in the spent extension
+// queue), which a k_photon_chain launch right after the bounce's casts takes (an empty launch
+// otherwise).  Chains read nothing that later bounces write, so neither order changes a result.
+// At most kPhotonCasts casts per photon (the oracle's bound, never reached by a photon that moves
+// along one line through finite geometry); the count travels in s3.w.
 constexpr int kPhotonCasts = 64;
 
 __device__ __forceinline__ bool photon_arrives(const Hit &h, int target, f3 hp) {
@@ -570,6 +579,7 @@ struct RefPhotonSource {
     const WaveArgs *A;
     ShadowQ sq;
     int *fetch;
+    int *carry_count;
     int *blocked, *blocked_count;
     int n, chunk;
     long long rays, nb, nt;
@@ -593,17 +603,32 @@ struct RefPhotonSource {
             photon_arrive(*A, sq, i);
             return false;
         }
-        const int casts = __float_as_int(sq.s3[i].w) + 1;
+        const float4 s3 = sq.s3[i];
+        const int casts = __float_as_int(s3.w) + 1;
         if (casts >= kPhotonCasts) return false;
-        sq.s0[i] = make_float4(h.p.x, h.p.y, h.p.z, sq.s0[i].w);
-        sq.s2[i] = make_float4(s2.x, s2.y, s2.z, __int_as_float(h.tri));
-        reinterpret_cast<float *>(sq.s3 + i)[3] = __int_as_float(-casts);
-        blocked[atomicAdd(blocked_count, 1)] = i;
+        const float4 b0 = make_float4(h.p.x, h.p.y, h.p.z, sq.s0[i].w);
+        const float4 b2 = make_float4(s2.x, s2.y, s2.z, __int_as_float(h.tri));
+        const float4 b3 = make_float4(s3.x, s3.y, s3.z, __int_as_float(-casts));
+        const int k = atomicAdd(carry_count, 1);
+        if (k < A->carry_cap) {
+            const ShadowQ &cq = A->cq;
+            cq.s0[k] = b0;
+            cq.s1[k] = sq.s1[i];
+            cq.s2[k] = b2;
+            cq.s3[k] = b3;
+            cq.s4[k] = sq.s4[i];
+        } else {
+            sq.s0[i] = b0;
+            sq.s2[i] = b2;
+            sq.s3[i] = b3;
+            blocked[atomicAdd(blocked_count, 1)] = i;
+        }
         return false;
     }
 };
 
-// The blocked photons of a bounce and their chains (k_photon_chain); entry i is photon blocked[i].
+// Blocked photons and their chains (k_photon_chain): entry i is record blocked[i] of `sq` (a
+// bounce's records), or record i when `blocked` is null (the carry region).
 template <bool MULTI>
 struct RefPhotonChainSource {
     static constexpr float kOccludeBelow = 0.0f;
@@ -615,7 +640,7 @@ struct RefPhotonChainSource {
     long long rays, nb, nt;
     __device__ __forceinline__ bool next(int &b, int &e) { return fetch_chunk(fetch, n, chunk, b, e); }
     __device__ __forceinline__ bool load(int i, f3 &o, f3 &d, int &ign, int &job) {
-        const int j = blocked[i];
+        const int j = blocked ? blocked[i] : i;
         const int w = __float_as_int(sq.s3[j].w);
         if (w < 0 && !photon_pass<MULTI>(*A, sq, j, __float_as_int(sq.s2[j].w), f3of(sq.s0[j]), -w)) return false;
         o = f3of(sq.s0[j]);
@@ -631,7 +656,7 @@ struct RefPhotonChainSource {
         nb += b_;
         nt += t_;
         if (h.tri < 0) return false;
-        const int j = blocked[i];
+        const int j = blocked ? blocked[i] : i;
         if (photon_arrives(h, __float_as_int(sq.s1[j].w), f3of(sq.s2[j]))) {
             photon_arrive(*A, sq, j);
             return false;
@@ -655,19 +680,24 @@ __global__ void __launch_bounds__(kTraceThreads, kShadowRefBlocksPerSM) k_shadow
     if (n == 0) return;
     uint32_t stack[kStack];
     __shared__ WarpLeafSlots slots[kTraceThreads / 32];
-    RefPhotonSource<MULTI> src{&A, A.sq, &C->fetch_shadow[b], blocked_list(A, b), &C->blocked_count[b], n, chunk_for(n), 0, 0, 0};
+    RefPhotonSource<MULTI> src{&A, A.sq, &C->fetch_shadow[b], &C->carry_count, blocked_list(A, b), &C->blocked_count[b], n,
+                               chunk_for(n), 0, 0, 0};
     trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5]);
     if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
 }
 
+// b >= 0: bounce b's blocked list (photons the full carry region turned away); b < 0: the carry
+// region, after the wave's last bounce.
 template <bool COUNT, bool MULTI>
 __global__ void __launch_bounds__(kTraceThreads, kPhotonChainBlocksPerSM) k_photon_chain(WaveArgs A, int b) {
     Ctrl *C = A.ctrl;
-    const int n = *((volatile int *)&C->blocked_count[b]);
+    const bool carry = b < 0;
+    const int n = carry ? min(*((volatile int *)&C->carry_count), A.carry_cap) : *((volatile int *)&C->blocked_count[b]);
     if (n == 0) return;
     uint32_t stack[kStack];
     __shared__ WarpLeafSlots slots[kTraceThreads / 32];
-    RefPhotonChainSource<MULTI> src{&A, A.sq, blocked_list(A, b), &C->fetch_chain[b], n, chunk_for(n), 0, 0, 0};
+    RefPhotonChainSource<MULTI> src{&A, carry ? A.cq : A.sq, carry ? nullptr : blocked_list(A, b),
+                                    carry ? &C->fetch_carry : &C->fetch_chain[b], n, chunk_for(n), 0, 0, 0};
     trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5]);
     if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
 }
@@ -1141,6 +1171,12 @@ static void fill_args(const WaveDesc &W, WaveArgs &A, unsigned long long *counte
     A.sq.s2 = W.s[2];
     A.sq.s3 = W.s[3];
     A.sq.s4 = W.s[4];
+    A.carry_cap = carry_capacity(W.shadow_cap);
+    A.cq.s0 = W.s[0] + W.shadow_cap;
+    A.cq.s1 = W.s[1] + W.shadow_cap;
+    A.cq.s2 = W.s[2] + W.shadow_cap;
+    A.cq.s3 = W.s[3] + W.shadow_cap;
+    A.cq.s4 = W.s[4] + W.shadow_cap;
     A.accum = W.accum;
     A.ctrl = reinterpret_cast<Ctrl *>(W.ctrl);
     A.counters = counters;
@@ -1185,6 +1221,14 @@ static void launch_wave_t(const WaveDesc &W, const WaveArgs &A, cudaStream_t str
         }
         P.end(KC_SHADOW, stream);
         nl += 3;
+    }
+    if (W.mode == DR_MODE_REFERENCE) {   // the chains of the wave's blocked photons
+        const int cgrid = sm_count() * kPhotonChainBlocksPerSM;
+        P.begin(KC_SHADOW, stream);
+        if (count) k_photon_chain<true, MULTI><<<cgrid, kTraceThreads, 0, stream>>>(A, -1);
+        else k_photon_chain<false, MULTI><<<cgrid, kTraceThreads, 0, stream>>>(A, -1);
+        P.end(KC_SHADOW, stream);
+        nl++;
     }
 }
 

@@ -1,6 +1,7 @@
 // dr_kernels.h - host-visible launch interface of the device kernels (no torch types).
 #pragma once
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <utility>
 #include <vector>
 #include "../../include/dr_api.h"
@@ -9,6 +10,11 @@
 namespace drd {
 constexpr int kMaxBounceSlots = 68;  // bounce limit 64 (DUMB_RENDERER_BOUNCE_LIMIT) + camera + spare
 constexpr int kAdjDepth = 66;        // prefix slots per path in the adjoint pass (bounces 0..64)
+
+// Reference photons stopped by a blocker wait for their transparency chains in a carry region of
+// the shadow planes, behind the `shadow_cap` photon records of a bounce, until the end of the wave.
+constexpr int carry_capacity(int shadow_cap) { return std::max(1024, (shadow_cap / 16 + 31) / 32 * 32); }
+constexpr size_t shadow_plane_records(int shadow_cap) { return (size_t)shadow_cap + (size_t)carry_capacity(shadow_cap); }
 }
 
 namespace drk {
@@ -45,7 +51,8 @@ struct WaveDesc {
     float4 *q_p0[2], *q_p1[2], *q_p2[2];
     int4 *q_p3[2];
     float2 *hits;
-    float4 *s[5];
+    float4 *s[5];                // shadow planes of drd::shadow_plane_records(shadow_cap) records
+    int shadow_cap;
     float *accum;
     void *ctrl;
     int *prefix;                 // adjoint: [wave capacity][kAdjDepth] triangle of each path vertex

@@ -41,7 +41,7 @@ constexpr int kWavePaths = 32768;
 constexpr int kShadowRecords = 2 * kWavePaths;
 constexpr size_t kQueuePlane = align_up(sizeof(float4) * (size_t)kWavePaths);
 constexpr size_t kHits = align_up(sizeof(float2) * (size_t)kWavePaths);
-constexpr size_t kShadowPlane = align_up(sizeof(float4) * (size_t)kShadowRecords);
+constexpr size_t kShadowPlane = align_up(sizeof(float4) * drd::shadow_plane_records(kShadowRecords));
 constexpr size_t kAccum = align_up(sizeof(float4) * (size_t)DR_NOALLOC_MAX_BLOCKS * DR_BLOCK_W * DR_BLOCK_H);
 constexpr size_t kCtrl = 64 * 1024;
 constexpr size_t kOffQueues = 0;                       // 2 queues x 4 planes
@@ -127,6 +127,7 @@ extern "C" dr_status dr_render_blocks_noalloc(const dr_scene *sc, const dr_camer
     }
     W.hits = reinterpret_cast<float2 *>(base + kOffHits);
     for (int j = 0; j < 5; j++) W.s[j] = reinterpret_cast<float4 *>(base + kOffShadow + j * kShadowPlane);
+    W.shadow_cap = kShadowRecords;
     W.accum = accum;
     W.ctrl = base + kOffCtrl;
     W.prefix = nullptr;
