@@ -108,6 +108,8 @@ struct WaveScratch {
     float2 *hits = nullptr;
     float4 *s[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     void *ctrl = nullptr;
+    int *prefix = nullptr;          // adjoint: per-path vertex triangles (allocated by the first adjoint)
+    int prefix_paths = 0;
     cudaStream_t stream = nullptr;  // extra lanes only
     cudaEvent_t done = nullptr;     // extra lanes only
 
@@ -131,6 +133,7 @@ struct WaveScratch {
         cudaFree(hits);
         for (auto *p : s) cudaFree(p);
         cudaFree(ctrl);
+        cudaFree(prefix);
         if (done) cudaEventDestroy(done);
         if (stream) cudaStreamDestroy(stream);
         *this = WaveScratch();
@@ -943,6 +946,7 @@ static dr_status run_waves(dr_renderer *r, drk::WaveDesc &W, long long total, lo
             Wl.hits = x.hits;
             for (int j = 0; j < 5; j++) Wl.s[j] = x.s[j];
             Wl.ctrl = x.ctrl;
+            Wl.prefix = x.prefix;
             sl = x.stream;
         }
         Wl.wave_begin = b;
@@ -962,6 +966,17 @@ static dr_status run_waves(dr_renderer *r, drk::WaveDesc &W, long long total, lo
         if (e != cudaSuccess) return cuda_fail(e, "render: resolve");
     }
     return DR_OK;
+}
+
+// An adjoint lane's prefix buffer: kAdjDepth triangle indices per path of a wave.
+static cudaError_t ensure_prefix(int *&prefix, int &paths, long long wave) {
+    if (paths >= wave) return cudaSuccess;
+    cudaFree(prefix);
+    prefix = nullptr;
+    paths = 0;
+    cudaError_t e = cudaMalloc((void **)&prefix, sizeof(int) * (size_t)wave * drd::kAdjDepth);
+    if (e == cudaSuccess) paths = (int)wave;
+    return e;
 }
 
 static long long wave_size(const dr_renderer *r, int lights_per_path, long long cap) {
@@ -1012,16 +1027,17 @@ dr_status dr_render_adjoint(dr_renderer *r, const dr_scene *sc, const dr_camera 
     I.dl_dfb = dl_dfb;
     I.grad_albedo = grad_albedo;
     I.grad_emission = grad_emission;
-    const long long cap = 1LL << 20;  // paths per adjoint wave: bounds the prefix buffer to ~280 MB
-    const long long wave = wave_size(r, 1, cap);
-    if (r->prefix_paths < wave) {
-        cudaFree(r->prefix);
-        r->prefix = nullptr;
-        r->prefix_paths = 0;
-        cudaError_t e = cudaMalloc((void **)&r->prefix, sizeof(int) * (size_t)wave * drd::kAdjDepth);
-        if (e != cudaSuccess) return cuda_fail(e, "dr_render_adjoint: prefix buffer");
-        r->prefix_paths = (int)wave;
+    const long long cap = 1LL << 20;  // paths per adjoint wave: bounds each lane's prefix buffer to ~280 MB
+    const long long total = (long long)I.n_slots * I.spp;
+    const long long wave = lane_wave(total, wave_size(r, 1, cap), r->lanes);
+    const int L = lanes_used(total, wave, r->lanes);
+    if (L > 1) {
+        st = ensure_lanes(r, L - 1);
+        if (st != DR_OK) return st;
     }
+    cudaError_t e = ensure_prefix(r->prefix, r->prefix_paths, wave);
+    for (int k = 0; k < L - 1 && e == cudaSuccess; k++) e = ensure_prefix(r->extra[k].prefix, r->extra[k].prefix_paths, wave);
+    if (e != cudaSuccess) return cuda_fail(e, "dr_render_adjoint: prefix buffer");
     st = ensure_accum(r, (size_t)I.n_slots);
     if (st != DR_OK) return st;
     W.items = nullptr;
@@ -1030,7 +1046,7 @@ dr_status dr_render_adjoint(dr_renderer *r, const dr_scene *sc, const dr_camera 
     W.max_bounces = I.max_bounces;
     W.adjoint = true;
     wave_buffers(r, W);
-    return run_waves(r, W, (long long)I.n_slots * I.spp, wave, I.n_slots, stream, &r->prof, false, false);
+    return run_waves(r, W, total, wave, I.n_slots, stream, &r->prof, false, false, L);
 } catch (...) {
     return dr_internal_exception("dr_render_adjoint");
 }

@@ -931,23 +931,11 @@ struct ShadowPhysSource {
         int light_tri = __float_as_int(sq.s1[i].w);
         bool vis = (h.tri < 0) || (h.tri == light_tri) || !(h.t < 0.999f);
         if (vis) {
-            float4 s4 = sq.s4[i];
-            c3 c = mkc(s4.x, s4.y, s4.z);
-            int slot = __float_as_int(sq.s0[i].w);
             if (ADJ) {
-                const Item &I = job_of<MULTI>(*A, __float_as_int(s4.w));
-                float4 s3 = sq.s3[i];
-                int path = __float_as_int(s3.x), vtx = __float_as_int(s3.y);
-                c3 delta = pixel_adjoint(I, slot);
-                const float *lep = I.S.emission + 3 * (size_t)light_tri;
-                float lr = __ldg(lep), lg = __ldg(lep + 1), lb = __ldg(lep + 2);
-                float *g = I.grad_emission + 3 * (size_t)light_tri;
-                if (lr > 0.0f && delta.r != 0.0f) atomicAdd(g, delta.r * c.r / lr);
-                if (lg > 0.0f && delta.g != 0.0f) atomicAdd(g + 1, delta.g * c.g / lg);
-                if (lb > 0.0f && delta.b != 0.0f) atomicAdd(g + 2, delta.b * c.b / lb);
-                scatter_albedo(I, A->prefix + (size_t)path * kAdjDepth, vtx, delta, c);
+                reinterpret_cast<float *>(sq.s2 + i)[0] = 1.0f;  // visible: k_adj_shadow scatters its gradients
             } else {
-                accum_add(accum, slot, c);
+                float4 s4 = sq.s4[i];
+                accum_add(accum, __float_as_int(sq.s0[i].w), mkc(s4.x, s4.y, s4.z));
             }
         }
         rays++;
@@ -956,6 +944,31 @@ struct ShadowPhysSource {
         return false;
     }
 };
+
+// Adjoint pass: gradients of the visible NEE contributions of bounce b (k_shadow_phys<ADJ> marks a
+// visible record with s2.x = 1; k_shade_phys writes s2 = {0, 0, 0, tri}), scattered here rather
+// than in the traversal kernel, whose registers then stay the traversal's.
+template <bool MULTI>
+__global__ void __launch_bounds__(256) k_adj_shadow(WaveArgs A, int b) {
+    const int n = *((volatile int *)&A.ctrl->shadow_count[b]);
+    for (int i = (int)(blockIdx.x * blockDim.x + threadIdx.x); i < n; i += (int)(gridDim.x * blockDim.x)) {
+        if (A.sq.s2[i].x == 0.0f) continue;
+        const float4 s4 = A.sq.s4[i];
+        const c3 c = mkc(s4.x, s4.y, s4.z);
+        const Item &I = job_of<MULTI>(A, __float_as_int(s4.w));
+        const float4 s3 = A.sq.s3[i];
+        const int path = __float_as_int(s3.x), vtx = __float_as_int(s3.y);
+        const int light_tri = __float_as_int(A.sq.s1[i].w);
+        const c3 delta = pixel_adjoint(I, __float_as_int(A.sq.s0[i].w));
+        const float *lep = I.S.emission + 3 * (size_t)light_tri;
+        const float lr = __ldg(lep), lg = __ldg(lep + 1), lb = __ldg(lep + 2);
+        float *g = I.grad_emission + 3 * (size_t)light_tri;
+        if (lr > 0.0f && delta.r != 0.0f) atomicAdd(g, delta.r * c.r / lr);
+        if (lg > 0.0f && delta.g != 0.0f) atomicAdd(g + 1, delta.g * c.g / lg);
+        if (lb > 0.0f && delta.b != 0.0f) atomicAdd(g + 2, delta.b * c.b / lb);
+        scatter_albedo(I, A.prefix + (size_t)path * kAdjDepth, vtx, delta, c);
+    }
+}
 
 // Physical visibility: closest hit from the shading point toward the sampled light point
 // (direction = light point - shading point, so the light is at t = 1), ignoring the shading
@@ -1215,6 +1228,8 @@ static void launch_wave_t(const WaveDesc &W, const WaveArgs &A, cudaStream_t str
             nl++;
         } else if (W.adjoint) {
             k_shadow_phys<false, MULTI, true, TT, TB><<<tgrid, TT, 0, stream>>>(A, b);
+            k_adj_shadow<MULTI><<<grid, 256, 0, stream>>>(A, b);
+            nl++;
         } else {
             if (count) k_shadow_phys<true, MULTI, false, TT, TB><<<tgrid, TT, 0, stream>>>(A, b);
             else k_shadow_phys<false, MULTI, false, TT, TB><<<tgrid, TT, 0, stream>>>(A, b);
