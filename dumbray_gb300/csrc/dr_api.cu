@@ -410,14 +410,28 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
         if (l.type == DR_LIGHT_SPOTLIGHT) spotlight_state(l, d);
     }
 
-    // child boxes of every node group as planes of 8 (see drd::Scene::gbox)
+    // child boxes of every node group as planes of 8 (see drd::Scene::gbox).  An empty leaf keeps
+    // nearly its whole octant box (reduceNode has nothing to shrink it to), so rays would enter
+    // empty leaves far more often than their number suggests (on a displaced sphere they hold about
+    // 2/3 of the leaves' surface area); they yield no hit and add to neither count of a cast (no
+    // triangles; the box-test count corrections follow the children taken on the way to a hit).
+    // Their group-test box is a point at kFar on every axis, which a ray reaches only if its three
+    // slab distances to it coincide; such a ray just enters the empty leaf, as it would otherwise.
+    constexpr float kFar = 1e30f;
+    auto bits = [](float f) {
+        int i;
+        std::memcpy(&i, &f, 4);
+        return i;
+    };
     std::vector<float> gbox(48 * (nodes.size() / 16));
     for (size_t g = 0; g < nodes.size() / 16; g++)
         for (int c = 0; c < 8; c++) {
             const float4 lo = nodes[16 * g + 2 * c], hi = nodes[16 * g + 2 * c + 1];
             float *p = &gbox[48 * g];
-            p[c] = lo.x; p[8 + c] = lo.y; p[16 + c] = lo.z;
-            p[24 + c] = hi.x; p[32 + c] = hi.y; p[40 + c] = hi.z;
+            const int w = bits(lo.w), cnt = bits(hi.w);
+            const bool empty = w < 0 && cnt == 0;
+            p[c] = empty ? kFar : lo.x; p[8 + c] = empty ? kFar : lo.y; p[16 + c] = empty ? kFar : lo.z;
+            p[24 + c] = empty ? kFar : hi.x; p[32 + c] = empty ? kFar : hi.y; p[40 + c] = empty ? kFar : hi.z;
         }
     float4 *d_nodes = nullptr, *d_gbox = nullptr, *d_leaf = nullptr, *d_tris = nullptr, *d_nrms = nullptr;
     int *d_mat = nullptr;
