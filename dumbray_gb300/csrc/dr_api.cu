@@ -410,36 +410,73 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
         if (l.type == DR_LIGHT_SPOTLIGHT) spotlight_state(l, d);
     }
 
-    // child boxes of every node group as planes of 8 (see drd::Scene::gbox).  An empty leaf keeps
-    // nearly its whole octant box (reduceNode has nothing to shrink it to), so rays would enter
-    // empty leaves far more often than their number suggests (on a displaced sphere they hold about
-    // 2/3 of the leaves' surface area); they yield no hit and add to neither count of a cast (no
-    // triangles; the box-test count corrections follow the children taken on the way to a hit).
-    // Their group-test box is a point at kFar on every axis, which a ray reaches only if its three
-    // slab distances to it coincide; such a ray just enters the empty leaf, as it would otherwise.
+    // Child boxes of every node group as planes of 8 (see drd::Scene::gbox), in two versions.
+    //  * gbox_ref: the reference's boxes, except that an empty leaf's box is a point at kFar on every
+    //    axis.  reduceNode has nothing to shrink an empty leaf to, so it keeps nearly its whole octant
+    //    box, and on a displaced sphere the empty leaves hold about 2/3 of the leaves' surface area.
+    //    An empty leaf yields no hit and adds to neither count of a cast (no triangles; the box-test
+    //    count corrections follow the children taken on the way to a hit), and a ray reaches the far
+    //    point only if its three slab distances to it coincide, when it just enters the empty leaf.
+    //    The counting traversals of reference-padding scenes read these, so their counts are the
+    //    reference's.
+    //  * gbox: the boxes refitted to the non-empty leaves below (a leaf's own box; an inner node's
+    //    union of its non-empty children's refitted boxes, empty subtrees at kFar).  The reference's
+    //    inner boxes are unions that include the empty leaves' octant boxes; the refitted ones have
+    //    about a third of their surface area.  A ray that misses a refitted box (the slab test's
+    //    rounding is monotone in the box) misses every non-empty leaf box below it, so no leaf below
+    //    could accept a hit: the visited leaves that matter, their order and every result are the
+    //    reference's.  Every other traversal reads these.
     constexpr float kFar = 1e30f;
-    auto bits = [](float f) {
-        int i;
-        std::memcpy(&i, &f, 4);
-        return i;
+    const int64_t NN = T.node_count;
+    std::vector<float> fit_lo(3 * (size_t)NN), fit_hi(3 * (size_t)NN);
+    std::vector<uint8_t> fit_live((size_t)NN, 0);
+    auto refit_children = [&](int64_t first, float *lo, float *hi) {
+        bool any = false;
+        for (int k = 0; k < 3; k++) { lo[k] = kFar; hi[k] = -kFar; }
+        for (int c = 0; c < 8; c++) {
+            const int64_t j = first + c;
+            if (!fit_live[j]) continue;
+            any = true;
+            for (int k = 0; k < 3; k++) {
+                lo[k] = std::fmin(lo[k], fit_lo[3 * j + k]);
+                hi[k] = std::fmax(hi[k], fit_hi[3 * j + k]);
+            }
+        }
+        return any;
     };
-    std::vector<float> gbox(48 * (nodes.size() / 16));
+    // node order is breadth-first (children after their parent), so reverse order is bottom-up
+    for (int64_t i = NN - 1; i >= 0; i--) {
+        if (T.node_child[i] < 0) {
+            fit_live[i] = T.node_leaf_count[i] > 0;
+            for (int k = 0; k < 3; k++) { fit_lo[3 * i + k] = T.node_lo[3 * i + k]; fit_hi[3 * i + k] = T.node_hi[3 * i + k]; }
+        } else {
+            fit_live[i] = refit_children(T.node_child[i], &fit_lo[3 * i], &fit_hi[3 * i]) ? 1 : 0;
+        }
+    }
+    std::vector<float> gbox(48 * (nodes.size() / 16)), gbox_ref(48 * (nodes.size() / 16));
     for (size_t g = 0; g < nodes.size() / 16; g++)
         for (int c = 0; c < 8; c++) {
-            const float4 lo = nodes[16 * g + 2 * c], hi = nodes[16 * g + 2 * c + 1];
-            float *p = &gbox[48 * g];
-            const int w = bits(lo.w), cnt = bits(hi.w);
-            const bool empty = w < 0 && cnt == 0;
-            p[c] = empty ? kFar : lo.x; p[8 + c] = empty ? kFar : lo.y; p[16 + c] = empty ? kFar : lo.z;
-            p[24 + c] = empty ? kFar : hi.x; p[32 + c] = empty ? kFar : hi.y; p[40 + c] = empty ? kFar : hi.z;
+            const int64_t j = 8 * (int64_t)g + c;
+            const bool empty_leaf = T.node_child[j] < 0 && T.node_leaf_count[j] == 0;
+            float *p = &gbox_ref[48 * g];
+            for (int k = 0; k < 3; k++) {
+                p[8 * k + c] = empty_leaf ? kFar : T.node_lo[3 * j + k];
+                p[24 + 8 * k + c] = empty_leaf ? kFar : T.node_hi[3 * j + k];
+            }
+            float *q = &gbox[48 * g];
+            for (int k = 0; k < 3; k++) {
+                q[8 * k + c] = fit_live[j] ? fit_lo[3 * j + k] : kFar;
+                q[24 + 8 * k + c] = fit_live[j] ? fit_hi[3 * j + k] : kFar;
+            }
         }
-    float4 *d_nodes = nullptr, *d_gbox = nullptr, *d_leaf = nullptr, *d_tris = nullptr, *d_nrms = nullptr;
+    float4 *d_nodes = nullptr, *d_gbox = nullptr, *d_gbox_ref = nullptr, *d_leaf = nullptr, *d_tris = nullptr, *d_nrms = nullptr;
     int *d_mat = nullptr;
     drd::Material *d_mats = nullptr;
     drd::Light *d_lights = nullptr;
     cudaError_t e = upload(&d_nodes, nodes.data(), nodes.size());
     if (e == cudaSuccess) { sc->allocs.push_back(d_nodes); e = upload(&d_gbox, (const float4 *)gbox.data(), gbox.size() / 4); }
-    if (e == cudaSuccess) { sc->allocs.push_back(d_gbox); e = upload(&d_leaf, leaf_tris.data(), leaf_tris.size()); }
+    if (e == cudaSuccess) { sc->allocs.push_back(d_gbox); e = upload(&d_gbox_ref, (const float4 *)gbox_ref.data(), gbox_ref.size() / 4); }
+    if (e == cudaSuccess) { sc->allocs.push_back(d_gbox_ref); e = upload(&d_leaf, leaf_tris.data(), leaf_tris.size()); }
     if (e == cudaSuccess) { sc->allocs.push_back(d_leaf); e = upload(&d_tris, tris.data(), tris.size()); }
     if (e == cudaSuccess) { sc->allocs.push_back(d_tris); e = upload(&d_nrms, nrms.data(), nrms.size()); }
     if (e == cudaSuccess) { sc->allocs.push_back(d_nrms); e = upload(&d_mat, sc->mat_id.data(), sc->mat_id.size()); }
@@ -455,6 +492,7 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
     drd::Scene &S = sc->dev;
     S.nodes = d_nodes;
     S.gbox = d_gbox;
+    S.gbox_ref = d_gbox_ref;
     S.leaf_tris = d_leaf;
     S.tris = d_tris;
     S.nrms = d_nrms;
@@ -1158,6 +1196,7 @@ static dr_status build_arena(dr_batch *b) {
         drd::Scene &S = b->items[i].S;
         S.nodes = b->arena_nodes;
         S.gbox = b->arena_gbox;
+        S.gbox_ref = b->arena_gbox;   // batches do not run the counting traversal
         S.leaf_tris = b->arena_leaf;
         if (S.root_child >= 0) S.root_child += (int)(node_off[k] / 8);
         S.root_leaf_first += (int)leaf_off[k];

@@ -50,7 +50,8 @@ struct Scene {
     const float4 *nodes;
     // The same child boxes per node group as planes of 8 floats (lo.x, lo.y, lo.z, hi.x, hi.y, hi.z;
     // 12 float4 = 192 B per group), read by the group tests: 12 vector loads instead of 16.
-    const float4 *gbox;
+    const float4 *gbox;         // child boxes of each node group as planes (refitted to non-empty leaves)
+    const float4 *gbox_ref;     // the same with the reference's boxes (counting on reference-padding scenes)
     const float4 *leaf_tris;
     const float4 *tris;
     const float4 *nrms;
@@ -283,12 +284,13 @@ __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool cl
                          S.root_hi[1], S.root_hi[2], o, d, clip, ignore, h, ntri);
     if (COUNT) nbox++;
     const bool front = !COUNT || S.front_only != 0;
+    const float4 *G = front ? S.gbox : S.gbox_ref;
     if (!slab_hit(S.root_lo[0], S.root_lo[1], S.root_lo[2], S.root_hi[0], S.root_hi[1], S.root_hi[2], o, inv, front)) return false;
     const int order = (d.z < 0 ? 1 : 0) + (d.y < 0 ? 2 : 0) + (d.x < 0 ? 4 : 0);
     constexpr int GS = group_shift<COUNT>();
     uint32_t stack[kStack];
     int sp = 0;
-    uint32_t cur = ((uint32_t)S.root_child << GS) | test_group(S.gbox, S.root_child, order, o, inv, front);
+    uint32_t cur = ((uint32_t)S.root_child << GS) | test_group(G, S.root_child, order, o, inv, front);
     if (COUNT) nbox += 8;
     for (;;) {
         uint32_t m = cur & 0xFFu;
@@ -315,7 +317,7 @@ __device__ __forceinline__ bool cast_closest(const Scene &S, f3 o, f3 d, bool cl
         } else {
             if (sp >= kStack) return false;  // unreachable for trees of depth <= 24
             stack[sp++] = COUNT ? ((cur & ~(7u << 8)) | ((uint32_t)k << 8)) : cur;
-            cur = ((uint32_t)(w >> 3) << GS) | test_group(S.gbox, w >> 3, order, o, inv, front);
+            cur = ((uint32_t)(w >> 3) << GS) | test_group(G, w >> 3, order, o, inv, front);
             if (COUNT) nbox += 8;
         }
     }

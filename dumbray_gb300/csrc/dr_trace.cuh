@@ -62,7 +62,7 @@ __device__ __forceinline__ int lane_start(const Scene &S, LaneRay &L) {
     const bool front = !COUNT || S.front_only != 0;
     if (slab_hit(S.root_lo[0], S.root_lo[1], S.root_lo[2], S.root_hi[0], S.root_hi[1], S.root_hi[2], L.o, L.inv, front)) {
         L.cur = ((uint32_t)S.root_child << group_shift<COUNT>()) |
-                test_group(S.gbox, S.root_child, L.order, L.o, L.inv, front);
+                test_group(front ? S.gbox : S.gbox_ref, S.root_child, L.order, L.o, L.inv, front);
         if (COUNT) L.nb += 8;
     }
     return kTrav;
@@ -113,6 +113,9 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
     constexpr int GS = group_shift<COUNT>();
     const bool clip = src.clip(0);
     const bool front = !COUNT || S.front_only != 0;   // uniform: one scene, or one arena of a batch
+    // group-test planes: refitted, except for counting on reference-padding scenes (their counts are
+    // the reference's)
+    const float4 *G = front ? S.gbox : S.gbox_ref;
     LaneRay L;
     L.r = 0;
     L.r_end = 0;
@@ -169,7 +172,7 @@ __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, ui
                     mode = kLeaf;
                 } else if (L.sp < kStack) {
                     stack[L.sp++] = COUNT ? ((L.cur & ~(7u << 8)) | ((uint32_t)k << 8)) : L.cur;
-                    L.cur = ((uint32_t)(w >> 3) << GS) | test_group(S.gbox, w >> 3, L.order, L.o, L.inv, front);
+                    L.cur = ((uint32_t)(w >> 3) << GS) | test_group(G, w >> 3, L.order, L.o, L.inv, front);
                     if (COUNT) L.nb += 8;
                 } else {  // unreachable for depth <= 24: finish as a miss rather than overflow
                     L.cur = 0;
