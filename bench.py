@@ -74,9 +74,10 @@ def parse():
     ap.add_argument("--twin-tree", default="reference", choices=["reference", "physical"],
                     help="octree padding of the reference-mode twin scene")
     ap.add_argument("--lanes", type=int, default=0, help="concurrent wave pipelines per renderer (0 = library default)")
-    ap.add_argument("--split", type=int, default=12,
-                    help="octree leaf split threshold of the path-trace scene (12: best of 8/12/16/24 on this "
-                         "workload with the physical-mode padding; the reference uses 8)")
+    ap.add_argument("--split", type=int, default=4,
+                    help="octree leaf split threshold of the path-trace scene (4: with 3 the best of 2-24 on this "
+                         "workload with the physical-mode padding and the refitted group-test planes; the "
+                         "reference uses 8)")
     ap.add_argument("--ref-tree", action="store_true",
                     help="build the path-trace scene with the reference's octree padding (1.28e-3) instead of the "
                          "physical-mode padding scaled to the coordinates")
@@ -105,7 +106,7 @@ def build_scene(dr, level, split=0, ref_tree=False):
     mats = [dr.lambert(), dr.mirror(), dr.glossy()]
     t0 = time.time()
     S["box_epsilon"] = 0.0 if ref_tree else dr.tight_box_epsilon(S["tris"])
-    S["split"] = split if split > 0 else 8
+    S["split"] = 8 if ref_tree else (split if split > 0 else 8)   # the reference's tree: its split rule and 8
     scene = dr.Scene(S["tris"], mat_id=S["mat_id"], materials=mats, split_threshold=S["split"],
                      box_epsilon=0.0 if ref_tree else dr.PHYSICAL_TREE, device_build=True)
     scene.set_triangle_params(S["albedo"], S["emission"], S["roughness"])

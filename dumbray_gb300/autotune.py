@@ -44,7 +44,7 @@ def _time_ms(fn, reps: int = 2) -> float:
 
 
 def tune_leaf_threshold(make_scene, scenes_by_class, camera_for, probe=(512, 512, 4), depth=6,
-                        candidates=(8, 12, 16, 24), device="cuda"):
+                        candidates=(3, 4, 6, 8, 12), device="cuda"):
     """make_scene(job, split_threshold) -> dr.Scene; scenes_by_class: {class: job} representative
     jobs; camera_for(job) -> dr camera.  Renders a probe frame (width, height, spp) of every
     representative with each candidate threshold; returns ({class: best}, {class: {cand: ms}})."""

@@ -50,7 +50,9 @@ typedef struct dr_renderer dr_renderer;
  * coordinate (margin for the rounding of hit points in the leaf-box acceptance test).  Traversals
  * skip octree boxes lying entirely behind the ray origin, which the reference's slab test keeps
  * (clipBackface = false) although no hit at t > 0 can come of them; dr_cast_counted, whose counts
- * reproduce the reference's, keeps them on scenes built with box_epsilon = 0. */
+ * reproduce the reference's, keeps them on scenes built with box_epsilon = 0.
+ * split_threshold: 0 = the reference's 8.  With a scene-scaled box_epsilon smaller leaves pay: a
+ * 1.31M-triangle displaced sphere path-traces fastest at 3-4 (793 Mpaths/s against 754 at 8). */
 typedef struct {
     int32_t max_depth;
     int32_t split_threshold;
