@@ -36,9 +36,9 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Mpaths/s 1080p 64spp on 1 GB300: plain vs batched, fwd vs fwd+adjoint, at RMSE"
 # DRAM bytes (read + write) per extension ray of k_trace: ncu dram__bytes_read.sum + dram__bytes_write.sum
 # of the bounce-1 launch of a 960x544, 4 spp frame of the same scene, camera and octree rendered as one
-# wave (346.9 MB over its 1,375,097 rays, caches flushed before the launch); the `traffic` of an average
+# wave (458.9 MB over its 1,375,097 rays, caches flushed before the launch); the `traffic` of an average
 # full-size launch is this times its ray count.
-TRACE_DRAM_BYTES_PER_RAY = 252.3
+TRACE_DRAM_BYTES_PER_RAY = 333.7
 UNIT = "Mpaths/s"
 
 
