@@ -146,6 +146,8 @@ def lib() -> ctypes.CDLL:
     L.dr_octree_stats.argtypes = [vp, P(i64), P(i64), P(i64), P(i32)]
     L.dr_octree_export.restype = i32
     L.dr_octree_export.argtypes = [vp, vp, vp, vp, vp]
+    L.dr_octree_group_planes.restype = i32
+    L.dr_octree_group_planes.argtypes = [vp, vp, vp]
     L.dr_octree_destroy.restype = None
     L.dr_octree_destroy.argtypes = [vp]
     L.dr_cast.restype = i32
@@ -553,6 +555,34 @@ def build_octree_host(tris, max_depth=0, split_threshold=0, threads=0, box_epsil
         check(L.dr_octree_export(h, box.ctypes.data, child.ctypes.data, leaf.ctypes.data, ref.ctypes.data))
         stats = dict(nodes=nodes.value, leaves=leaves.value, refs=refs.value, depth=depth.value)
         return stats, box, child, leaf, ref[: refs.value]
+    finally:
+        L.dr_octree_destroy(h)
+
+
+def octree_group_planes_host(tris, split_threshold=0, box_epsilon=0.0):
+    """Host-only octree build and its group-test planes (dr_octree_group_planes): returns
+    (box, child, leaf, gbox, gbox_ref) with box/child/leaf as build_octree_host (node 0 = root) and
+    gbox / gbox_ref float32 [(nodes - 1) / 8, 6, 8] (lo x/y/z, hi x/y/z planes of each group's 8
+    children; group g = export nodes 8g + 1 .. 8g + 8)."""
+    L = lib()
+    t = np.ascontiguousarray(tris, dtype=np.float32).reshape(-1, 3, 3)
+    bp = DrBuildParams(0, split_threshold, 0, box_epsilon, 0)
+    h = ctypes.c_void_p()
+    check(L.dr_octree_create_host(t.ctypes.data, len(t), ctypes.byref(bp), ctypes.byref(h)))
+    try:
+        nodes, leaves, refs = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        depth = ctypes.c_int32()
+        check(L.dr_octree_stats(h, ctypes.byref(nodes), ctypes.byref(leaves), ctypes.byref(refs), ctypes.byref(depth)))
+        box = np.zeros((nodes.value, 6), np.float32)
+        child = np.zeros(nodes.value, np.int32)
+        leaf = np.zeros((nodes.value, 2), np.int32)
+        ref = np.zeros(max(1, refs.value), np.int32)
+        check(L.dr_octree_export(h, box.ctypes.data, child.ctypes.data, leaf.ctypes.data, ref.ctypes.data))
+        groups = (nodes.value - 1) // 8
+        g = np.zeros((max(groups, 1), 6, 8), np.float32)
+        r = np.zeros((max(groups, 1), 6, 8), np.float32)
+        check(L.dr_octree_group_planes(h, g.ctypes.data, r.ctypes.data))
+        return box, child, leaf, g[:groups], r[:groups]
     finally:
         L.dr_octree_destroy(h)
 

@@ -292,6 +292,71 @@ static void spotlight_state(const dr_light &l, drd::Light &d) {
     d.sphere = l.emit_from_sphere ? 1 : 0;
 }
 
+// Child boxes of every node group of T as planes of 8 (drd::Scene::gbox layout: 48 floats per group,
+// lo x / y / z then hi x / y / z, 8 children each), in two versions.
+static void group_planes(const drb::FlatOctree &T, std::vector<float> &gbox, std::vector<float> &gbox_ref) {
+    //  * gbox_ref: the reference's boxes, except that an empty leaf's box is a point at kFar on every
+    //    axis.  reduceNode has nothing to shrink an empty leaf to, so it keeps nearly its whole octant
+    //    box, and on a displaced sphere the empty leaves hold about 2/3 of the leaves' surface area.
+    //    An empty leaf yields no hit and adds to neither count of a cast (no triangles; the box-test
+    //    count corrections follow the children taken on the way to a hit), and a ray reaches the far
+    //    point only if its three slab distances to it coincide, when it just enters the empty leaf.
+    //    The counting traversals of reference-padding scenes read these, so their counts are the
+    //    reference's.
+    //  * gbox: the boxes refitted to the non-empty leaves below (a leaf's own box; an inner node's
+    //    union of its non-empty children's refitted boxes, empty subtrees at kFar).  The reference's
+    //    inner boxes are unions that include the empty leaves' octant boxes; the refitted ones have
+    //    about a third of their surface area.  A ray that misses a refitted box (the slab test's
+    //    rounding is monotone in the box) misses every non-empty leaf box below it, so no leaf below
+    //    could accept a hit: the visited leaves that matter, their order and every result are the
+    //    reference's.  Every other traversal reads these.
+    constexpr float kFar = 1e30f;
+    const int64_t NN = T.node_count;
+    const size_t groups = (size_t)(NN / 8);
+    std::vector<float> fit_lo(3 * (size_t)NN), fit_hi(3 * (size_t)NN);
+    std::vector<uint8_t> fit_live((size_t)NN, 0);
+    auto refit_children = [&](int64_t first, float *lo, float *hi) {
+        bool any = false;
+        for (int k = 0; k < 3; k++) { lo[k] = kFar; hi[k] = -kFar; }
+        for (int c = 0; c < 8; c++) {
+            const int64_t j = first + c;
+            if (!fit_live[j]) continue;
+            any = true;
+            for (int k = 0; k < 3; k++) {
+                lo[k] = std::fmin(lo[k], fit_lo[3 * j + k]);
+                hi[k] = std::fmax(hi[k], fit_hi[3 * j + k]);
+            }
+        }
+        return any;
+    };
+    // node order is breadth-first (children after their parent), so reverse order is bottom-up
+    for (int64_t i = NN - 1; i >= 0; i--) {
+        if (T.node_child[i] < 0) {
+            fit_live[i] = T.node_leaf_count[i] > 0;
+            for (int k = 0; k < 3; k++) { fit_lo[3 * i + k] = T.node_lo[3 * i + k]; fit_hi[3 * i + k] = T.node_hi[3 * i + k]; }
+        } else {
+            fit_live[i] = refit_children(T.node_child[i], &fit_lo[3 * i], &fit_hi[3 * i]) ? 1 : 0;
+        }
+    }
+    gbox.assign(48 * groups, 0.0f);
+    gbox_ref.assign(48 * groups, 0.0f);
+    for (size_t g = 0; g < groups; g++)
+        for (int c = 0; c < 8; c++) {
+            const int64_t j = 8 * (int64_t)g + c;
+            const bool empty_leaf = T.node_child[j] < 0 && T.node_leaf_count[j] == 0;
+            float *p = &gbox_ref[48 * g];
+            for (int k = 0; k < 3; k++) {
+                p[8 * k + c] = empty_leaf ? kFar : T.node_lo[3 * j + k];
+                p[24 + 8 * k + c] = empty_leaf ? kFar : T.node_hi[3 * j + k];
+            }
+            float *q = &gbox[48 * g];
+            for (int k = 0; k < 3; k++) {
+                q[8 * k + c] = fit_live[j] ? fit_lo[3 * j + k] : kFar;
+                q[24 + 8 * k + c] = fit_live[j] ? fit_hi[3 * j + k] : kFar;
+            }
+        }
+}
+
 dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat_id, int32_t n, const dr_material *mats,
                           int32_t n_mats, const dr_light *lights, int32_t n_lights, const dr_build_params *bp, dr_scene **out) try {
     if (out == nullptr) return fail(DR_E_ARG, "dr_scene_create: out is NULL");
@@ -410,65 +475,8 @@ dr_status dr_scene_create(const float *xyz, const float *nrm, const int32_t *mat
         if (l.type == DR_LIGHT_SPOTLIGHT) spotlight_state(l, d);
     }
 
-    // Child boxes of every node group as planes of 8 (see drd::Scene::gbox), in two versions.
-    //  * gbox_ref: the reference's boxes, except that an empty leaf's box is a point at kFar on every
-    //    axis.  reduceNode has nothing to shrink an empty leaf to, so it keeps nearly its whole octant
-    //    box, and on a displaced sphere the empty leaves hold about 2/3 of the leaves' surface area.
-    //    An empty leaf yields no hit and adds to neither count of a cast (no triangles; the box-test
-    //    count corrections follow the children taken on the way to a hit), and a ray reaches the far
-    //    point only if its three slab distances to it coincide, when it just enters the empty leaf.
-    //    The counting traversals of reference-padding scenes read these, so their counts are the
-    //    reference's.
-    //  * gbox: the boxes refitted to the non-empty leaves below (a leaf's own box; an inner node's
-    //    union of its non-empty children's refitted boxes, empty subtrees at kFar).  The reference's
-    //    inner boxes are unions that include the empty leaves' octant boxes; the refitted ones have
-    //    about a third of their surface area.  A ray that misses a refitted box (the slab test's
-    //    rounding is monotone in the box) misses every non-empty leaf box below it, so no leaf below
-    //    could accept a hit: the visited leaves that matter, their order and every result are the
-    //    reference's.  Every other traversal reads these.
-    constexpr float kFar = 1e30f;
-    const int64_t NN = T.node_count;
-    std::vector<float> fit_lo(3 * (size_t)NN), fit_hi(3 * (size_t)NN);
-    std::vector<uint8_t> fit_live((size_t)NN, 0);
-    auto refit_children = [&](int64_t first, float *lo, float *hi) {
-        bool any = false;
-        for (int k = 0; k < 3; k++) { lo[k] = kFar; hi[k] = -kFar; }
-        for (int c = 0; c < 8; c++) {
-            const int64_t j = first + c;
-            if (!fit_live[j]) continue;
-            any = true;
-            for (int k = 0; k < 3; k++) {
-                lo[k] = std::fmin(lo[k], fit_lo[3 * j + k]);
-                hi[k] = std::fmax(hi[k], fit_hi[3 * j + k]);
-            }
-        }
-        return any;
-    };
-    // node order is breadth-first (children after their parent), so reverse order is bottom-up
-    for (int64_t i = NN - 1; i >= 0; i--) {
-        if (T.node_child[i] < 0) {
-            fit_live[i] = T.node_leaf_count[i] > 0;
-            for (int k = 0; k < 3; k++) { fit_lo[3 * i + k] = T.node_lo[3 * i + k]; fit_hi[3 * i + k] = T.node_hi[3 * i + k]; }
-        } else {
-            fit_live[i] = refit_children(T.node_child[i], &fit_lo[3 * i], &fit_hi[3 * i]) ? 1 : 0;
-        }
-    }
-    std::vector<float> gbox(48 * (nodes.size() / 16)), gbox_ref(48 * (nodes.size() / 16));
-    for (size_t g = 0; g < nodes.size() / 16; g++)
-        for (int c = 0; c < 8; c++) {
-            const int64_t j = 8 * (int64_t)g + c;
-            const bool empty_leaf = T.node_child[j] < 0 && T.node_leaf_count[j] == 0;
-            float *p = &gbox_ref[48 * g];
-            for (int k = 0; k < 3; k++) {
-                p[8 * k + c] = empty_leaf ? kFar : T.node_lo[3 * j + k];
-                p[24 + 8 * k + c] = empty_leaf ? kFar : T.node_hi[3 * j + k];
-            }
-            float *q = &gbox[48 * g];
-            for (int k = 0; k < 3; k++) {
-                q[8 * k + c] = fit_live[j] ? fit_lo[3 * j + k] : kFar;
-                q[24 + 8 * k + c] = fit_live[j] ? fit_hi[3 * j + k] : kFar;
-            }
-        }
+    std::vector<float> gbox, gbox_ref;
+    group_planes(T, gbox, gbox_ref);
     float4 *d_nodes = nullptr, *d_gbox = nullptr, *d_gbox_ref = nullptr, *d_leaf = nullptr, *d_tris = nullptr, *d_nrms = nullptr;
     int *d_mat = nullptr;
     drd::Material *d_mats = nullptr;
@@ -679,6 +687,17 @@ dr_status dr_octree_export(const dr_octree *t, float *node_box, int32_t *node_ch
     return DR_OK;
 } catch (...) {
     return dr_internal_exception("dr_octree_export");
+}
+
+dr_status dr_octree_group_planes(const dr_octree *t, float *gbox, float *gbox_ref) try {
+    if (!t) return fail(DR_E_ARG, "dr_octree_group_planes: tree is NULL");
+    std::vector<float> g, r;
+    group_planes(t->tree, g, r);
+    if (gbox && !g.empty()) std::memcpy(gbox, g.data(), sizeof(float) * g.size());
+    if (gbox_ref && !r.empty()) std::memcpy(gbox_ref, r.data(), sizeof(float) * r.size());
+    return DR_OK;
+} catch (...) {
+    return dr_internal_exception("dr_octree_group_planes");
 }
 
 void dr_octree_destroy(dr_octree *t) { delete t; }

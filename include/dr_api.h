@@ -248,6 +248,14 @@ typedef struct dr_octree dr_octree;
 dr_status dr_octree_create_host(const float *xyz, int32_t n, const dr_build_params *bp, dr_octree **out);
 dr_status dr_octree_stats(const dr_octree *tree, int64_t *nodes, int64_t *leaves, int64_t *refs, int32_t *depth);
 dr_status dr_octree_export(const dr_octree *tree, float *node_box, int32_t *node_child, int32_t *node_leaf, int32_t *leaf_tri);
+/* The group-test boxes the traversal reads for this tree (no reference counterpart; they replace the
+ * child-box reads of Octree::cast, Octree.impl.cuh:174-212, without changing any hit or count):
+ * float[(nodes - 1) / 8][48] each; group g (the 8 children of an inner node: export nodes 8g + 1 ..
+ * 8g + 8) holds planes lo x, lo y, lo z, hi x, hi y, hi z of its 8 children.  gbox: boxes refitted to the non-empty
+ * leaves below each child (a leaf's own box; an inner child's union of its non-empty children's
+ * refitted boxes); gbox_ref: the reference's boxes.  In both an empty leaf (and in gbox a subtree
+ * without triangles) is the point (1e30, 1e30, 1e30).  Either pointer may be NULL. */
+dr_status dr_octree_group_planes(const dr_octree *tree, float *gbox, float *gbox_ref);
 void dr_octree_destroy(dr_octree *tree);
 
 /* ---- scene ---------------------------------------------------------------------------------
