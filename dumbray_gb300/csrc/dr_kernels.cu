@@ -354,6 +354,11 @@ __global__ void __launch_bounds__(256) k_camera(WaveArgs A) {
     }
 }
 
+// Traversal steps a lane may take between two cooperative leaf rounds on physical-tree scenes
+// (small leaves; the reference's tree keeps 1).  Path trace, Mpaths/s: 1: 654, 2: 789, 3: 795,
+// 4: 810, 6: 723, 8: 648.
+constexpr int kPhysStepsPerRound = 4;
+
 template <bool MULTI>
 struct TraceSource {
     static constexpr float kOccludeBelow = 0.0f;
@@ -403,7 +408,7 @@ __global__ void __launch_bounds__(TT, TB) k_trace(WaveArgs A, int b) {
     uint32_t stack[kStack];
     __shared__ WarpLeafSlots slots[TT / 32];
     TraceSource<MULTI> src{&A, A.q[b & 1], A.hits, &C->fetch_trace[b], n, chunk_for(n), 0, 0, 0};
-    trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5], A.inl.S.front_only ? 2 : 1);
+    trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5], A.inl.S.front_only ? kPhysStepsPerRound : 1);
     if (COUNT) count_add64(A.counters, src.rays, src.nb, src.nt);
 }
 
@@ -980,7 +985,7 @@ __global__ void __launch_bounds__(TT, TB) k_shadow_phys(WaveArgs A, int b) {
     uint32_t stack[kStack];
     __shared__ WarpLeafSlots slots[TT / 32];
     ShadowPhysSource<MULTI, ADJ> src{&A, A.sq, A.accum, &C->fetch_shadow[b], n, chunk_for(n), 0, 0, 0};
-    trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5], A.inl.S.front_only ? 2 : 1);
+    trace_persistent<COUNT, MULTI>(A.inl.S, src, stack, slots[threadIdx.x >> 5], A.inl.S.front_only ? kPhysStepsPerRound : 1);
     if (COUNT) count_add64(A.counters + 3, src.rays, src.nb, src.nt);
 }
 
