@@ -48,10 +48,13 @@ struct Light {
 
 struct Scene {
     const float4 *nodes;
-    // The same child boxes per node group as planes of 8 floats (lo.x, lo.y, lo.z, hi.x, hi.y, hi.z;
-    // 12 float4 = 192 B per group), read by the group tests: 12 vector loads instead of 16.
-    const float4 *gbox;         // child boxes of each node group as planes (refitted to non-empty leaves)
-    const float4 *gbox_ref;     // the same with the reference's boxes (counting on reference-padding scenes)
+    // Child boxes per node group as planes of 8 floats (lo.x, lo.y, lo.z, hi.x, hi.y, hi.z; 12 float4
+    // = 192 B per group), read by the group tests: 12 vector loads instead of 16.  gbox: refitted to
+    // the non-empty leaves below each child (every traversal but the next); gbox_ref: the reference's
+    // boxes (counting traversals of reference-padding scenes).  Empty leaves sit at a far point in
+    // both (dr_octree_group_planes in the C ABI gives both for a host-built tree).
+    const float4 *gbox;
+    const float4 *gbox_ref;
     const float4 *leaf_tris;
     const float4 *tris;
     const float4 *nrms;

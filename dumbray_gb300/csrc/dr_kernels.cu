@@ -5,17 +5,20 @@
 //   k_trace           ray queue -> hit records                       (Octree::cast)
 //   k_shade_ref       DumbRenderer layer step (DumbRenderer.cu:249-443) as one forward path step:
 //                     indirect request, light photons -> shadow queue, next ray -> next queue
-//   k_shadow_ref      light -> point visibility with the reference's transparency re-casts
+//   k_shadow_ref      light -> point visibility, first cast of every photon (DumbRenderer.cu:361-428)
+//   k_photon_chain    photons stopped by a blocker: the reference's transparency re-casts
 //   k_shade_phys      physical path step (emission + MIS, NEE -> shadow queue, BSDF sample);
 //                     in the adjoint pass it also scatters gradients of emission hits
-//   k_shadow_phys     point -> light visibility; in the adjoint pass it scatters NEE gradients
+//   k_shadow_phys     point -> light visibility; in the adjoint pass it marks the visible records
+//   k_adj_shadow      adjoint pass: gradients of the visible NEE contributions
 //   k_resolve         accumulators -> BlockBasedFrameBuffer<8,16> set / blend (BlockBasedFrameBuffer.impl.cuh:149-156)
 //
 // Wavefront design: queues are structure-of-arrays of float4/int4 records in HBM; work is pulled by
 // persistent warps (shading: blocks) through one atomic per warp (block); outputs are compacted with
-// ballots and one atomic per warp (block; extension rays grouped by direction octant).  Queue counts live in a device control block, so a whole wave is a fixed launch
-// sequence with no host synchronisation (and can be captured in a CUDA graph).  Every path record
-// carries the index of its render job, so the paths of many scenes can share a wave (batches).
+// ballots and one atomic per warp (block; rays grouped by direction octant).  Queue counts live in
+// a device control block, so a whole wave is a fixed launch sequence with no host synchronisation
+// (and can be captured in a CUDA graph).  Every path record carries the index of its render job, so
+// the paths of many scenes can share a wave (batches).
 #include <algorithm>
 #include <atomic>
 #include "dr_kernels.h"
