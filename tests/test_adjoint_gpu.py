@@ -238,3 +238,43 @@ def test_adjoint_rejects_reference_mode(cuda):
     g = torch.zeros((len(room), 3), device=cuda)
     with pytest.raises(dr.DumbRayError):
         dr.Renderer(1 << 12).render_adjoint(sc, cam, fb, 0, 2, p, g, g)
+
+
+def test_adjoint_over_concurrent_lanes_equals_one_lane(cuda):
+    """The adjoint pass runs its waves on the renderer's concurrent lanes, each with its own prefix
+    buffer.  The C5 workload's full frame (4.2M paths: four 1Mi-path waves) with 4 lanes gives the
+    gradients of one lane, up to the order of the float atomic additions."""
+    S = scenes.differentiable_scene(7)
+    tris, n = S["tris"], len(S["tris"])
+    sc = dr.Scene(tris, mat_id=S["mat_id"], materials=[dr.lambert()], box_epsilon=dr.PHYSICAL_TREE)
+    sc.set_triangle_params(S["albedo"], S["emission"], S["roughness"])
+    cam = dr.camera(dr.LENS_PINHOLE, position=(0.0, 0.0, -0.99), angle=60.0)
+    p = dr.render_params(512, 512, dr.MODE_PHYSICAL, samples=(4, 4), max_bounces=5, seed=7)
+    nb = dr.block_count(512, 512)
+    dl = torch.zeros((nb * 128, 4), dtype=torch.float32, device=cuda)
+    dl[:, :3] = 1.0
+    grads = {}
+    for run, lanes in (("one", 1), ("one_again", 1), ("four", 4)):
+        rend = dr.Renderer(1 << 20)
+        rend.set_lanes(lanes)
+        ga = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
+        ge = torch.zeros((n, 3), dtype=torch.float32, device=cuda)
+        rend.render_adjoint(sc, cam, dl, 0, nb, p, ga, ge)
+        torch.cuda.synchronize()
+        grads[run] = (ga.cpu().numpy().astype(np.float64), ge.cpu().numpy().astype(np.float64))
+        rend.close()
+    # The gradients are float32 atomic sums of millions of small terms: the largest components (the
+    # walls' albedo, ~10) take terms far below their ulp's worth of precision, so another order of
+    # the additions moves them by parts in 1e4 (two one-lane runs, whose order stays the same in
+    # practice, agree closely; four lanes interleave the waves: measured 1.7e-3 relative L2).  A lane
+    # that lost or doubled its wave would move the gradient by ~25%.
+    def rel_l2(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    for k in range(2):
+        one, again, four = grads["one"][k], grads["one_again"][k], grads["four"][k]
+        assert np.abs(one).sum() > 0
+        assert rel_l2(again, one) <= 5e-3, rel_l2(again, one)
+        assert rel_l2(four, one) <= 5e-3, rel_l2(four, one)
+        big = np.abs(one) > 1e-3 * np.abs(one).max()
+        worst = float((np.abs(four - one)[big] / np.abs(one)[big]).max())
+        assert worst <= 2e-2, worst

@@ -210,3 +210,41 @@ def test_render_argument_errors(cuda):
         r.render_blocks(sc, cam, fb, 0, 2, dr.render_params(16, 16, mode=dr.MODE_PHYSICAL))  # reference lens in physical mode
     with pytest.raises(dr.DumbRayError):
         r.render_blocks(sc, cam, fb, 0, 2, dr.render_params(16, 16, max_bounces=65))
+
+
+def test_reference_photon_chains_past_a_full_carry_region(cuda):
+    """Photons stopped by a blocker wait for their transparency chains in a carry region of 1/16 of
+    the renderer's photon records (at least 1,024); beyond that they take the per-bounce fallback
+    (blocked list, chain launch right after the bounce).  A plane under the light blocks the photons
+    of nearly every point, and a renderer of 1,024-path waves overflows the carry region every wave:
+    the frame equals the oracle's per pixel and a large-wave render's (no overflow), and both cast
+    the same photons."""
+    tris, mat, mats, lights, cam = _ref_scene("diffuse")
+    veil = scenes.quad((0.0, 0.55, 0.0), (1.9, 1.9), (0.0, -1.0, 0.0))
+    tris = np.concatenate([tris, veil])
+    mat = np.concatenate([mat, np.zeros(len(veil), np.int32)])
+    sc = dr.Scene(tris, mat_id=mat, materials=mats, lights=lights)
+    osc = O.OracleScene(tris, mat_id=mat, materials=mats, lights=lights)
+    W, H = 32, 24
+    p = dr.render_params(W, H, dr.MODE_REFERENCE, samples=(2, 2), max_bounces=4, seed=21)
+    nb = dr.block_count(W, H)
+    out = {}
+    for wave in (1024, 1 << 16):
+        fb = dr.new_frame_buffer(W, H, cuda)
+        r = dr.Renderer(wave)
+        r.set_counting(True)
+        r.render_blocks(sc, cam, fb, 0, nb, p)
+        torch.cuda.synchronize()
+        casts = r.counters()["shadow_casts"]
+        _, photons = r.wave_counts(p.max_bounces + 1)
+        r.close()
+        out[wave] = (dr.blockmajor_to_image(fb, W, H), casts, sum(photons))
+    small, big = out[1024], out[1 << 16]
+    # every photon toward a point under the veil is blocked by it (whether it goes on is the veil's
+    # shading, decided in the chain launches), so one small wave blocks far more photons than its
+    # carry region holds
+    assert small[2] > 1.5 * 1024, small[2]
+    assert big[1] >= big[2] and small[1] == big[1], (small[1], big[1], big[2])   # the same casts either way
+    ora = dr.blockmajor_to_image(osc.render_blocks(cam, p), W, H)
+    _compare(small[0], ora)
+    np.testing.assert_allclose(small[0][..., :3], big[0][..., :3], rtol=1e-4, atol=1e-6)
