@@ -358,9 +358,10 @@ __global__ void __launch_bounds__(256) k_camera(WaveArgs A) {
 }
 
 // Traversal steps a lane may take between two cooperative leaf rounds on physical-tree scenes
-// (small leaves; the reference's tree keeps 1).  Path trace, Mpaths/s: 1: 654, 2: 789, 3: 795,
-// 4: 810, 6: 723, 8: 648.
-constexpr int kPhysStepsPerRound = 4;
+// (small leaves; the reference's tree keeps 1).  Path trace of the open 1.31M-triangle scene at leaf
+// split 4, Mpaths/s: 1: 654, 2: 789, 3: 795, 4: 810, 6: 723, 8: 648; but 4 slowed the closed scenes
+// (box rooms: adjoint forward 43.5 -> 51.5 ms, 64-scene batch 405 -> 378 Mpaths/s), so it stays 2.
+constexpr int kPhysStepsPerRound = 2;
 
 template <bool MULTI>
 struct TraceSource {

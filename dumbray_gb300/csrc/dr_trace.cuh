@@ -101,7 +101,7 @@ struct WarpLeafSlots {
 template <bool COUNT, bool MULTI, class Source>
 // steps_per_round: traversal steps a lane may take between two cooperative leaf rounds while it
 // stays in inner nodes; more means fewer per-round ballots and prefix sums, but lanes that reached a
-// leaf wait longer (measured: 4 pays on physical-tree scenes, whose leaves are small; 1 elsewhere).
+// leaf wait longer (measured: 2 pays on physical-tree scenes, whose leaves are small; 1 elsewhere).
 __device__ __forceinline__ void trace_persistent(const Scene &S, Source &src, uint32_t *stack, WarpLeafSlots &ws,
                                                  int steps_per_round = 1) {
     const unsigned lane = threadIdx.x & 31u;
