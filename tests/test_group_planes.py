@@ -123,3 +123,26 @@ def test_refitted_boxes_keep_every_leaf_a_ray_reaches(padding):
             checked += int(ok.size)
             a = parent[a]
     assert checked > 1000
+
+
+def test_group_planes_of_degenerate_trees():
+    """A tree whose root is a leaf has no groups; a split tree whose triangles crowd into one corner
+    keeps its other children as empty leaves at the far point in both plane sets."""
+    one = scenes.quad((0.0, 0.0, 0.0), (1.0, 1.0), (0.0, 1.0, 0.0))
+    box, child, leaf, g, r = dr.octree_group_planes_host(one)
+    assert len(child) == 1 and g.shape[0] == 0 and r.shape[0] == 0
+    # 400 small triangles near (0.75, 0.75, 0.75) and one at (-1, -1, -1): most octants stay empty
+    rng = np.random.default_rng(5)
+    c = rng.uniform(0.6, 0.9, size=(400, 1, 3)).astype(np.float32)
+    small = c + rng.uniform(-0.01, 0.01, size=(400, 3, 3)).astype(np.float32)
+    tris = np.concatenate([small, np.array([[[-1, -1, -1], [-0.99, -1, -1], [-1, -0.99, -1]]], np.float32)])
+    box, child, leaf, g, r = dr.octree_group_planes_host(tris, split_threshold=4, box_epsilon=-1.0)
+    gb, rb = _planes_to_boxes(g), _planes_to_boxes(r)
+    nodes = np.arange(1, len(child))
+    empty = (child[nodes] < 0) & (leaf[nodes, 1] == 0)
+    assert empty.any()
+    assert np.all(gb[empty] == FAR) and np.all(rb[empty] == FAR)
+    live, lo, hi = _refit(box, child, leaf)
+    assert live[0]
+    lv = live[nodes]
+    assert np.array_equal(gb[lv, :3], lo[nodes][lv]) and np.array_equal(gb[lv, 3:], hi[nodes][lv])
