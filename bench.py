@@ -73,7 +73,9 @@ def parse():
     ap.add_argument("--twin-spp", type=int, default=64, help="reference-mode twin samples per pixel (a square)")
     ap.add_argument("--twin-tree", default="reference", choices=["reference", "physical"],
                     help="octree padding of the reference-mode twin scene")
-    ap.add_argument("--lanes", type=int, default=0, help="concurrent wave pipelines per renderer (0 = library default)")
+    ap.add_argument("--lanes", type=int, default=8,
+                    help="concurrent wave pipelines per renderer (0 = the library default, 4; path trace at 16Mi-path "
+                         "waves: 4 lanes 788.5, 6 791.6, 8 798.3 Mpaths/s)")
     ap.add_argument("--split", type=int, default=4,
                     help="octree leaf split threshold of the path-trace scene (4: with 3 the best of 2-24 on this "
                          "workload with the physical-mode padding and the refitted group-test planes; the "
